@@ -1,0 +1,352 @@
+"""ctypes binding of include/bd_capi.h (libbdgb300.so).
+
+``Fiber`` holds one fiber's model (topology, parameters, per-bead constants)
+and initial state as numpy arrays in the reference's layouts; it is built
+from the reference input files through the library's own readers
+(``Fiber.load``) or directly from arrays (``Fiber.from_arrays``).
+``Context`` owns the device state of one fiber and runs steps.  There is no
+CPU fallback: a missing library raises at import of the first call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libbdgb300.so")
+
+BD_OK, BD_ERR_ARG, BD_ERR_IO, BD_ERR_CUDA, BD_ERR_NOMEM, BD_ERR_NONFINITE, BD_ERR_NOT_SPD, BD_ERR_STATE = range(8)
+PREC_FP64, PREC_MIXED = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class BDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class bd_model(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("n", "n_c", "Nq", "n_t", "n_tail", "n_lh_n", "n_lh_g", "n_lh_c", "n_LH")] + [
+        (k, C.c_double)
+        for k in ("h", "g", "s", "debyell", "debye", "q_l", "k_e", "k_ex", "k_h1", "sigma_DNA_DNA", "sigma_DNA_Core",
+                  "sigma_Core_Core", "sigma_Tail_Tail", "sigma_Tail_Linker", "sigma_Tail_Core", "a1", "a2",
+                  "time_step", "del_", "s2dt")
+    ] + [
+        ("type", _ip), ("rad", _dp), ("phi_o", _dp), ("r_var", _dp), ("core_pos", _dp), ("core_q", _dp),
+        ("tail_pos", _dp), ("tail_fix", _ip), ("nc_t_flag", _ip), ("h_t", _dp), ("g_t", _dp), ("lo_t", _dp),
+        ("beta_o_t", _dp), ("t_q", _dp), ("t_rad", _dp), ("t_grp", _ip), ("t_fix", _ip), ("LH_g_pos", _dp),
+        ("LH_conn", _ip), ("nc_lh_flag", _ip), ("LH_q", _dp), ("LH_vdw_hh", _dp), ("LH_vdw_hc", _dp),
+        ("LH_vdw_hl", _dp), ("LH_vdw_ht", _dp), ("LH_kstr", _dp), ("LH_kben", _dp), ("LH_streq", _dp),
+        ("LH_betaeq", _dp), ("lh_rad", _dp),
+    ]
+
+
+class bd_state(C.Structure):
+    _fields_ = [("r", _dp), ("a", _dp), ("b", _dp), ("c", _dp), ("r_t", _dp), ("r_lh", _dp), ("refresh_frames", C.c_int),
+                ("alpha", _dp), ("beta", _dp), ("gamma", _dp), ("length", _dp), ("a_dna", _dp), ("b_dna", _dp),
+                ("c_dna", _dp), ("alpha_p", _dp), ("beta_p", _dp), ("gamma_p", _dp)]
+
+
+class bd_options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("frequency_RP", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
+                ("stream", C.c_void_p)]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads libbdgb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} is missing: run brownian_dynamics_cuda_gb300.build.build_lib() first")
+    L = C.CDLL(p)
+    L.bd_last_error.restype = C.c_char_p
+    L.bd_version.restype = C.c_char_p
+    L.bd_system_load.argtypes = [C.c_char_p] * 6 + [C.POINTER(C.c_void_p)]
+    L.bd_system_model.argtypes = [C.c_void_p, C.POINTER(bd_model)]
+    L.bd_system_state.argtypes = [C.c_void_p, C.POINTER(bd_state)]
+    L.bd_system_setup.argtypes = [C.c_void_p, _dp]
+    L.bd_system_free.argtypes = [C.c_void_p]
+    L.bd_system_free.restype = None
+    L.bd_write_xyz.argtypes = [C.POINTER(bd_model)] + [_dp] * 6 + [C.c_char_p]
+    L.bd_noise_create.argtypes = [C.c_ulong, C.POINTER(C.c_void_p)]
+    L.bd_noise_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]
+    L.bd_noise_u32.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]
+    L.bd_noise_free.argtypes = [C.c_void_p]
+    L.bd_noise_free.restype = None
+    L.bd_create.argtypes = [C.POINTER(bd_model), C.POINTER(bd_state), C.POINTER(bd_options), C.POINTER(C.c_void_p)]
+    L.bd_destroy.argtypes = [C.c_void_p]
+    L.bd_sizes.argtypes = [C.c_void_p, _ip]
+    L.bd_step.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    L.bd_step_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bd_step_reference.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp] + [_dp] * 6
+    L.bd_forces.argtypes = [C.c_void_p] + [_dp] * 5
+    L.bd_diffusion_tensor.argtypes = [C.c_void_p, _dp]
+    L.bd_cholesky.argtypes = [C.c_void_p, _dp]
+    L.bd_noise_displacement.argtypes = [C.c_void_p, _dp, _dp]
+    L.bd_get_state.argtypes = [C.c_void_p, C.c_char_p, _dp, _ip]
+    L.bd_set_state.argtypes = [C.c_void_p, C.c_char_p, _dp]
+    L.bd_dev_rpy.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_int]
+    L.bd_dev_potrf.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.bd_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    L.bd_launch_count.argtypes = [C.c_void_p, _ip]
+    L.bd_negative_pivots.argtypes = [C.c_void_p, _ip]
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != BD_OK:
+        raise BDError(rc, load_library().bd_last_error().decode())
+
+
+def _pd(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _pi(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+SCALARS = ("h", "g", "s", "debyell", "debye", "q_l", "k_e", "k_ex", "k_h1", "sigma_DNA_DNA", "sigma_DNA_Core",
+           "sigma_Core_Core", "sigma_Tail_Tail", "sigma_Tail_Linker", "sigma_Tail_Core", "a1", "a2", "time_step",
+           "del_", "s2dt")
+SIZES = ("n", "n_c", "Nq", "n_t", "n_tail", "n_lh_n", "n_lh_g", "n_lh_c", "n_LH")
+INT_ARRAYS = ("type", "tail_fix", "nc_t_flag", "t_grp", "t_fix", "LH_conn", "nc_lh_flag")
+DBL_ARRAYS = ("rad", "phi_o", "r_var", "core_pos", "core_q", "tail_pos", "h_t", "g_t", "lo_t", "beta_o_t", "t_q",
+              "t_rad", "LH_g_pos", "LH_q", "LH_vdw_hh", "LH_vdw_hc", "LH_vdw_hl", "LH_vdw_ht", "LH_kstr", "LH_kben",
+              "LH_streq", "LH_betaeq", "lh_rad")
+STATE = ("r", "a", "b", "c", "r_t", "r_lh")
+
+
+def _array_len(name: str, sz: dict) -> int:
+    n, nc, Nq, nt, ntail, nL = sz["n"], sz["n_c"], sz["Nq"], sz["n_t"], sz["n_tail"], sz["n_LH"]
+    npar = sz["n_lh_n"] + sz["n_lh_g"] + sz["n_lh_c"]
+    return {
+        "type": n, "rad": n, "phi_o": n, "r_var": 3 * n, "core_pos": 3 * Nq, "core_q": Nq, "tail_pos": 3 * nt,
+        "tail_fix": nt, "nc_t_flag": nc, "h_t": ntail, "g_t": ntail, "lo_t": ntail, "beta_o_t": ntail, "t_q": ntail,
+        "t_rad": ntail, "t_grp": ntail, "t_fix": ntail, "LH_g_pos": 3 * sz["n_lh_g"], "LH_conn": npar,
+        "nc_lh_flag": nc, "LH_q": npar, "LH_vdw_hh": npar, "LH_vdw_hc": npar, "LH_vdw_hl": npar, "LH_vdw_ht": npar,
+        "LH_kstr": npar, "LH_kben": npar, "LH_streq": npar, "LH_betaeq": npar, "lh_rad": nL,
+        "r": 3 * n, "a": 3 * n, "b": 3 * n, "c": 3 * n, "r_t": 3 * ntail, "r_lh": 3 * nL,
+    }[name]
+
+
+@dataclass
+class Fiber:
+    """One fiber: sizes, scalar parameters, per-bead arrays and state (numpy, reference layouts)."""
+    sizes: dict
+    scalars: dict
+    arrays: dict
+    state: dict
+    setup: np.ndarray = field(default_factory=lambda: np.zeros(15))
+
+    @property
+    def n_D(self) -> int:
+        return self.sizes["n"] + self.sizes["n_tail"] + self.sizes["n_LH"]
+
+    @property
+    def m(self) -> int:
+        return 3 * self.n_D
+
+    @staticmethod
+    def load(directory: str, core_file: str, tail_file: str, lh_file: str, data_file: str = "data_mod",
+             lh_flags_file: str = "LH.in") -> "Fiber":
+        """Reads the reference input files with the library's readers (readfile.cpp formats)."""
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.bd_system_load(directory.encode(), data_file.encode(), core_file.encode(), tail_file.encode(),
+                                lh_file.encode(), lh_flags_file.encode(), C.byref(h)))
+        try:
+            m = bd_model()
+            _check(L.bd_system_model(h, C.byref(m)))
+            s = bd_state()
+            _check(L.bd_system_state(h, C.byref(s)))
+            setup = np.zeros(15)
+            _check(L.bd_system_setup(h, _pd(setup)))
+            sizes = {k: int(getattr(m, k)) for k in SIZES}
+            scalars = {k: float(getattr(m, k)) for k in SCALARS}
+            arrays = {}
+            for k in INT_ARRAYS:
+                cnt = _array_len(k, sizes)
+                p = getattr(m, k)
+                arrays[k] = np.ctypeslib.as_array(p, shape=(cnt,)).astype(np.int32).copy() if cnt else np.zeros(0, np.int32)
+            for k in DBL_ARRAYS:
+                cnt = _array_len(k, sizes)
+                p = getattr(m, k)
+                arrays[k] = np.ctypeslib.as_array(p, shape=(cnt,)).copy() if cnt else np.zeros(0)
+            state = {}
+            for k in STATE:
+                cnt = _array_len(k, sizes)
+                p = getattr(s, k)
+                state[k] = np.ctypeslib.as_array(p, shape=(cnt,)).copy() if cnt else np.zeros(0)
+        finally:
+            L.bd_system_free(h)
+        return Fiber(sizes, scalars, arrays, state, setup)
+
+    @staticmethod
+    def from_arrays(d: dict) -> "Fiber":
+        """Inverse of ``to_arrays`` (e.g. a golden .npz)."""
+        sizes = {k: int(d["size_" + k]) for k in SIZES}
+        scalars = {k: float(d["scalar_" + k]) for k in SCALARS}
+        arrays = {k: np.ascontiguousarray(d["arr_" + k], dtype=np.int32 if k in INT_ARRAYS else np.float64)
+                  for k in INT_ARRAYS + DBL_ARRAYS}
+        state = {k: np.ascontiguousarray(d["state_" + k], dtype=np.float64) for k in STATE}
+        setup = np.asarray(d["setup"], dtype=np.float64) if "setup" in d else np.zeros(15)
+        return Fiber(sizes, scalars, arrays, state, setup)
+
+    def to_arrays(self) -> dict:
+        out = {"size_" + k: v for k, v in self.sizes.items()}
+        out.update({"scalar_" + k: v for k, v in self.scalars.items()})
+        out.update({"arr_" + k: v for k, v in self.arrays.items()})
+        out.update({"state_" + k: v for k, v in self.state.items()})
+        out["setup"] = self.setup
+        return out
+
+    def model_struct(self) -> bd_model:
+        m = bd_model()
+        for k, v in self.sizes.items():
+            setattr(m, k, v)
+        for k, v in self.scalars.items():
+            setattr(m, k, v)
+        for k in INT_ARRAYS:
+            setattr(m, k, _pi(self.arrays[k]))
+        for k in DBL_ARRAYS:
+            setattr(m, k, _pd(self.arrays[k]))
+        return m
+
+    def state_struct(self, refresh: bool = True, angles: dict | None = None) -> bd_state:
+        s = bd_state()
+        for k in STATE:
+            setattr(s, k, _pd(self.state[k]))
+        s.refresh_frames = 1 if refresh else 0
+        if angles:
+            for k, v in angles.items():
+                setattr(s, k, _pd(v))
+        return s
+
+    def write_xyz(self, path: str, state: dict | None = None) -> None:
+        st = state or self.state
+        m = self.model_struct()
+        _check(load_library().bd_write_xyz(C.byref(m), *[_pd(st[k]) for k in STATE], path.encode()))
+
+
+class Noise:
+    """Reference-order MT19937 + polar Box-Muller noise (host)."""
+
+    def __init__(self, seed: int):
+        self._L = load_library()
+        self._h = C.c_void_p()
+        _check(self._L.bd_noise_create(seed, C.byref(self._h)))
+
+    def step(self, step: int, r_var: np.ndarray, n_D3: int) -> tuple[np.ndarray, np.ndarray]:
+        rr = np.zeros(r_var.size)
+        p = np.zeros(n_D3)
+        _check(self._L.bd_noise_step(self._h, step, r_var.size, _pd(r_var), n_D3, _pd(rr), _pd(p)))
+        return rr, p
+
+    def u32(self, count: int) -> np.ndarray:
+        out = np.zeros(count, dtype=np.uint32)
+        _check(self._L.bd_noise_u32(self._h, count, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.bd_noise_free(self._h)
+            self._h = None
+
+
+class Context:
+    """Device state of one fiber (bd_create / bd_step / bd_destroy)."""
+
+    def __init__(self, fiber: Fiber, precision: int = PREC_FP64, use_graph: bool = False, frequency_RP: int = 1,
+                 refresh: bool = True, angles: dict | None = None, device: int = 0):
+        self._L = load_library()
+        self.fiber = fiber
+        m = fiber.model_struct()
+        s = fiber.state_struct(refresh, angles)
+        o = bd_options(precision=precision, frequency_RP=frequency_RP, use_graph=int(use_graph), device=device,
+                       stream=None)
+        self._h = C.c_void_p()
+        _check(self._L.bd_create(C.byref(m), C.byref(s), C.byref(o), C.byref(self._h)))
+        sz = (C.c_int * 8)()
+        _check(self._L.bd_sizes(self._h, sz))
+        self.n, self.n_c, self.n_tail, self.n_LH, self.n_D, self.m, self.lda, self.precision = list(sz)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.bd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def step(self, rr: np.ndarray, p: np.ndarray) -> float:
+        e = C.c_double()
+        _check(self._L.bd_step(self._h, _pd(rr), _pd(p), C.byref(e)))
+        return e.value
+
+    def step_device(self, d_rr: int, d_p: int, d_energy: int = 0) -> None:
+        _check(self._L.bd_step_device(self._h, C.c_void_p(d_rr), C.c_void_p(d_p), C.c_void_p(d_energy or None)))
+
+    def forces(self) -> dict:
+        n, nt, nl = self.n, self.n_tail, self.n_LH
+        F, T, tF, lF, E = np.zeros(3 * n), np.zeros(3 * n), np.zeros(3 * nt), np.zeros(3 * nl), np.zeros(1)
+        _check(self._L.bd_forces(self._h, _pd(F), _pd(T), _pd(tF), _pd(lF), _pd(E)))
+        return {"force": F, "torque": T, "t_force": tF, "LH_force": lF, "energy": float(E[0])}
+
+    def diffusion_tensor(self) -> np.ndarray:
+        D = np.zeros((self.m, self.m))
+        _check(self._L.bd_diffusion_tensor(self._h, _pd(D)))
+        return D
+
+    def cholesky(self) -> np.ndarray:
+        Lm = np.zeros((self.m, self.m))
+        _check(self._L.bd_cholesky(self._h, _pd(Lm)))
+        return Lm
+
+    def noise_displacement(self, p: np.ndarray) -> np.ndarray:
+        rd = np.zeros(self.m)
+        _check(self._L.bd_noise_displacement(self._h, _pd(p), _pd(rd)))
+        return rd
+
+    def get(self, name: str) -> np.ndarray:
+        cnt = C.c_int()
+        _check(self._L.bd_get_state(self._h, name.encode(), None, C.byref(cnt)))
+        out = np.zeros(cnt.value)
+        _check(self._L.bd_get_state(self._h, name.encode(), _pd(out), C.byref(cnt)))
+        return out
+
+    def set(self, name: str, value: np.ndarray) -> None:
+        _check(self._L.bd_set_state(self._h, name.encode(), _pd(np.ascontiguousarray(value, dtype=np.float64))))
+
+    def phase_times(self) -> np.ndarray:
+        out = (C.c_float * 9)()
+        _check(self._L.bd_phase_times(self._h, out))
+        return np.array(list(out))
+
+    def launch_count(self) -> int:
+        v = C.c_int()
+        _check(self._L.bd_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def negative_pivots(self) -> int:
+        v = C.c_int()
+        _check(self._L.bd_negative_pivots(self._h, C.byref(v)))
+        return v.value

@@ -1,0 +1,621 @@
+// Device context and step orchestration behind include/bd_capi.h.
+//
+// One context owns every device buffer of one fiber (no file-scope
+// globals, unlike func_cuda.cu:3-104).  All buffers are allocated once at
+// creation; a step allocates nothing (the reference frees and re-allocates
+// D, Chol, the cuSOLVER handle and workspace every step,
+// func_cuda.cu:3436-3534).  The device part of a step is stream-ordered and
+// can be captured once into a CUDA graph and replayed.
+//
+// Step order follows main_cuda (func_cuda.cu:3434-3680):
+//   r_all <- state; D <- RPY(r_all); L <- chol(D) in place; rd <- s2dt L p;
+//   F0 <- forces(X); Y <- move(X, F0); frames(Y); F1 <- forces(Y);
+//   Fa <- (F0 + F1)/2; Y <- move(X, Fa); X <- Y; frames(X).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bd_internal.h"
+
+namespace bdh {
+static thread_local std::string g_err;
+int set_error(int code, const char* msg) {
+  g_err = msg ? msg : "";
+  return code;
+}
+}  // namespace bdh
+
+using bdh::set_error;
+
+extern "C" const char* bd_last_error(void) { return bdh::g_err.c_str(); }
+extern "C" const char* bd_version(void) { return "bd-gb300 0.1 (sm_103a)"; }
+
+#define CK(call)                                                                                 \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) {                                                                     \
+      char b_[256];                                                                              \
+      snprintf(b_, sizeof b_, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return set_error(e_ == cudaErrorMemoryAllocation ? BD_ERR_NOMEM : BD_ERR_CUDA, b_);        \
+    }                                                                                            \
+  } while (0)
+
+namespace {
+
+// Bump allocator over one device allocation (256-byte aligned slices).
+struct Arena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  template <class T>
+  T* take(size_t count) {
+    size_t bytes = ((count * sizeof(T)) + 255) & ~size_t(255);
+    if (bytes == 0) bytes = 256;
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+template <class T>
+size_t slab(size_t count) {
+  size_t b = ((count * sizeof(T)) + 255) & ~size_t(255);
+  return b ? b : 256;
+}
+
+}  // namespace
+
+struct bd_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int precision = BD_PREC_FP64;
+  int freq_rp = 1;
+  int use_graph = 0;
+  long step_count = 0;
+  DevModel M{};
+  DevState X{}, Y{};
+  DevForces F0{}, F1{}, Fa{};
+  DevScratch S{};
+  void* arena_base = nullptr;
+  double* A = nullptr;   // m x lda, column-major; holds D then L
+  int m = 0, lda = 0;
+  double *r_all = nullptr, *rd = nullptr, *p = nullptr, *rr = nullptr, *rd_part = nullptr, *energy = nullptr;
+  int* negpiv = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int last_launches = 0;
+  int host_negpiv = 0;
+  cudaEvent_t ev[10] = {};
+  bool timing = false;
+  // host copies for the drop-in paths
+  std::vector<int> h_type;
+};
+
+namespace {
+
+int validate(const bd_model* m) {
+  if (!m || m->n < 3 || m->n_c < 1 || !m->type || !m->phi_o || !m->rad) return set_error(BD_ERR_ARG, "bd_create: model sizes/arrays");
+  if (m->type[0] != 1 || m->type[m->n - 1] != 0)
+    return set_error(BD_ERR_ARG, "bd_create: chain must start with a core and end with linker DNA");
+  int nc = 0;
+  for (int i = 0; i < m->n; i++) nc += m->type[i] == 1;
+  if (nc != m->n_c) return set_error(BD_ERR_ARG, "bd_create: n_c does not match type[]");
+  if (m->Nq < 1 || !m->core_pos || !m->core_q) return set_error(BD_ERR_ARG, "bd_create: core charges");
+  if (m->n_tail != m->n_c * m->n_t) return set_error(BD_ERR_ARG, "bd_create: n_tail must be n_c * n_t");
+  if (m->n_lh_n != 0) return set_error(BD_ERR_ARG, "bd_create: LH N-terminal beads are not supported");
+  int nlh = m->n_lh_n + m->n_lh_c;
+  int nlhc = 0;
+  for (int i = 0; i < m->n_c; i++) nlhc += m->nc_lh_flag && m->nc_lh_flag[i] == 1;
+  if (m->n_LH != nlhc * nlh) return set_error(BD_ERR_ARG, "bd_create: n_LH does not match nc_lh_flag");
+  return BD_OK;
+}
+
+template <class T>
+int up(T* d, const T* h, size_t cnt, cudaStream_t st) {
+  if (cnt == 0) return BD_OK;
+  if (!h) return set_error(BD_ERR_ARG, "bd_create: missing array");
+  CK(cudaMemcpyAsync(d, h, cnt * sizeof(T), cudaMemcpyHostToDevice, st));
+  return BD_OK;
+}
+
+int record(bd_ctx* c, int k) {
+  if (c->timing) CK(cudaEventRecord(c->ev[k], c->stream));
+  return BD_OK;
+}
+
+// The device part of one step (stream-ordered, capturable).
+int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
+  DevModel& M = c->M;
+  cudaStream_t st = c->stream;
+  int L = 0;
+  record(c, 0);
+  bdk::gather_rall(M, c->X, c->r_all, st);
+  L++;
+  bool rebuild = (c->step_count % c->freq_rp) == 0;
+  if (rebuild) {
+    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st);
+    L++;
+  }
+  record(c, 1);
+  if (rebuild) {
+    CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
+    L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
+  }
+  record(c, 2);
+  bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
+  L += 2;
+  record(c, 3);
+  bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
+  L += 9;
+  record(c, 4);
+  bdk::rotate_translate(M, c->X, c->Y, c->F0, d_rr, c->rd, c->r_all, c->precision, st);
+  L += 2;
+  record(c, 5);
+  bdk::frames(M, c->Y, st);
+  L++;
+  record(c, 6);
+  bdk::forces(M, c->Y, c->F1, c->S, c->precision, st);
+  L += 9;
+  record(c, 7);
+  bdk::average_forces(M, c->F0, c->F1, c->Fa, st);
+  bdk::rotate_translate(M, c->X, c->Y, c->Fa, d_rr, c->rd, c->r_all, c->precision, st);
+  L += 3;
+  // X <- Y (final_updates, func_cuda.cu:2643-2662), then refresh frames
+  size_t n3 = 3 * (size_t)M.n;
+  CK(cudaMemcpyAsync(c->X.r, c->Y.r, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->X.a, c->Y.a, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->X.b, c->Y.b, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->X.c, c->Y.c, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if (M.n_tail) CK(cudaMemcpyAsync(c->X.r_t, c->Y.r_t, 3 * (size_t)M.n_tail * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if (M.n_LH) CK(cudaMemcpyAsync(c->X.r_lh, c->Y.r_lh, 3 * (size_t)M.n_LH * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  bdk::frames(M, c->X, st);
+  L++;
+  record(c, 8);
+  CK(cudaGetLastError());
+  c->last_launches = L;
+  return BD_OK;
+}
+
+}  // namespace
+
+extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options* opt, bd_ctx** out) {
+  if (!out || !s) return set_error(BD_ERR_ARG, "bd_create: null argument");
+  int rc = validate(m);
+  if (rc) return rc;
+  if (!s->r || !s->a || !s->b || !s->c || (m->n_tail && !s->r_t) || (m->n_LH && !s->r_lh))
+    return set_error(BD_ERR_ARG, "bd_create: state arrays");
+  if (!s->refresh_frames && (!s->alpha || !s->beta || !s->gamma || !s->length || !s->a_dna || !s->b_dna || !s->c_dna ||
+                             !s->alpha_p || !s->beta_p || !s->gamma_p))
+    return set_error(BD_ERR_ARG, "bd_create: angles required when refresh_frames == 0");
+  bd_ctx* c = new bd_ctx();
+  if (opt) {
+    c->precision = opt->precision;
+    c->freq_rp = opt->frequency_RP > 0 ? opt->frequency_RP : 1;
+    c->use_graph = opt->use_graph;
+    c->device = opt->device;
+    c->stream = (cudaStream_t)opt->stream;
+  }
+  auto fail = [&](int code) {
+    bd_destroy(c);
+    return code;
+  };
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    return set_error(BD_ERR_CUDA, (std::string("bd_create: cudaSetDevice: ") + cudaGetErrorString(e)).c_str());
+  }
+  if (!c->stream) {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return set_error(BD_ERR_CUDA, "bd_create: stream creation failed");
+    }
+    c->own_stream = true;
+  }
+  DevModel& M = c->M;
+  M.n = m->n; M.n_c = m->n_c; M.Nq = m->Nq; M.n_t = m->n_t; M.n_tail = m->n_tail;
+  M.n_lh_n = m->n_lh_n; M.n_lh_g = m->n_lh_g; M.n_lh_c = m->n_lh_c; M.n_LH = m->n_LH;
+  M.n_D = M.n + M.n_tail + M.n_LH;
+  M.nlh = M.n_lh_n + M.n_lh_c;
+  M.h = m->h; M.g = m->g; M.s = m->s; M.debyell = m->debyell; M.debye = m->debye; M.q_l = m->q_l;
+  M.k_e = m->k_e; M.k_ex = m->k_ex;
+  M.sDD = m->sigma_DNA_DNA; M.sDC = m->sigma_DNA_Core; M.sCC = m->sigma_Core_Core;
+  M.sTT = m->sigma_Tail_Tail; M.sTL = m->sigma_Tail_Linker; M.sTC = m->sigma_Tail_Core;
+  M.a1 = m->a1; M.a2 = m->a2; M.dt = m->time_step; M.del = m->del; M.s2dt = m->s2dt;
+  const int n = M.n, nc = M.n_c, nt = M.n_tail, nL = M.n_LH, np = M.n_lh_n + M.n_lh_g + M.n_lh_c;
+  // host-side derived index arrays
+  std::vector<int> core_rank(n), core_bead, dna_bead, lh_core_bead, core_lh(nc, -1), t_core_bead(nt, -1);
+  {
+    int cnt = 0;
+    for (int i = 0; i < n; i++) {
+      if (m->type[i] == 1) { cnt++; core_bead.push_back(i); } else dna_bead.push_back(i);
+      core_rank[i] = cnt - 1;
+    }
+    for (int k = 0; k < nc; k++)
+      if (m->nc_lh_flag && m->nc_lh_flag[k] == 1) { core_lh[k] = (int)lh_core_bead.size(); lh_core_bead.push_back(core_bead[k]); }
+    for (int t = 0; t < nt; t++) {
+      int grp = m->t_grp[t], k = (grp - 1) / 10;
+      t_core_bead[t] = (k >= 0 && k < nc) ? core_bead[k] : -1;  // func.cpp:2366-2375
+    }
+  }
+  M.n_dna = (int)dna_bead.size();
+  M.n_lhcore = (int)lh_core_bead.size();
+  c->h_type.assign(m->type, m->type + n);
+  double qmax = 0, gmax = 0;
+  for (int k = 0; k < M.Nq; k++) {
+    const double* p = m->core_pos + 3 * k;
+    qmax = fmax(qmax, sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]));
+  }
+  for (int k = 0; k < M.n_lh_g; k++) {
+    const double* p = m->LH_g_pos + 3 * k;
+    gmax = fmax(gmax, sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]));
+  }
+  M.qmax_core = qmax;
+  M.gmax = gmax;
+  std::vector<double> rad_all(M.n_D);
+  for (int i = 0; i < n; i++) rad_all[i] = m->rad[i];
+  for (int i = 0; i < nt; i++) rad_all[n + i] = m->t_rad[i];
+  for (int i = 0; i < nL; i++) rad_all[n + nt + i] = m->lh_rad[i];
+  // sizes
+  c->m = 3 * M.n_D;
+  c->lda = (c->m + 31) & ~31;
+  const size_t ndna = M.n_dna, nlhc = M.n_lhcore;
+  size_t ebuf = (size_t)8 * n + nt + nL;
+  size_t tot = 0;
+  auto addD = [&](size_t k) { tot += slab<double>(k); };
+  auto addI = [&](size_t k) { tot += slab<int>(k); };
+  // model
+  addI(n); addI(n); addI(nc); addI(ndna); addI(nlhc); addI(nc); addD(n); addD(M.n_D); addD(3 * M.Nq); addD(M.Nq);
+  addD(3 * M.n_t); addI(M.n_t); addI(nc); for (int q = 0; q < 5; q++) addD(nt); addI(nt + 2); addI(nt); addI(nt);
+  addD(3 * M.n_lh_g); addI(np); addI(nc); for (int q = 0; q < 9; q++) addD(np);
+  // two states
+  for (int q = 0; q < 2; q++) {
+    for (int k = 0; k < 4; k++) addD(3 * n);
+    addD(3 * nt); addD(3 * nL);
+    for (int k = 0; k < 4; k++) addD(n);
+    for (int k = 0; k < 3; k++) addD(3 * nc);
+    for (int k = 0; k < 3; k++) addD(nc);
+    addD(nt); addD(nL); addD(3 * nlhc * M.n_lh_g);
+  }
+  for (int q = 0; q < 3; q++) { addD(3 * n); addD(3 * n); addD(3 * nt); addD(3 * nL); addD(1); }
+  addD((size_t)nc * nc * 10); addD(ndna * nc * 7); addD(nlhc * nc * 10); addD(ebuf);
+  addD(3 * (size_t)M.n_D); addD(c->m); addD(c->m); addD(3 * n); addD(bdk::trmv_scratch_doubles(c->m)); addD(1); addI(1);
+  e = cudaMalloc(&c->arena_base, tot);
+  if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
+  e = cudaMalloc((void**)&c->A, (size_t)c->m * c->lda * sizeof(double));
+  if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
+  Arena ar{(char*)c->arena_base, tot, 0};
+  int *d_type = ar.take<int>(n), *d_core_rank = ar.take<int>(n), *d_core_bead = ar.take<int>(nc),
+      *d_dna_bead = ar.take<int>(ndna), *d_lhcb = ar.take<int>(nlhc), *d_core_lh = ar.take<int>(nc);
+  double *d_phi = ar.take<double>(n), *d_rad_all = ar.take<double>(M.n_D), *d_cpos = ar.take<double>(3 * M.Nq),
+         *d_cq = ar.take<double>(M.Nq), *d_tpos = ar.take<double>(3 * M.n_t);
+  int *d_tfix_tmpl = ar.take<int>(M.n_t), *d_nct = ar.take<int>(nc);
+  double *d_ht = ar.take<double>(nt), *d_gt = ar.take<double>(nt), *d_lot = ar.take<double>(nt),
+         *d_bot = ar.take<double>(nt), *d_tq = ar.take<double>(nt);
+  int *d_tgrp = ar.take<int>(nt + 2), *d_tfix = ar.take<int>(nt), *d_tcb = ar.take<int>(nt);
+  double* d_gpos0 = ar.take<double>(3 * M.n_lh_g);
+  int *d_conn = ar.take<int>(np), *d_nclh = ar.take<int>(nc);
+  double* d_lhp[9];
+  for (int q = 0; q < 9; q++) d_lhp[q] = ar.take<double>(np);
+  DevState* sts[2] = {&c->X, &c->Y};
+  for (int q = 0; q < 2; q++) {
+    DevState& D = *sts[q];
+    D.r = ar.take<double>(3 * n); D.a = ar.take<double>(3 * n); D.b = ar.take<double>(3 * n); D.c = ar.take<double>(3 * n);
+    D.r_t = ar.take<double>(3 * nt); D.r_lh = ar.take<double>(3 * nL);
+    D.alpha = ar.take<double>(n); D.beta = ar.take<double>(n); D.gamma = ar.take<double>(n); D.length = ar.take<double>(n);
+    D.a_dna = ar.take<double>(3 * nc); D.b_dna = ar.take<double>(3 * nc); D.c_dna = ar.take<double>(3 * nc);
+    D.alpha_p = ar.take<double>(nc); D.beta_p = ar.take<double>(nc); D.gamma_p = ar.take<double>(nc);
+    D.beta_t = ar.take<double>(nt); D.beta_lh = ar.take<double>(nL); D.gpos = ar.take<double>(3 * nlhc * M.n_lh_g);
+  }
+  DevForces* fs[3] = {&c->F0, &c->F1, &c->Fa};
+  for (int q = 0; q < 3; q++) {
+    fs[q]->F = ar.take<double>(3 * n); fs[q]->T = ar.take<double>(3 * n); fs[q]->tF = ar.take<double>(3 * nt);
+    fs[q]->lF = ar.take<double>(3 * nL); fs[q]->E = ar.take<double>(1);
+  }
+  c->S.cc = ar.take<double>((size_t)nc * nc * 10);
+  c->S.dc = ar.take<double>(ndna * nc * 7);
+  c->S.gc = ar.take<double>(nlhc * nc * 10);
+  c->S.ebuf = ar.take<double>(ebuf);
+  c->S.nE = (int)ebuf;
+  c->r_all = ar.take<double>(3 * (size_t)M.n_D);
+  c->rd = ar.take<double>(c->m);
+  c->p = ar.take<double>(c->m);
+  c->rr = ar.take<double>(3 * n);
+  c->rd_part = ar.take<double>(bdk::trmv_scratch_doubles(c->m));
+  c->energy = ar.take<double>(1);
+  c->negpiv = ar.take<int>(1);
+  cudaStream_t st = c->stream;
+  std::vector<int> tgrp_pad(nt + 2, -1);
+  for (int t = 0; t < nt; t++) tgrp_pad[t] = m->t_grp[t];
+  if ((rc = up(d_type, m->type, n, st)) || (rc = up(d_core_rank, core_rank.data(), n, st)) ||
+      (rc = up(d_core_bead, core_bead.data(), nc, st)) || (rc = up(d_dna_bead, dna_bead.data(), ndna, st)) ||
+      (rc = up(d_lhcb, lh_core_bead.data(), nlhc, st)) || (rc = up(d_core_lh, core_lh.data(), nc, st)) ||
+      (rc = up(d_phi, m->phi_o, n, st)) || (rc = up(d_rad_all, rad_all.data(), M.n_D, st)) ||
+      (rc = up(d_cpos, m->core_pos, 3 * M.Nq, st)) || (rc = up(d_cq, m->core_q, M.Nq, st)) ||
+      (rc = up(d_tpos, m->tail_pos, 3 * M.n_t, st)) || (rc = up(d_tfix_tmpl, m->tail_fix, M.n_t, st)) ||
+      (rc = up(d_nct, m->nc_t_flag, nc, st)) || (rc = up(d_ht, m->h_t, nt, st)) || (rc = up(d_gt, m->g_t, nt, st)) ||
+      (rc = up(d_lot, m->lo_t, nt, st)) || (rc = up(d_bot, m->beta_o_t, nt, st)) || (rc = up(d_tq, m->t_q, nt, st)) ||
+      (rc = up(d_tgrp, tgrp_pad.data(), nt + 2, st)) || (rc = up(d_tfix, m->t_fix, nt, st)) ||
+      (rc = up(d_tcb, t_core_bead.data(), nt, st)) || (rc = up(d_gpos0, m->LH_g_pos, 3 * M.n_lh_g, st)) ||
+      (rc = up(d_conn, m->LH_conn, np, st)) || (rc = up(d_nclh, m->nc_lh_flag, nc, st)))
+    return fail(rc);
+  const double* lhsrc[9] = {m->LH_q, m->LH_vdw_hh, m->LH_vdw_hc, m->LH_vdw_hl, m->LH_vdw_ht,
+                            m->LH_kstr, m->LH_kben, m->LH_streq, m->LH_betaeq};
+  for (int q = 0; q < 9; q++)
+    if ((rc = up(d_lhp[q], lhsrc[q], np, st))) return fail(rc);
+  M.type = d_type; M.core_rank = d_core_rank; M.core_bead = d_core_bead; M.dna_bead = d_dna_bead;
+  M.lh_core_bead = d_lhcb; M.core_lh = d_core_lh; M.phi_o = d_phi; M.rad_all = d_rad_all;
+  M.core_pos = d_cpos; M.core_q = d_cq; M.tail_pos = d_tpos; M.tail_fix = d_tfix_tmpl; M.nc_t_flag = d_nct;
+  M.h_t = d_ht; M.g_t = d_gt; M.lo_t = d_lot; M.beta_o_t = d_bot; M.t_q = d_tq; M.t_grp = d_tgrp; M.t_fix = d_tfix;
+  M.t_core_bead = d_tcb; M.LH_g_pos = d_gpos0; M.LH_conn = d_conn; M.nc_lh_flag = d_nclh;
+  M.LH_q = d_lhp[0]; M.LH_vdw_hh = d_lhp[1]; M.LH_vdw_hc = d_lhp[2]; M.LH_vdw_hl = d_lhp[3]; M.LH_vdw_ht = d_lhp[4];
+  M.LH_kstr = d_lhp[5]; M.LH_kben = d_lhp[6]; M.LH_streq = d_lhp[7]; M.LH_betaeq = d_lhp[8];
+  // state
+  if ((rc = up(c->X.r, s->r, 3 * n, st)) || (rc = up(c->X.a, s->a, 3 * n, st)) || (rc = up(c->X.b, s->b, 3 * n, st)) ||
+      (rc = up(c->X.c, s->c, 3 * n, st)) || (rc = up(c->X.r_t, s->r_t, 3 * nt, st)) ||
+      (rc = up(c->X.r_lh, s->r_lh, 3 * nL, st)))
+    return fail(rc);
+  if (cudaMemsetAsync(c->X.alpha_p, 0, nc * sizeof(double), st) != cudaSuccess ||
+      cudaMemsetAsync(c->X.gamma_p, 0, nc * sizeof(double), st) != cudaSuccess ||
+      cudaMemsetAsync(c->Y.alpha_p, 0, nc * sizeof(double), st) != cudaSuccess ||
+      cudaMemsetAsync(c->Y.gamma_p, 0, nc * sizeof(double), st) != cudaSuccess ||
+      cudaMemsetAsync(c->negpiv, 0, sizeof(int), st) != cudaSuccess)
+    return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
+  bdk::frames(M, c->X, st);   // also the tail and LH bend angles
+  if (!s->refresh_frames) {
+    // keep the caller's frames and angles (cuda_application_init_data form)
+    if ((rc = up(c->X.a, s->a, 3 * n, st)) || (rc = up(c->X.b, s->b, 3 * n, st)) || (rc = up(c->X.c, s->c, 3 * n, st)) ||
+        (rc = up(c->X.alpha, s->alpha, n, st)) || (rc = up(c->X.beta, s->beta, n, st)) ||
+        (rc = up(c->X.gamma, s->gamma, n, st)) || (rc = up(c->X.length, s->length, n, st)) ||
+        (rc = up(c->X.a_dna, s->a_dna, 3 * nc, st)) || (rc = up(c->X.b_dna, s->b_dna, 3 * nc, st)) ||
+        (rc = up(c->X.c_dna, s->c_dna, 3 * nc, st)) || (rc = up(c->X.alpha_p, s->alpha_p, nc, st)) ||
+        (rc = up(c->X.beta_p, s->beta_p, nc, st)) || (rc = up(c->X.gamma_p, s->gamma_p, nc, st)))
+      return fail(rc);
+  }
+  for (int k = 0; k < 10; k++) cudaEventCreate(&c->ev[k]);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(set_error(BD_ERR_CUDA, (std::string("bd_create: ") + cudaGetErrorString(e)).c_str()));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(set_error(BD_ERR_CUDA, (std::string("bd_create: ") + cudaGetErrorString(e)).c_str()));
+  *out = c;
+  return BD_OK;
+}
+
+extern "C" int bd_destroy(bd_ctx* c) {
+  if (!c) return BD_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (int k = 0; k < 10; k++)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->A) cudaFree(c->A);
+  if (c->arena_base) cudaFree(c->arena_base);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return BD_OK;
+}
+
+extern "C" int bd_sizes(const bd_ctx* c, int* o) {
+  if (!c || !o) return set_error(BD_ERR_ARG, "bd_sizes: null argument");
+  o[0] = c->M.n; o[1] = c->M.n_c; o[2] = c->M.n_tail; o[3] = c->M.n_LH; o[4] = c->M.n_D; o[5] = c->m; o[6] = c->lda;
+  o[7] = c->precision;
+  return BD_OK;
+}
+
+static int run_step(bd_ctx* c, const double* d_rr, const double* d_p) {
+  int rc;
+  if (c->use_graph && d_rr == c->rr && d_p == c->p && c->freq_rp == 1) {
+    if (!c->graph) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      bool t = c->timing;
+      c->timing = false;
+      rc = step_device(c, d_rr, d_p);
+      c->timing = t;
+      cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+      if (rc) return rc;
+      if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_step: graph capture failed");
+      e = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_step: graph instantiation failed");
+    }
+    CK(cudaGraphLaunch(c->graph, c->stream));
+  } else {
+    if ((rc = step_device(c, d_rr, d_p))) return rc;
+  }
+  c->step_count++;
+  return BD_OK;
+}
+
+extern "C" int bd_step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* d_energy) {
+  if (!c || !d_rr || !d_p) return set_error(BD_ERR_ARG, "bd_step_device: null argument");
+  int rc = run_step(c, d_rr, d_p);
+  if (rc) return rc;
+  if (d_energy) CK(cudaMemcpyAsync(d_energy, c->F0.E, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  return BD_OK;
+}
+
+extern "C" int bd_step(bd_ctx* c, const double* rr, const double* p, double* energy) {
+  if (!c || !rr || !p) return set_error(BD_ERR_ARG, "bd_step: null argument");
+  CK(cudaMemcpyAsync(c->rr, rr, 3 * (size_t)c->M.n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int rc = run_step(c, c->rr, c->p);
+  if (rc) return rc;
+  double e = 0.0;
+  CK(cudaMemcpyAsync(&e, c->F0.E, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (!std::isfinite(e)) return set_error(BD_ERR_NONFINITE, "bd_step: non-finite energy");
+  if (energy) *energy = e;
+  return BD_OK;
+}
+
+extern "C" int bd_step_reference(bd_ctx* c, int step, int number_of_steps, int freq, const double* rr, const double* p,
+                                 double* energy, double* h_r, double* h_a, double* h_b, double* h_c, double* h_r_t,
+                                 double* h_r_lh) {
+  int rc = bd_step(c, rr, p, energy);
+  if (rc) return rc;
+  cudaStream_t st = c->stream;
+  size_t n3 = 3 * (size_t)c->M.n;
+  if (h_r_lh && c->M.n_LH) CK(cudaMemcpyAsync(h_r_lh, c->X.r_lh, 3 * (size_t)c->M.n_LH * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if ((freq > 0 && step % freq == 0) || step == number_of_steps - 1) {
+    if (h_r) CK(cudaMemcpyAsync(h_r, c->X.r, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (h_a) CK(cudaMemcpyAsync(h_a, c->X.a, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (h_b) CK(cudaMemcpyAsync(h_b, c->X.b, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (h_c) CK(cudaMemcpyAsync(h_c, c->X.c, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (h_r_t && c->M.n_tail) CK(cudaMemcpyAsync(h_r_t, c->X.r_t, 3 * (size_t)c->M.n_tail * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  return BD_OK;
+}
+
+extern "C" int bd_forces(bd_ctx* c, double* F, double* T, double* tF, double* lF, double* E) {
+  if (!c) return set_error(BD_ERR_ARG, "bd_forces: null context");
+  bdk::forces(c->M, c->X, c->F0, c->S, c->precision, c->stream);
+  CK(cudaGetLastError());
+  cudaStream_t st = c->stream;
+  size_t n3 = 3 * (size_t)c->M.n;
+  if (F) CK(cudaMemcpyAsync(F, c->F0.F, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (T) CK(cudaMemcpyAsync(T, c->F0.T, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (tF && c->M.n_tail) CK(cudaMemcpyAsync(tF, c->F0.tF, 3 * (size_t)c->M.n_tail * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (lF && c->M.n_LH) CK(cudaMemcpyAsync(lF, c->F0.lF, 3 * (size_t)c->M.n_LH * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (E) CK(cudaMemcpyAsync(E, c->F0.E, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return BD_OK;
+}
+
+static int copy_lower(bd_ctx* c, double* out, bool mirror) {
+  std::vector<double> h((size_t)c->m * c->lda);
+  CK(cudaMemcpyAsync(h.data(), c->A, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const int m = c->m, lda = c->lda;
+  for (int i = 0; i < m; i++)
+    for (int j = 0; j < m; j++) {
+      double v;
+      if (i >= j) v = h[(size_t)j * lda + i];
+      else v = mirror ? h[(size_t)i * lda + j] : 0.0;
+      out[(size_t)i * m + j] = v;
+    }
+  return BD_OK;
+}
+
+extern "C" int bd_diffusion_tensor(bd_ctx* c, double* D) {
+  if (!c || !D) return set_error(BD_ERR_ARG, "bd_diffusion_tensor: null argument");
+  bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
+  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+  CK(cudaGetLastError());
+  return copy_lower(c, D, true);
+}
+
+static int factor_now(bd_ctx* c) {
+  bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
+  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+  CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
+  bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, c->stream);
+  CK(cudaGetLastError());
+  return BD_OK;
+}
+
+extern "C" int bd_cholesky(bd_ctx* c, double* L) {
+  if (!c || !L) return set_error(BD_ERR_ARG, "bd_cholesky: null argument");
+  int rc = factor_now(c);
+  if (rc) return rc;
+  return copy_lower(c, L, false);
+}
+
+extern "C" int bd_noise_displacement(bd_ctx* c, const double* p, double* rd) {
+  if (!c || !p || !rd) return set_error(BD_ERR_ARG, "bd_noise_displacement: null argument");
+  int rc = factor_now(c);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
+  CK(cudaMemcpyAsync(rd, c->rd, (size_t)c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BD_OK;
+}
+
+static double* state_field(bd_ctx* c, const char* nm, int* cnt) {
+  DevState& X = c->X;
+  const int n = c->M.n, nc = c->M.n_c, nt = c->M.n_tail, nL = c->M.n_LH;
+  struct F { const char* k; double* p; int n; } tab[] = {
+      {"r", X.r, 3 * n}, {"a", X.a, 3 * n}, {"b", X.b, 3 * n}, {"c", X.c, 3 * n}, {"r_t", X.r_t, 3 * nt},
+      {"r_lh", X.r_lh, 3 * nL}, {"alpha", X.alpha, n}, {"beta", X.beta, n}, {"gamma", X.gamma, n},
+      {"length", X.length, n}, {"a_dna", X.a_dna, 3 * nc}, {"b_dna", X.b_dna, 3 * nc}, {"c_dna", X.c_dna, 3 * nc},
+      {"alpha_p", X.alpha_p, nc}, {"beta_p", X.beta_p, nc}, {"gamma_p", X.gamma_p, nc}, {"beta_t", X.beta_t, nt},
+      {"beta_lh", X.beta_lh, nL}, {"rd", c->rd, c->m}, {"force", c->F0.F, 3 * n}, {"torque", c->F0.T, 3 * n},
+      {"t_force", c->F0.tF, 3 * nt}, {"LH_force", c->F0.lF, 3 * nL}};
+  for (auto& f : tab)
+    if (!strcmp(f.k, nm)) { *cnt = f.n; return f.p; }
+  return nullptr;
+}
+
+extern "C" int bd_get_state(bd_ctx* c, const char* name, double* out, int* count) {
+  if (!c || !name) return set_error(BD_ERR_ARG, "bd_get_state: null argument");
+  int cnt = 0;
+  double* p = state_field(c, name, &cnt);
+  if (!p) return set_error(BD_ERR_ARG, "bd_get_state: unknown name");
+  if (count) *count = cnt;
+  if (out && cnt) {
+    CK(cudaMemcpyAsync(out, p, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return BD_OK;
+}
+
+extern "C" int bd_set_state(bd_ctx* c, const char* name, const double* in) {
+  if (!c || !name || !in) return set_error(BD_ERR_ARG, "bd_set_state: null argument");
+  static const char* ok[] = {"r", "a", "b", "c", "r_t", "r_lh"};
+  bool allowed = false;
+  for (auto k : ok) allowed |= !strcmp(k, name);
+  if (!allowed) return set_error(BD_ERR_ARG, "bd_set_state: only r a b c r_t r_lh can be set");
+  int cnt = 0;
+  double* p = state_field(c, name, &cnt);
+  if (cnt) CK(cudaMemcpyAsync(p, in, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  bdk::frames(c->M, c->X, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return BD_OK;
+}
+
+extern "C" int bd_dev_rpy(bd_ctx* c, int nb, const double* d_r, const double* d_rad, double a1, double a2, double* d_D,
+                          int lda) {
+  if (!c || !d_r || !d_rad || !d_D || nb <= 0 || lda < 3 * nb) return set_error(BD_ERR_ARG, "bd_dev_rpy: bad argument");
+  bdk::rpy_assemble(nb, d_r, d_rad, a1, a2, d_D, lda, c->stream);
+  CK(cudaGetLastError());
+  return BD_OK;
+}
+
+extern "C" int bd_dev_potrf(bd_ctx* c, int m, double* d_A, int lda, int precision, int* d_info) {
+  if (!c || !d_A || m <= 0 || lda < m || !d_info) return set_error(BD_ERR_ARG, "bd_dev_potrf: bad argument");
+  if (precision != BD_PREC_FP64) return set_error(BD_ERR_ARG, "bd_dev_potrf: only BD_PREC_FP64 is available");
+  bdk::potrf_fp64(m, d_A, lda, nullptr, nullptr, 0.0, d_info, c->stream);
+  CK(cudaGetLastError());
+  return BD_OK;
+}
+
+extern "C" int bd_phase_times(bd_ctx* c, float* out9) {
+  if (!c || !out9) return set_error(BD_ERR_ARG, "bd_phase_times: null argument");
+  if (!c->timing) {
+    c->timing = true;  // enabled from the next step on
+    for (int k = 0; k < 9; k++) out9[k] = 0.f;
+    return BD_OK;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 8; k++) cudaEventElapsedTime(&out9[k], c->ev[k], c->ev[k + 1]);
+  cudaEventElapsedTime(&out9[8], c->ev[0], c->ev[8]);
+  return BD_OK;
+}
+
+extern "C" int bd_launch_count(bd_ctx* c, int* out) {
+  if (!c || !out) return set_error(BD_ERR_ARG, "bd_launch_count: null argument");
+  *out = c->last_launches;
+  return BD_OK;
+}
+
+extern "C" int bd_negative_pivots(bd_ctx* c, int* out) {
+  if (!c || !out) return set_error(BD_ERR_ARG, "bd_negative_pivots: null argument");
+  CK(cudaMemcpyAsync(&c->host_negpiv, c->negpiv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *out = c->host_negpiv;
+  return BD_OK;
+}

@@ -1,0 +1,123 @@
+// Internal declarations shared by the host code and the CUDA kernels of
+// libbdgb300.so.  Not part of the public ABI (include/bd_capi.h is).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "../../include/bd_capi.h"
+
+namespace bdh {
+
+// error reporting (bd_capi.cpp)
+int set_error(int code, const char* msg);
+
+// ------------------------------------------------------------ host system
+struct HostSystem {
+  bd_model m{};
+  std::vector<double> setup;
+  std::vector<int> type, tail_fix, nc_t_flag, t_grp, t_fix, LH_conn, nc_lh_flag;
+  std::vector<double> r, a, b, c, rad, phi_o, r_var, core_pos, core_q, tail_pos, r_t, h_t, g_t, lo_t, beta_o_t, t_q,
+      t_rad, LH_g_pos, LH_q, LH_vdw_hh, LH_vdw_hc, LH_vdw_hl, LH_vdw_ht, LH_kstr, LH_kben, LH_streq, LH_betaeq,
+      r_lh, lh_rad;
+};
+
+int load_system(const char* dir, const char* data_f, const char* core_f, const char* tail_f, const char* lh_f,
+                const char* lhflag_f, HostSystem& S, std::string& err);
+void refresh_model_pointers(HostSystem& S);
+int write_xyz(const bd_model* m, const double* r, const double* a, const double* b, const double* c,
+              const double* r_t, const double* r_lh, const char* path);
+
+struct Mt19937 {
+  uint32_t st[624];
+  int idx = 625;
+  double cached = 0.0;
+  bool have = false;
+  void seed(uint32_t s);
+  uint32_t next();
+  double real1() { return next() * (1.0 / 4294967295.0); }
+  double normal(double mean, double sd);
+};
+
+}  // namespace bdh
+
+// ------------------------------------------------------------ device model
+// Everything a kernel needs about one fiber, passed by value.  Pointers are
+// device pointers.  Bead classes: chain beads [0,n) (cores and linker DNA),
+// tail beads [0,n_tail), mobile LH beads [0,n_LH); in the diffusion tensor
+// they are stacked chain | tails | LH (n_D = n + n_tail + n_LH).
+struct DevModel {
+  int n, n_c, Nq, n_t, n_tail, n_lh_n, n_lh_g, n_lh_c, n_LH, n_D, nlh, n_dna, n_lhcore;
+  double h, g, s, debyell, debye, q_l, k_e, k_ex;
+  double sDD, sDC, sCC, sTT, sTL, sTC;
+  double a1, a2, dt, del, s2dt;
+  const int* type;         // [n]
+  const int* core_rank;    // [n] cores in [0,i] minus 1
+  const int* core_bead;    // [n_c] bead index of core k
+  const int* dna_bead;     // [n_dna] bead index of the k-th linker bead
+  const int* lh_core_bead; // [n_lhcore] bead index of the k-th LH-bearing core
+  const int* core_lh;      // [n_c] LH ordinal of core k or -1
+  const double* phi_o;     // [n]
+  const double* rad_all;   // [n_D]
+  const double* core_pos;  // [3 Nq]
+  const double* core_q;    // [Nq]
+  const double* tail_pos;  // [3 n_t]
+  const int* tail_fix;     // [n_t]
+  const int* nc_t_flag;    // [n_c]
+  const double *h_t, *g_t, *lo_t, *beta_o_t, *t_q;  // [n_tail]
+  const int *t_grp, *t_fix;                        // [n_tail]
+  const int* t_core_bead;  // [n_tail] core bead of the tail's group ((t_grp-1)/10)
+  const double* LH_g_pos;  // [3 n_lh_g]
+  const int* LH_conn;      // [n_lh_n + n_lh_g + n_lh_c]
+  const int* nc_lh_flag;   // [n_c]
+  const double *LH_q, *LH_vdw_hh, *LH_vdw_hc, *LH_vdw_hl, *LH_vdw_ht, *LH_kstr, *LH_kben, *LH_streq, *LH_betaeq;
+  double qmax_core;        // max |core_pos| (nm), for exact far-pair skipping
+  double gmax;             // max |LH_g_pos|
+};
+
+// Configuration-dependent arrays of one state (current or predicted).
+struct DevState {
+  double *r, *a, *b, *c;          // [3n]
+  double *r_t, *r_lh;             // [3 n_tail], [3 n_LH]
+  double *alpha, *beta, *gamma, *length;   // [n]
+  double *a_dna, *b_dna, *c_dna;           // [3 n_c]
+  double *alpha_p, *beta_p, *gamma_p;      // [n_c]
+  double *beta_t, *beta_lh;                // [n_tail], [n_LH]
+  double* gpos;                            // [3 n_lhcore n_lh_g] G-head sites (per force pass)
+};
+
+struct DevForces {
+  double *F, *T, *tF, *lF;   // [3n] [3n] [3 n_tail] [3 n_LH]
+  double* E;                 // [1]
+};
+
+// Scratch for the deterministic two-stage pair sums (one slot per
+// interacting object pair, reduced per bead in a fixed order).
+struct DevScratch {
+  double* cc;    // [n_c * n_c * 10]  core-core: F(3) T_i(3) T_j(3) E
+  double* dc;    // [n_dna * n_c * 7] DNA-core: F_on_dna(3) T_core(3) E
+  double* gc;    // [n_lhcore * n_c * 10] G-head(core I) - charges(core L): F_I(3) T_I(3) T_L(3) E
+  double* ebuf;  // [nE] per-kernel energy partials
+  int nE;
+};
+
+namespace bdk {
+// frames.cu
+void frames(const DevModel& M, DevState& S, cudaStream_t st);
+void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const DevForces& Fo, const double* rr,
+                      const double* rd, const double* r_all, int mixed, cudaStream_t st);
+void average_forces(const DevModel& M, const DevForces& A, const DevForces& B, DevForces& out, cudaStream_t st);
+void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream_t st);
+// forces.cu
+void forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);
+// rpy_chol.cu
+void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
+                  cudaStream_t st);
+int potrf_fp64(int m, double* A, int lda, double* rd_acc, const double* p, double s2dt, int* d_negpiv,
+               cudaStream_t st);
+size_t trmv_scratch_doubles(int m);
+void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
+                   cudaStream_t st);
+}  // namespace bdk

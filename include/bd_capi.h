@@ -1,0 +1,201 @@
+/*
+ * bd_capi.h - C ABI of the GB300 Brownian-dynamics step for the mesoscale
+ * chromatin fiber (libbdgb300.so).
+ *
+ * The reference (Schlicklab/Brownian_Dynamics_CUDA) exposes its GPU step as
+ * four C++ functions (BD_cuda/func_cuda.h:37-52) backed by file-scope
+ * globals.  This header replaces them with a handle-based C ABI: plain
+ * pointers and sizes, host arrays in the reference's own layouts (xyz
+ * interleaved per bead, row-major matrices), an int status from every call,
+ * no globals and no C++ types.  A shim in the same library re-exports the
+ * four reference symbols on top of it, so the
+ * reference's main.cpp links against this library unchanged.
+ *
+ * Threading: a context is used by one host thread at a time; different
+ * contexts are independent.  All device work of a context runs on the
+ * stream given at creation (0 = a stream the context creates).
+ */
+#ifndef BD_CAPI_H
+#define BD_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum {
+  BD_OK = 0,
+  BD_ERR_ARG = 1,        /* bad pointer, size or name */
+  BD_ERR_IO = 2,         /* input file missing or malformed */
+  BD_ERR_CUDA = 3,       /* a CUDA runtime call failed (bd_last_error has it) */
+  BD_ERR_NOMEM = 4,      /* device allocation failed */
+  BD_ERR_NONFINITE = 5,  /* a NaN/Inf appeared in forces or positions */
+  BD_ERR_NOT_SPD = 6,    /* reserved: strict-SPD mode found a non-positive pivot */
+  BD_ERR_STATE = 7       /* call not valid in the context's current state */
+};
+
+/* Message of the last failing call on this thread (static storage). */
+const char* bd_last_error(void);
+/* Library version string. */
+const char* bd_version(void);
+
+/* --------------------------------------------------------------- precision */
+enum {
+  BD_PREC_FP64 = 0,   /* plain FP64 step: parity path against the FP64 oracle */
+  BD_PREC_MIXED = 1   /* tensor-core Cholesky (BF16 split operands), FP64 refinement */
+};
+
+/* ------------------------------------------------------------ model (host)
+ * Topology, parameters and per-bead constants of one fiber.  Field names and
+ * meanings are those of cuda_application_init_data (func_cuda.cu:2676) and
+ * main.cpp:38-372.  Arrays are borrowed: bd_create copies what it needs. */
+typedef struct bd_model {
+  int n, n_c;              /* beads on the chain (cores + linker DNA), cores   */
+  int Nq;                  /* charges per core (300)                           */
+  int n_t, n_tail;         /* tail beads per core (template), total tail beads */
+  int n_lh_n, n_lh_g, n_lh_c, n_LH;  /* LH N-term / G-head / C-term per LH, total mobile LH beads */
+  double h, g, s;          /* stretch, bend, twist constants (main.cpp:90-95)  */
+  double debyell, debye, q_l, k_e, k_ex, k_h1;
+  double sigma_DNA_DNA, sigma_DNA_Core, sigma_Core_Core;
+  double sigma_Tail_Tail, sigma_Tail_Linker, sigma_Tail_Core;
+  double a1, a2;           /* kT/(6 pi eta), kT/(8 pi eta)                      */
+  double time_step, del, s2dt;  /* dt, dt/kT, sqrt(2 dt)                        */
+  const int* type;         /* [n] 1 = core, 0 = linker DNA                      */
+  const double* rad;       /* [n] hydrodynamic radius                           */
+  const double* phi_o;     /* [n] intrinsic twist (update_phi_o)                */
+  const double* r_var;     /* [3n] rotational noise "stddev" (main.cpp:292-303) */
+  const double* core_pos;  /* [3 Nq] charge sites, core frame, nm               */
+  const double* core_q;    /* [Nq]                                              */
+  const double* tail_pos;  /* [3 n_t] tail template, core frame, nm             */
+  const int* tail_fix;     /* [n_t] template anchor flags                       */
+  const int* nc_t_flag;    /* [n_c] cores carrying tails                        */
+  const double* h_t; const double* g_t; const double* lo_t; const double* beta_o_t;
+  const double* t_q; const double* t_rad;   /* [n_tail]                          */
+  const int* t_grp; const int* t_fix;       /* [n_tail]                          */
+  const double* LH_g_pos;  /* [3 n_lh_g] globular head, core frame               */
+  const int* LH_conn;      /* [n_lh_n+n_lh_g+n_lh_c]                             */
+  const int* nc_lh_flag;   /* [n_c] cores carrying a linker histone              */
+  const double* LH_q; const double* LH_vdw_hh; const double* LH_vdw_hc;
+  const double* LH_vdw_hl; const double* LH_vdw_ht; const double* LH_kstr;
+  const double* LH_kben; const double* LH_streq; const double* LH_betaeq;
+  const double* lh_rad;    /* [n_LH]                                            */
+} bd_model;
+
+/* Configuration state.  With refresh_frames != 0 the internal coordinates
+ * (Euler angles, exit frames, bend angles) are computed on the device from
+ * r,a,b,c as main.cpp:166 does on the host, re-orthonormalising the DNA
+ * frames; otherwise the angle arrays must be given (as init_data takes them). */
+typedef struct bd_state {
+  const double* r; const double* a; const double* b; const double* c;   /* [3n] */
+  const double* r_t;       /* [3 n_tail] */
+  const double* r_lh;      /* [3 n_LH]   */
+  int refresh_frames;
+  const double* alpha; const double* beta; const double* gamma; const double* length;  /* [n] */
+  const double* a_dna; const double* b_dna; const double* c_dna;                       /* [3 n_c] */
+  const double* alpha_p; const double* beta_p; const double* gamma_p;                  /* [n_c] */
+} bd_state;
+
+typedef struct bd_options {
+  int precision;           /* BD_PREC_FP64 or BD_PREC_MIXED                      */
+  int frequency_RP;        /* rebuild + refactor D every k steps (1 = every step,
+                              as the reference does)                             */
+  int use_graph;           /* capture the device part of a step in a CUDA graph  */
+  int device;              /* CUDA device ordinal                                */
+  void* stream;            /* cudaStream_t to run on, or NULL                    */
+} bd_options;
+
+/* ---------------------------------------------------- host system loader
+ * Reads the reference's input files from dir exactly as main.cpp:38-372
+ * does with readfile.cpp (setup.txt, data_mod, core charges, tail table,
+ * LH table, LH.in) and builds tails, linker histones, phi_o, r_var and the
+ * physical constants.  Frames are returned as read (not yet refreshed). */
+typedef struct bd_system bd_system;
+int bd_system_load(const char* dir, const char* data_file, const char* core_file, const char* tail_file,
+                   const char* lh_file, const char* lh_flags_file, bd_system** out);
+/* Model and state views that point into the system's own storage. */
+int bd_system_model(const bd_system* sys, bd_model* out);
+int bd_system_state(const bd_system* sys, bd_state* out);
+/* setup.txt values: T steps freq freq_RP sigma x6 Mg Cs restart unbind Pbind (15) */
+int bd_system_setup(const bd_system* sys, double* out15);
+void bd_system_free(bd_system* sys);
+/* Appends one out.xyz frame (readfile.cpp:346-405 format). */
+int bd_write_xyz(const bd_model* m, const double* r, const double* a, const double* b, const double* c,
+                 const double* r_t, const double* r_lh, const char* path);
+
+/* ------------------------------------------------------------ noise (host)
+ * MT19937 + polar Box-Muller stream in the reference order (mt.cpp,
+ * utilities.cpp:304-336, main.cpp:386-388 and :479-486). */
+typedef struct bd_noise bd_noise;
+int bd_noise_create(unsigned long seed, bd_noise** out);
+/* Draws one step's noise: two uniforms when step % 100 == 0, then rr[n3]
+ * with per-DOF scale r_var, then p[n_D3] ~ N(0,1). */
+int bd_noise_step(bd_noise* g, int step, int n3, const double* r_var, int n_D3, double* rr, double* p);
+int bd_noise_u32(bd_noise* g, int count, uint32_t* out);
+void bd_noise_free(bd_noise* g);
+
+/* ------------------------------------------------------------ device step */
+typedef struct bd_ctx bd_ctx;
+
+/* Allocates device state and copies model + state to the device.
+ * Replaces cuda_application_init_D_Chol + cuda_application_init_data
+ * (func_cuda.cu:2665, :2676). */
+int bd_create(const bd_model* m, const bd_state* s, const bd_options* opt, bd_ctx** out);
+int bd_destroy(bd_ctx* ctx);
+
+/* Sizes: n n_c n_tail n_LH n_D m(=3 n_D) lda(padded leading dim) precision */
+int bd_sizes(const bd_ctx* ctx, int* out8);
+
+/* One predictor-corrector BD step (main_cuda, func_cuda.cu:3434-3680).
+ * rr[3n] and p[3 n_D] are host noise arrays; energy (may be NULL) receives
+ * the pass-1 energy.  Host copies of the state are refreshed on return for
+ * every non-NULL pointer in out_state-like arguments of bd_get_state. */
+int bd_step(bd_ctx* ctx, const double* rr, const double* p, double* energy);
+
+/* Same step, noise already on the device (device pointers, stream-ordered). */
+int bd_step_device(bd_ctx* ctx, const double* d_rr, const double* d_p, double* d_energy);
+
+/* Drop-in form of main_cuda: runs bd_step and copies back exactly what
+ * main_cuda copies back: r_lh every step; r, a, b, c, r_t when
+ * step % frequency_of_sampling == 0 or step == number_of_steps - 1. */
+int bd_step_reference(bd_ctx* ctx, int step, int number_of_steps, int frequency_of_sampling, const double* rr,
+                      const double* p, double* energy, double* h_r, double* h_a, double* h_b, double* h_c,
+                      double* h_r_t, double* h_r_lh);
+
+/* Finer entry points (each works on the context's current state). */
+/* Forces [3n], torques [3n], tail forces [3 n_tail], LH forces [3 n_LH], energy. */
+int bd_forces(bd_ctx* ctx, double* force, double* torque, double* t_force, double* LH_force, double* energy);
+/* Full symmetric RPY tensor, row-major m x m (m = 3 n_D). */
+int bd_diffusion_tensor(bd_ctx* ctx, double* D);
+/* Lower Cholesky factor of D, row-major m x m, upper triangle zero. */
+int bd_cholesky(bd_ctx* ctx, double* L);
+/* Noise displacement rd = sqrt(2 dt) L p for the current state, rd[m]. */
+int bd_noise_displacement(bd_ctx* ctx, const double* p, double* rd);
+
+/* Named state arrays (host copies): r a b c r_t r_lh alpha beta gamma length
+ * a_dna b_dna c_dna alpha_p beta_p gamma_p beta_t beta_lh rd force torque
+ * t_force LH_force.  Returns BD_ERR_ARG for an unknown name. */
+int bd_get_state(bd_ctx* ctx, const char* name, double* out, int* count);
+/* Overwrites r a b c r_t or r_lh and refreshes the internal coordinates. */
+int bd_set_state(bd_ctx* ctx, const char* name, const double* in);
+
+/* Standalone dense kernels on caller-owned device buffers (stream-ordered on
+ * the context's stream).  Matrices are column-major with leading dim lda. */
+int bd_dev_rpy(bd_ctx* ctx, int n_beads, const double* d_r, const double* d_rad, double a1, double a2,
+               double* d_D, int lda);
+int bd_dev_potrf(bd_ctx* ctx, int m, double* d_A, int lda, int precision, int* d_info);
+
+/* Timing of the last step's phases on the device (ms): rpy chol rd forces1
+ * update1 frames forces2 update2 total.  Valid after a step with use_graph=0. */
+int bd_phase_times(bd_ctx* ctx, float* out9);
+/* Count of kernel launches issued by the last bd_step (graph nodes count once each). */
+int bd_launch_count(bd_ctx* ctx, int* out);
+/* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
+int bd_negative_pivots(bd_ctx* ctx, int* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BD_CAPI_H */
