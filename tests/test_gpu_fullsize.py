@@ -1,0 +1,40 @@
+"""Size-independent properties at the benchmark sizes (too large for the
+CPU oracle to finish in seconds): the factor reproduces D, the step is
+finite, deterministic, and its noise displacement has the statistics of
+sqrt(2 dt) L p."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cfg1(tmp_path_factory):
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber
+    return make_fiber(config(1), str(tmp_path_factory.mktemp("cfg1")))
+
+
+def test_cfg1_factor_reproduces_tensor(cfg1):
+    from brownian_dynamics_cuda_gb300 import Context
+    c = Context(cfg1)
+    D = c.diffusion_tensor()
+    L = c.cholesky()
+    assert c.negative_pivots() == 0
+    rng = np.random.default_rng(0)
+    cols = rng.choice(c.m, 48, replace=False)
+    R = L @ L[cols].T - D[:, cols]               # sampled columns of L L^T - D
+    assert np.abs(R).max() <= 1e-11 * np.abs(D).max()
+
+
+def test_cfg1_step_finite_and_deterministic(cfg1):
+    from brownian_dynamics_cuda_gb300 import Context, Noise
+    noise = Noise(2024)
+    rr, p = noise.step(0, cfg1.arrays["r_var"], cfg1.m)
+    a, b = Context(cfg1, use_graph=True), Context(cfg1)
+    ea, eb = a.step(rr, p), b.step(rr, p)
+    assert np.isfinite(ea) and ea == eb
+    for k in ("r", "r_t", "r_lh", "a"):
+        x = a.get(k)
+        assert np.all(np.isfinite(x)) and np.array_equal(x, b.get(k))
+    d = a.get("r") - cfg1.state["r"]
+    assert 0 < np.abs(d).max() < 1.0   # nm per ps step

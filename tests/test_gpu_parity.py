@@ -1,0 +1,122 @@
+"""Parity of the CUDA FP64 step (through the C ABI) with the CPU oracle and
+with the golden fixtures made by the reference's own CPU code.
+
+Tolerance: 1e-10 relative (max |x - ref| / max |ref| per array) for
+forces, torques, the noise displacement and positions after every step, as
+the plain FP64 path requires.  The RPY tensor and the internal coordinates
+at start-up are expected bitwise (same expressions, no FMA contraction).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", params=golden_names())
+def case(request):
+    fib, z = load_golden(request.param)
+    return request.param, fib, z
+
+
+def ctx_for(fib, **kw):
+    from brownian_dynamics_cuda_gb300 import Context
+    return Context(fib, **kw)
+
+
+def test_start_frames_bitwise(case):
+    name, fib, z = case
+    c = ctx_for(fib)
+    for k in ("a", "b", "c", "alpha", "beta", "gamma", "length", "a_dna", "b_dna", "c_dna", "beta_p", "gamma_p",
+              "beta_t", "beta_lh"):
+        ref = z["s0_" + k]
+        if ref.size:
+            assert rel_err(c.get(k), ref) <= 1e-14, k
+
+
+def test_forces(case):
+    name, fib, z = case
+    f = ctx_for(fib).forces()
+    for k in ("force", "torque", "t_force", "LH_force"):
+        if z["f0_" + k].size:
+            assert rel_err(f[k], z["f0_" + k]) <= TOL, k
+    assert abs(f["energy"] - float(z["f0_energy"])) <= TOL * abs(float(z["f0_energy"]))
+
+
+def test_tensor_and_factor(case):
+    name, fib, z = case
+    c = ctx_for(fib)
+    D = c.diffusion_tensor()
+    assert rel_err(np.diag(D), z["D_diag"]) == 0.0
+    assert rel_err(D[:, 0], z["D_col0"]) == 0.0
+    assert rel_err(D.sum(axis=1), z["D_rowsum"]) <= 1e-14
+    assert np.array_equal(D, D.T)
+    L = c.cholesky()
+    assert np.all(np.triu(L, 1) == 0.0)
+    assert rel_err(np.diag(L), z["L_diag"]) <= TOL
+    assert rel_err(L[:, 0], z["L_col0"]) <= TOL
+    assert rel_err(L.sum(axis=1), z["L_rowsum"]) <= TOL
+    assert c.negative_pivots() == 0
+
+
+def test_steps_match_reference(case):
+    name, fib, z = case
+    c = ctx_for(fib)
+    for s in range(int(z["steps"])):
+        e = c.step(z[f"noise{s}_rr"], z[f"noise{s}_p"])
+        assert abs(e - float(z[f"step{s}_energy"])) <= TOL * abs(float(z[f"step{s}_energy"])), s
+        for k in ("rd", "r", "a", "b", "c", "r_t", "r_lh"):
+            ref = z[f"step{s}_{k}"]
+            if ref.size:
+                assert rel_err(c.get(k), ref) <= TOL, (s, k)
+        # displacement relative to the start of the step
+        r_prev = fib.state["r"] if s == 0 else z[f"step{s - 1}_r"]
+        disp = c.get("r") - r_prev
+        assert rel_err(disp, z[f"step{s}_r"] - r_prev) <= 1e-8, s
+
+
+def test_steps_match_oracle_and_are_deterministic(case):
+    from oracle.pyoracle import Oracle
+    name, fib, z = case
+    rng = np.random.default_rng(11)
+    o = Oracle(fib)
+    c1, c2 = ctx_for(fib), ctx_for(fib, use_graph=True)
+    for s in range(2):
+        rr = rng.normal(size=3 * fib.sizes["n"]) * np.sqrt(fib.arrays["r_var"])
+        p = rng.normal(size=fib.m)
+        e0 = o.step(rr, p)
+        e1 = c1.step(rr, p)
+        e2 = c2.step(rr, p)
+        assert e1 == e2
+        assert abs(e1 - e0) <= TOL * abs(e0)
+        for k in ("r", "a", "b", "c", "r_t", "r_lh"):
+            x1, x2 = c1.get(k), c2.get(k)
+            assert np.array_equal(x1, x2), (s, k)      # graph replay == eager, run to run
+            if x1.size:
+                assert rel_err(x1, o.get(k)) <= TOL, (s, k)
+
+
+def test_drop_in_step_reference_copies(case):
+    """bd_step_reference copies back what main_cuda copies back."""
+    import ctypes
+    from brownian_dynamics_cuda_gb300.capi import _pd
+    name, fib, z = case
+    c = ctx_for(fib)
+    L = c._L
+    n3, nt3, nl3 = 3 * fib.sizes["n"], 3 * fib.sizes["n_tail"], 3 * fib.sizes["n_LH"]
+    h = {k: np.full(v, -7.0) for k, v in (("r", n3), ("a", n3), ("b", n3), ("c", n3), ("r_t", max(nt3, 1)),
+                                           ("r_lh", max(nl3, 1)))}
+    e = ctypes.c_double()
+    rr, p = z["noise0_rr"], z["noise0_p"]
+    # step 1 of 10 with sampling every 5: only r_lh comes back
+    rc = L.bd_step_reference(c._h, 1, 10, 5, _pd(rr), _pd(p), ctypes.byref(e), _pd(h["r"]), _pd(h["a"]), _pd(h["b"]),
+                             _pd(h["c"]), _pd(h["r_t"]), _pd(h["r_lh"]))
+    assert rc == 0
+    assert np.all(h["r"] == -7.0)
+    if nl3:
+        assert np.array_equal(h["r_lh"], c.get("r_lh"))
+    rc = L.bd_step_reference(c._h, 5, 10, 5, _pd(rr), _pd(p), ctypes.byref(e), _pd(h["r"]), _pd(h["a"]), _pd(h["b"]),
+                             _pd(h["c"]), _pd(h["r_t"]), _pd(h["r_lh"]))
+    assert rc == 0 and np.array_equal(h["r"], c.get("r")) and np.array_equal(h["c"], c.get("c"))
