@@ -1,0 +1,276 @@
+#!/usr/bin/env python
+"""Benchmark of the BD step for the mesoscale chromatin fiber on GB300.
+
+One "step" is one full predictor-corrector BD step (RPY tensor, Cholesky,
+noise displacement, two force passes, two moves) of the 50-nucleosome fiber
+with 44-bp linkers and a linker histone on every nucleosome (3N = 11,700),
+with seeded MT19937 noise.  Inputs are resident in HBM for `value`; `e2e`
+runs the same steps through the reference-facing call (host noise in, host
+copies of the state out, as main_cuda does).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config 0..4] [--precision fp64|mixed]
+
+Multi-GPU: replicas only (independent fibers, one per rank, no collective in
+the step); rank 0 prints the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BD steps/s vs plain FP64 on 1 GB300 at <=1e-6 rel. error; replica-steps/s"
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "fallback": True}
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) > 8 for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def make_fiber(cfg: int, seed: int):
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber as mk
+    d = tempfile.mkdtemp(prefix="bdfiber_")
+    spec = config(cfg, seed=seed)
+    return mk(spec, d), spec
+
+
+def cpu_sample(fib, threads: int, n0_beads: int = 400) -> dict:
+    """Bounded CPU sample of one step with the oracle port: one full force
+    pass (x2 for the corrector), the RPY assembly and the reference Cholesky
+    of the leading n0 beads, extrapolated by (m/m0)^2 and (m/m0)^3."""
+    from oracle.pyoracle import Oracle, cholesky, rpy
+    o = Oracle(fib)
+    t = time.perf_counter()
+    o.forces()
+    t_f = time.perf_counter() - t
+    r_all = np.concatenate([fib.state["r"], fib.state["r_t"], fib.state["r_lh"]])
+    rad = np.concatenate([fib.arrays["rad"], fib.arrays["t_rad"], fib.arrays["lh_rad"]])
+    n0 = min(n0_beads, fib.n_D)
+    t = time.perf_counter()
+    D = rpy(r_all[:3 * n0], rad[:n0], fib.scalars["a1"], fib.scalars["a2"])
+    t_r = time.perf_counter() - t
+    t = time.perf_counter()
+    cholesky(D, nthreads=threads)
+    t_c = time.perf_counter() - t
+    m, m0 = fib.m, 3 * n0
+    step_s = 2 * t_f + t_r * (m / m0) ** 2 + t_c * (m / m0) ** 3
+    return {"step_s": step_s, "t_forces": t_f, "t_rpy0": t_r, "t_chol0": t_c, "m0": m0,
+            "sample": f"one force pass of the full fiber (x2), RPY assembly + reference Cholesky of the leading "
+                      f"{m0}x{m0} block extrapolated by (m/m0)^2 and (m/m0)^3 to m={m}"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    fib, spec = make_fiber(args.config, 1)
+    threads = os.cpu_count() or 1
+    samples = []
+    for i in range(args.warmup + args.steps):
+        s = cpu_sample(fib, threads)
+        if i >= args.warmup:
+            samples.append(s["step_s"])
+    step_s = float(np.mean(samples))
+    v = 1.0 / step_s
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fiber generator)",
+            "config": {"workload": spec.name, "n_D": fib.n_D, "3N": fib.m, "precision": "fp64"},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port", "sample": s["sample"]},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context, Noise
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
+    fib, spec = make_fiber(args.config, 1 + rank)
+    stream = torch.cuda.Stream()
+    ctx = Context(fib, precision=prec, use_graph=True, device=local, stream=stream.cuda_stream)
+    n3, m = 3 * fib.sizes["n"], fib.m
+    nsteps = args.warmup + args.steps
+    noise = Noise(1000 + rank)
+    host = [noise.step(i, fib.arrays["r_var"], m) for i in range(nsteps)]
+    rr_d = torch.tensor(np.stack([h[0] for h in host]), device="cuda", dtype=torch.float64)
+    p_d = torch.tensor(np.stack([h[1] for h in host]), device="cuda", dtype=torch.float64)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            ctx.step_device(rr_d[i].data_ptr(), p_d[i].data_ptr())
+        stream.synchronize()
+        # per-phase times of one eager step (events on the context's stream)
+        ctx.phase_times()
+        ph_ctx = Context(fib, precision=prec, use_graph=False, device=local, stream=stream.cuda_stream)
+        ph_ctx.phase_times()
+        ph_ctx.step_device(rr_d[0].data_ptr(), p_d[0].data_ptr())
+        phases = ph_ctx.phase_times()
+        ph_ctx.close()
+        barrier()
+        torch.cuda.synchronize()
+        clk = ClockSampler(local)
+        clk.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.warmup, nsteps):
+            ctx.step_device(rr_d[i].data_ptr(), p_d[i].data_ptr())
+        e1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+    launches = ctx.launch_count() * args.steps
+    # e2e: reference-facing call with host buffers (noise H2D, r_lh D2H every
+    # step, full state D2H on sampling steps every 100 steps)
+    e2e_ctx = Context(fib, precision=prec, use_graph=True, device=local, stream=stream.cuda_stream)
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    rr_h = [pin(h[0]) for h in host]
+    p_h = [pin(h[1]) for h in host]
+    out = {k: pin(np.zeros(v)) for k, v in (("r", n3), ("a", n3), ("b", n3), ("c", n3),
+                                              ("r_t", max(3 * fib.sizes["n_tail"], 1)),
+                                              ("r_lh", max(3 * fib.sizes["n_LH"], 1)))}
+    freq = 100
+    for i in range(args.warmup):
+        e2e_ctx.step_reference(i, 1 << 30, freq, rr_h[i], p_h[i], out)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.warmup, nsteps):
+        e2e_ctx.step_reference(i, 1 << 30, freq, rr_h[i], p_h[i], out)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = (n3 + m) * 8
+    d2h = 8 + 3 * fib.sizes["n_LH"] * 8 + (4 * n3 + 3 * fib.sizes["n_tail"]) * 8 / freq
+    # roofline of the dominant phase: the Cholesky factorisation, m^3/3 flops
+    pk = peaks()
+    chol_ms = float(phases[1])
+    chol_flop = m ** 3 / 3.0
+    if prec == PREC_FP64:
+        fp64_peak = 1.10  # TFLOP/s: cuBLAS DGEMM 8192^3 measured on this machine's GB300 (profiles/fp64_peak_probe.md)
+        roof = {"bound": "fp64", "achieved": chol_flop / (chol_ms * 1e-3) / 1e12, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": None, "traffic": None, "kernel": "potrf_fp64 (diag+trsm+syrk)",
+                "peak_source": "measured cuBLAS DGEMM (no FP64 entry in MEASURED_PEAKS.json)"}
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    else:
+        roof = {"bound": "tensor", "achieved": chol_flop / (chol_ms * 1e-3) / 1e12, "peak": pk["bf16_tflops"],
+                "unit": "TFLOP/s", "traffic": None, "kernel": "potrf mixed", "peak_source": "MEASURED_PEAKS.json"}
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        s = cpu_sample(fib, 1)
+        cpu = {"value": 1.0 / s["step_s"], "unit": "steps/s", "cores": 1, "kind": "port", "sample": s["sample"]}
+    if rank == 0:
+        names = ["rpy", "chol", "rd", "forces1", "move1", "frames", "forces2", "move2+frames", "total"]
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if prec == PREC_FP64 else "bf16x3+f64",
+                "data": "synthetic (seeded fiber generator, reference file formats)",
+                "config": {"workload": spec.name, "n_D": fib.n_D, "3N": m, "precision": args.precision,
+                           "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (D is %.2f GB)" %
+                                                                         (m * m * 8 / 1e9)},
+                "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+                "phases_ms": dict(zip(names, [round(float(x), 4) for x in phases])),
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -276,13 +276,13 @@ class Context:
     """Device state of one fiber (bd_create / bd_step / bd_destroy)."""
 
     def __init__(self, fiber: Fiber, precision: int = PREC_FP64, use_graph: bool = False, frequency_RP: int = 1,
-                 refresh: bool = True, angles: dict | None = None, device: int = 0):
+                 refresh: bool = True, angles: dict | None = None, device: int = 0, stream: int = 0):
         self._L = load_library()
         self.fiber = fiber
         m = fiber.model_struct()
         s = fiber.state_struct(refresh, angles)
         o = bd_options(precision=precision, frequency_RP=frequency_RP, use_graph=int(use_graph), device=device,
-                       stream=None)
+                       stream=C.c_void_p(stream) if stream else None)
         self._h = C.c_void_p()
         _check(self._L.bd_create(C.byref(m), C.byref(s), C.byref(o), C.byref(self._h)))
         sz = (C.c_int * 8)()
@@ -304,6 +304,14 @@ class Context:
 
     def step_device(self, d_rr: int, d_p: int, d_energy: int = 0) -> None:
         _check(self._L.bd_step_device(self._h, C.c_void_p(d_rr), C.c_void_p(d_p), C.c_void_p(d_energy or None)))
+
+    def step_reference(self, step: int, number_of_steps: int, freq: int, rr: np.ndarray, p: np.ndarray,
+                       out: dict) -> float:
+        """main_cuda-form step: host noise in, host state copies out (bd_step_reference)."""
+        e = C.c_double()
+        _check(self._L.bd_step_reference(self._h, step, number_of_steps, freq, _pd(rr), _pd(p), C.byref(e),
+                                         *[_pd(out[k]) for k in ("r", "a", "b", "c", "r_t", "r_lh")]))
+        return e.value
 
     def forces(self) -> dict:
         n, nt, nl = self.n, self.n_tail, self.n_LH

@@ -148,8 +148,7 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
   L += 2;
   record(c, 3);
-  bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
-  L += 9;
+  L += bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
   record(c, 4);
   bdk::rotate_translate(M, c->X, c->Y, c->F0, d_rr, c->rd, c->r_all, c->precision, st);
   L += 2;
@@ -157,8 +156,7 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   bdk::frames(M, c->Y, st);
   L++;
   record(c, 6);
-  bdk::forces(M, c->Y, c->F1, c->S, c->precision, st);
-  L += 9;
+  L += bdk::forces(M, c->Y, c->F1, c->S, c->precision, st);
   record(c, 7);
   bdk::average_forces(M, c->F0, c->F1, c->Fa, st);
   bdk::rotate_translate(M, c->X, c->Y, c->Fa, d_rr, c->rd, c->r_all, c->precision, st);
@@ -430,7 +428,11 @@ static int run_step(bd_ctx* c, const double* d_rr, const double* d_p) {
 
 extern "C" int bd_step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* d_energy) {
   if (!c || !d_rr || !d_p) return set_error(BD_ERR_ARG, "bd_step_device: null argument");
-  int rc = run_step(c, d_rr, d_p);
+  // stage the noise into the context's buffers so a captured graph can replay
+  if (d_rr != c->rr)
+    CK(cudaMemcpyAsync(c->rr, d_rr, 3 * (size_t)c->M.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  if (d_p != c->p) CK(cudaMemcpyAsync(c->p, d_p, (size_t)c->m * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  int rc = run_step(c, c->rr, c->p);
   if (rc) return rc;
   if (d_energy) CK(cudaMemcpyAsync(d_energy, c->F0.E, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   return BD_OK;

@@ -111,7 +111,8 @@ void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const D
 void average_forces(const DevModel& M, const DevForces& A, const DevForces& B, DevForces& out, cudaStream_t st);
 void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream_t st);
 // forces.cu
-void forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);
+// returns the number of kernels launched
+int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);
 // rpy_chol.cu
 void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
                   cudaStream_t st);

@@ -781,7 +781,7 @@ __global__ void k_energy(int n0, const double* e0, double* E) {
 
 namespace bdk {
 
-void forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mixed, cudaStream_t st) {
+int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mixed, cudaStream_t st) {
   (void)mixed;
   // energy layout in S.ebuf: [0,n) chain, [n, n+n_tail) tails, then LH
   double* Ech = S.ebuf;
@@ -790,18 +790,22 @@ void forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int m
   double* Ebond = S.ebuf + M.n + M.n_tail + M.n_LH;  // [n] bonded shares
   double* Fm = S.ebuf + 2 * M.n + M.n_tail + M.n_LH; // [3n]
   double* Tm = Fm + 3 * M.n;                          // [3n]
-  if (M.n_lhcore > 0) k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X);
+  int L = 0;
+  if (M.n_lhcore > 0) { k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X); L++; }
   k_chain_bonded<<<cdiv(M.n, 128), 128, 0, st>>>(M, X, Fm, Tm, Ebond);
+  L++;
   if (M.n_c > 1) {
     size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
     k_core_core<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+    L++;
   }
-  if (M.n_dna > 0 && M.n_c > 0) k_dna_core<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc);
-  if (M.n_lhcore > 0) k_ghead_core<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc);
-  if (M.n_tail > 0) k_tail_gather<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et);
-  if (M.n_LH > 0) k_lh_gather<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El);
+  if (M.n_dna > 0 && M.n_c > 0) { k_dna_core<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc); L++; }
+  if (M.n_lhcore > 0) { k_ghead_core<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc); L++; }
+  if (M.n_tail > 0) { k_tail_gather<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et); L++; }
+  if (M.n_LH > 0) { k_lh_gather<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El); L++; }
   k_chain_gather<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
   k_energy<<<1, 256, 0, st>>>(M.n + M.n_tail + M.n_LH, S.ebuf, out.E);
+  return L + 2;
 }
 
 }  // namespace bdk

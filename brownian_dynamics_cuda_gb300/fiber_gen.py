@@ -25,11 +25,12 @@ Model choices (the configurations leave them open):
   * linker histone N0-G6-C22: six globular-head sites near the dyad and a
     22-bead C-terminal chain leaving the last head site; with
     `lh_charge_range=(0, 1)` every LH site charge is drawn U[0, 1];
-  * geometry: two-start zigzag - consecutive linkers cross the fiber axis
-    with a 36 degree twist per nucleosome and a small rise, each linker
-    direction perturbed by a random bend of up to 10 degrees; linker beads sit
-    3 nm apart between the exit site of one core and the entry site of the
-    next (the first_coord/second_coord sites of func.cpp:687-723).
+  * geometry: two-column zigzag - consecutive cores on opposite sides of
+    the fiber axis with 36 degrees of twist per nucleosome, the rise chosen
+    so each linker's beads sit about 3 nm apart between the exit site of one
+    core and the entry site of the next (the first_coord/second_coord sites
+    of func.cpp:687-723), random bends and frame jitter of up to 10 degrees;
+    the construction is checked for charge-site clashes.
 """
 from __future__ import annotations
 
@@ -158,86 +159,128 @@ def _lh_template(rng, lh_range):
     return g, c, qg, qc
 
 
-def build_geometry(spec: FiberSpec, rng):
-    """Bead list [(pos, a, b, c, type)] of the zigzag chain.
+def _core_frame(toward, rng):
+    """Core frame with its disk roughly horizontal (c ~ -z, jittered by up to
+    10 degrees) and its exit site (second_coord: r - ro b - d1 c) on the rim
+    facing `toward` (a horizontal direction)."""
+    tilt = math.radians(rng.uniform(-10.0, 10.0))
+    axis = _unit(np.cross([0.0, 0.0, 1.0], rng.normal(size=3)))
+    c = _rot(axis, tilt) @ np.array([0.0, 0.0, -1.0])
+    b = -toward
+    b = _unit(b - np.dot(b, c) * c)
+    a = np.cross(b, c)
+    return a, b, c
 
-    Each linker leaves its core along a zigzag direction (crossing the fiber
-    axis, +36 degrees per nucleosome, small rise) and bends by up to 10
-    degrees at every bead; the next core is placed so that its entry site
-    (first_coord, func.cpp:687-709) is one bond length past the last bead.
-    Core frames are tilted 20 degrees off the exit direction so that no exit
-    angle is exactly zero (func.cpp:1228 divides by its sine).
+
+def build_geometry(spec: FiberSpec, rng, sites=None):
+    """Bead list [(pos, a, b, c, type)] of a two-column zigzag fiber.
+
+    Core k sits at azimuth k * 216 degrees (consecutive cores on opposite
+    sides of the fiber axis, 36 degrees of twist per nucleosome) at radius
+    6 nm, its disk about horizontal and its exit site facing the next core;
+    the rise to the next core (at least 9 nm) is solved so that its entry
+    site (first_coord, func.cpp:687-709) lies (w + 1) * 3 nm from this
+    core's exit site (second_coord, :711-723), w being the linker's bead
+    count, and the w linker beads are spaced evenly on that segment with a
+    random bend of up to 10 degrees.  The reference's core/core and DNA/core
+    Lennard-Jones terms are not clamped (func.cpp:1401-1422, 1535-1561), so
+    the construction is checked: no two cores' charge sites closer than
+    2.5 nm, no linker bead closer than 3.0 nm to the sites of a core it
+    interacts with.  A violation raises.
     """
-    beads = []
-    rise = 1.1
+    if sites is None:
+        sites = np.zeros((1, 3))
+    R, DZ_MIN = 6.0, 9.0
+    beads, cores, frames = [], [], []
 
-    def zigzag(k):
-        psi = k * math.radians(180.0 + 36.0)
-        return _unit(np.array([math.cos(psi), math.sin(psi), rise / 10.0]))
+    def centre(k, z):
+        psi = math.radians(216.0 * k)
+        return np.array([R * math.cos(psi), R * math.sin(psi), z])
 
-    def bend(u):
-        ang = math.radians(rng.uniform(-10.0, 10.0))
-        axis = _unit(np.cross(u, rng.normal(size=3)))
-        return _unit(_rot(axis, ang) @ u)
+    def horiz(v):
+        v = np.array([v[0], v[1], 0.0])
+        return _unit(v)
 
-    u_in = bend(zigzag(-1))
-    last = None
-    cores = []
+    z = 0.0
+    r = centre(0, 0.0)
+    a, b, c = _core_frame(horiz(centre(1, 0.0) - r), rng)
     for k in range(spec.n_nuc):
-        # draw this nucleosome and its linker; re-draw (bounded) while it
-        # clashes with earlier cores
-        for attempt in range(256):
-            u_out = bend(zigzag(k))
-            nrm = np.cross(u_out, u_in)
-            nrm = _unit(nrm if np.linalg.norm(nrm) > 1e-6 else np.cross(u_out, [0.0, 0.0, 1.0]))
-            a = _unit(_rot(nrm, math.radians(20.0)) @ u_out)
-            b = _unit(u_in - np.dot(u_in, a) * a)
-            c = np.cross(a, b)
-            if last is None:
-                r = np.zeros(3)
-            else:
-                entry = last + LO * u_in
-                bm = -math.sin(THETA) * a + math.cos(THETA) * b
-                r = entry + RO * bm - D1 * c
-            w = linker_beads(spec.linker_bp[k])
-            d = r - (RO * b + D1 * c)
-            u = u_out
-            lk = []
-            for q in range(w):
-                if q > 0:
-                    u = bend(u)
-                d = d + LO * u
-                bb = _unit(np.cross(u, c) if abs(np.dot(u, c)) < 0.99 else np.cross(u, b))
-                lk.append((d.copy(), u.copy(), bb, np.cross(u, bb), 0))
-            ok = True
-            if cores:
-                prev = np.array(cores)
-                ok = np.linalg.norm(prev - r, axis=1).min() >= 9.5
-                if ok and len(cores) > 1:
-                    pts = np.array([x[0] for x in lk])
-                    ok = np.linalg.norm(pts[:, None] - prev[None, :-1], axis=-1).min() >= 5.5
-            if ok:
-                break
-            u_in = bend(u_in)
         beads.append((r.copy(), a, b, c, 1))
-        beads.extend(lk)
-        cores.append(r.copy())
-        last = d
-        u_in = bend(u)
+        cores.append(r)
+        frames.append((a, b, c))
+        w = linker_beads(spec.linker_bp[k])
+        exit_ = r - (RO * b + D1 * c)
+        r2_xy = centre(k + 1, 0.0)
+        a2, b2, c2 = _core_frame(horiz(centre(k + 2, 0.0) - r2_xy), rng)
+        bm2 = -math.sin(THETA) * a2 + math.cos(THETA) * b2
+        want = LO * (w + 1)
+
+        def entry_at(dz):
+            return centre(k + 1, z + dz) - RO * bm2 + D1 * c2
+
+        lo_, hi_ = DZ_MIN, 80.0
+        if np.linalg.norm(entry_at(lo_) - exit_) < want:
+            for _ in range(80):
+                mid = 0.5 * (lo_ + hi_)
+                if np.linalg.norm(entry_at(mid) - exit_) < want:
+                    lo_ = mid
+                else:
+                    hi_ = mid
+        dz = lo_
+        entry = entry_at(dz)
+        seg = entry - exit_
+        u = _unit(seg)
+        side = _unit(np.cross(u, [0.0, 0.0, 1.0]) if abs(u[2]) < 0.99 else np.cross(u, [1.0, 0.0, 0.0]))
+        for q in range(1, w + 1):
+            frac = q / (w + 1)
+            bulge = math.sin(math.pi * frac) * math.tan(math.radians(rng.uniform(-10.0, 10.0))) * np.linalg.norm(seg) / 4
+            p = exit_ + frac * seg + bulge * side
+            bb = _unit(np.cross(u, c) if abs(np.dot(u, c)) < 0.99 else np.cross(u, b))
+            beads.append((p, u.copy(), bb, np.cross(u, bb), 0))
+        z += dz
+        r = centre(k + 1, z)
+        a, b, c = a2, b2, c2
+    _check_clashes(beads, cores, frames, sites)
     return beads
+
+
+def _check_clashes(beads, cores, frames, sites):
+    cores = np.array(cores)
+    site_sets = [cores[j] + sites @ np.array(frames[j]) for j in range(len(cores))]
+    typ = [bd[4] for bd in beads]
+    core_index = np.cumsum(typ) - 1
+    for j in range(len(cores)):
+        for i in range(j + 1, len(cores)):
+            if np.linalg.norm(cores[i] - cores[j]) > 14.0:
+                continue
+            dmin = np.sqrt(((site_sets[i][:, None] - site_sets[j][None]) ** 2).sum(-1)).min()
+            if dmin < 2.5:
+                raise RuntimeError(f"fiber_gen: cores {j} and {i} clash ({dmin:.2f} nm between sites)")
+    n = len(beads)
+    for bi, bd in enumerate(beads):
+        if bd[4] != 0:
+            continue
+        if beads[bi - 1][4] == 1 or (bi + 1 < n and beads[bi + 1][4] == 1):
+            continue  # next to a core: no DNA/core interaction (func.cpp:1316-1323)
+        for j in range(len(cores)):
+            if np.linalg.norm(cores[j] - bd[0]) > 14.0:
+                continue
+            dmin = np.sqrt(((site_sets[j] - bd[0]) ** 2).sum(-1)).min()
+            if dmin < 3.0:
+                raise RuntimeError(f"fiber_gen: linker bead {bi} is {dmin:.2f} nm from core {j}")
 
 
 def write_fiber(spec: FiberSpec, directory: str) -> dict:
     """Writes the six reference input files; returns the file names for Fiber.load."""
     os.makedirs(directory, exist_ok=True)
     rng = np.random.default_rng(spec.seed)
-    beads = build_geometry(spec, rng)
+    pos, q = _core_sites(rng, spec.n_sites)
+    beads = build_geometry(spec, rng, pos)
     with open(os.path.join(directory, "data_mod"), "w") as f:
         for p, a, b, c, t in beads:
             f.write(f"{p[0]:20.13f}{p[1]:20.13f}{p[2]:20.13f}  {t}\n")
             for v in (a, b, c):
                 f.write(f"{v[0]:20.13f}{v[1]:20.13f}{v[2]:20.13f}\n")
-    pos, q = _core_sites(rng, spec.n_sites)
     with open(os.path.join(directory, "core_data"), "w") as f:
         for p in pos * 10.0:
             f.write(f"{p[0]: .7e} {p[1]: .7e} {p[2]: .7e}\n")

@@ -1051,6 +1051,19 @@ extern "C" int orc_cholesky(int m, const double* D, double* L, int nthreads) {
   return neg;
 }
 
+// Diffusion_Tensor's assembly part alone (func.cpp:737-804) for nD beads,
+// row-major m x m; used to time a bounded CPU sample of the step.
+extern "C" void orc_rpy(int nD, const double* r, const double* rad, double a1, double a2, double* D) {
+  System S;
+  S.n_D = nD;
+  S.a1 = a1;
+  S.a2 = a2;
+  S.rad_all.assign(rad, rad + nD);
+  Vec ra(r, r + 3 * nD), Dv;
+  rpy(S, ra, Dv);
+  memcpy(D, Dv.data(), sizeof(double) * Dv.size());
+}
+
 namespace {
 template <class T>
 std::vector<T> copyv(const T* p, int cnt) {

@@ -64,6 +64,9 @@ int orc_set(void* h, const char* name, const double* in);
 // number of negative pivots that were replaced by their absolute value.
 int orc_cholesky(int m, const double* D, double* L, int nthreads);
 
+// RPY assembly alone (func.cpp:737-804) for nD beads, row-major 3nD x 3nD.
+void orc_rpy(int nD, const double* r, const double* rad, double a1, double a2, double* D);
+
 // MT19937 + polar Box-Muller noise in the reference order (mt.cpp,
 // utilities.cpp:304-336, main.cpp:386-388,479-486).
 void* orc_noise_create(unsigned long seed);

@@ -53,6 +53,7 @@ def lib() -> C.CDLL:
         L.orc_get.argtypes = [C.c_void_p, C.c_char_p, _dp]
         L.orc_set.argtypes = [C.c_void_p, C.c_char_p, _dp]
         L.orc_cholesky.argtypes = [C.c_int, _dp, _dp, C.c_int]
+        L.orc_rpy.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]
         L.orc_noise_create.restype = C.c_void_p
         L.orc_noise_create.argtypes = [C.c_ulong]
         L.orc_noise_destroy.argtypes = [C.c_void_p]
@@ -135,6 +136,14 @@ def cholesky(D: np.ndarray, nthreads: int = 1) -> tuple[np.ndarray, int]:
     Lm = np.zeros_like(D)
     neg = lib().orc_cholesky(D.shape[0], D.ctypes.data_as(_dp), Lm.ctypes.data_as(_dp), nthreads)
     return Lm, neg
+
+
+def rpy(r_all: np.ndarray, rad: np.ndarray, a1: float, a2: float) -> np.ndarray:
+    """RPY tensor assembly (func.cpp:737-804), row-major."""
+    nD = rad.size
+    D = np.zeros((3 * nD, 3 * nD))
+    lib().orc_rpy(nD, _pd(r_all), _pd(rad), a1, a2, D.ctypes.data_as(_dp))
+    return D
 
 
 class OracleNoise:
