@@ -30,6 +30,7 @@ UNITS = [
     ("k_frames.cu", ["-fmad=false"]),
     ("k_forces.cu", ["-fmad=false"]),
     ("k_rpy_chol.cu", ["-fmad=false"]),
+    ("k_tc_chol.cu", []),
 ]
 
 

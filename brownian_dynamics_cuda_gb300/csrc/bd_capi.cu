@@ -81,8 +81,12 @@ struct bd_ctx {
   DevForces F0{}, F1{}, Fa{};
   DevScratch S{};
   void* arena_base = nullptr;
-  double* A = nullptr;   // m x lda, column-major; holds D then L
-  int m = 0, lda = 0;
+  double* A = nullptr;   // m x lda, column-major; holds D then L (FP64 path)
+  float* A32 = nullptr;  // mixed path: FP32 storage, leading dim lda32
+  unsigned char* PS = nullptr;  // mixed path: BF16 panel slices
+  float* W = nullptr;           // mixed path: inverse of the diagonal block
+  int* d_err = nullptr;         // device error code of the tensor-core kernels
+  int m = 0, lda = 0, lda32 = 0;
   double *r_all = nullptr, *rd = nullptr, *p = nullptr, *rr = nullptr, *rd_part = nullptr, *energy = nullptr;
   int* negpiv = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -135,17 +139,21 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   bdk::gather_rall(M, c->X, c->r_all, st);
   L++;
   bool rebuild = (c->step_count % c->freq_rp) == 0;
+  const bool mixed = c->precision == BD_PREC_MIXED;
   if (rebuild) {
-    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st);
+    if (mixed) bdk::rpy_assemble32(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A32, c->lda32, st);
+    else bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st);
     L++;
   }
   record(c, 1);
   if (rebuild) {
     CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
-    L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
+    if (mixed) L += bdk::potrf_mixed(c->m, c->A32, c->lda32, c->PS, c->W, c->negpiv, c->d_err, st);
+    else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
   }
   record(c, 2);
-  bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
+  if (mixed) bdk::trmv32(c->m, c->A32, c->lda32, d_p, M.s2dt, c->rd, c->rd_part, st);
+  else bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
   L += 2;
   record(c, 3);
   L += bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
@@ -282,8 +290,23 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   addD(3 * (size_t)M.n_D); addD(c->m); addD(c->m); addD(3 * n); addD(bdk::trmv_scratch_doubles(c->m)); addD(1); addI(1);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
-  e = cudaMalloc((void**)&c->A, (size_t)c->m * c->lda * sizeof(double));
-  if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
+  if (c->precision == BD_PREC_MIXED) {
+    if (bdk::set_mixed_attributes()) return fail(set_error(BD_ERR_CUDA, "bd_create: kernel attributes (shared memory)"));
+    c->lda32 = bdk::mixed_pad(c->m);
+    e = cudaMalloc((void**)&c->A32, (size_t)c->lda32 * c->lda32 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->PS, bdk::mixed_panel_bytes(c->m));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->W, 128 * 128 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
+    if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
+    if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
+        cudaMemset(c->A32, 0, (size_t)c->lda32 * c->lda32 * sizeof(float)) != cudaSuccess)
+      return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
+  } else if (c->precision == BD_PREC_FP64) {
+    e = cudaMalloc((void**)&c->A, (size_t)c->m * c->lda * sizeof(double));
+    if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
+  } else {
+    return fail(set_error(BD_ERR_ARG, "bd_create: unknown precision"));
+  }
   Arena ar{(char*)c->arena_base, tot, 0};
   int *d_type = ar.take<int>(n), *d_core_rank = ar.take<int>(n), *d_core_bead = ar.take<int>(nc),
       *d_dna_bead = ar.take<int>(ndna), *d_lhcb = ar.take<int>(nlhc), *d_core_lh = ar.take<int>(nc);
@@ -355,6 +378,13 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
       (rc = up(c->X.c, s->c, 3 * n, st)) || (rc = up(c->X.r_t, s->r_t, 3 * nt, st)) ||
       (rc = up(c->X.r_lh, s->r_lh, 3 * nL, st)))
     return fail(rc);
+  // angle slots the reference never writes (the last bead's) read as zero
+  for (DevState* D : {&c->X, &c->Y})
+    if (cudaMemsetAsync(D->alpha, 0, n * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(D->beta, 0, n * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(D->gamma, 0, n * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(D->length, 0, n * sizeof(double), st) != cudaSuccess)
+      return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
   if (cudaMemsetAsync(c->X.alpha_p, 0, nc * sizeof(double), st) != cudaSuccess ||
       cudaMemsetAsync(c->X.gamma_p, 0, nc * sizeof(double), st) != cudaSuccess ||
       cudaMemsetAsync(c->Y.alpha_p, 0, nc * sizeof(double), st) != cudaSuccess ||
@@ -388,6 +418,10 @@ extern "C" int bd_destroy(bd_ctx* c) {
   for (int k = 0; k < 10; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->A) cudaFree(c->A);
+  if (c->A32) cudaFree(c->A32);
+  if (c->PS) cudaFree(c->PS);
+  if (c->W) cudaFree(c->W);
+  if (c->d_err) cudaFree(c->d_err);
   if (c->arena_base) cudaFree(c->arena_base);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -445,8 +479,11 @@ extern "C" int bd_step(bd_ctx* c, const double* rr, const double* p, double* ene
   int rc = run_step(c, c->rr, c->p);
   if (rc) return rc;
   double e = 0.0;
+  int derr = 0;
   CK(cudaMemcpyAsync(&e, c->F0.E, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (c->d_err) CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (derr) return set_error(BD_ERR_CUDA, "bd_step: a tensor-core kernel timed out waiting on its copies/MMAs");
   if (!std::isfinite(e)) return set_error(BD_ERR_NONFINITE, "bd_step: non-finite energy");
   if (energy) *energy = e;
   return BD_OK;
@@ -487,10 +524,20 @@ extern "C" int bd_forces(bd_ctx* c, double* F, double* T, double* tF, double* lF
 }
 
 static int copy_lower(bd_ctx* c, double* out, bool mirror) {
-  std::vector<double> h((size_t)c->m * c->lda);
-  CK(cudaMemcpyAsync(h.data(), c->A, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  const int m = c->m, lda = c->lda;
+  std::vector<double> h;
+  int lda = c->lda;
+  if (c->precision == BD_PREC_MIXED) {
+    lda = c->lda32;
+    std::vector<float> f((size_t)c->m * lda);
+    CK(cudaMemcpyAsync(f.data(), c->A32, f.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    h.assign(f.begin(), f.end());
+  } else {
+    h.resize((size_t)c->m * c->lda);
+    CK(cudaMemcpyAsync(h.data(), c->A, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  const int m = c->m;
   for (int i = 0; i < m; i++)
     for (int j = 0; j < m; j++) {
       double v;
@@ -501,19 +548,33 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
   return BD_OK;
 }
 
+static void assemble_now(bd_ctx* c) {
+  bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
+  if (c->precision == BD_PREC_MIXED)
+    bdk::rpy_assemble32(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A32, c->lda32, c->stream);
+  else
+    bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+}
+
 extern "C" int bd_diffusion_tensor(bd_ctx* c, double* D) {
   if (!c || !D) return set_error(BD_ERR_ARG, "bd_diffusion_tensor: null argument");
-  bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
-  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+  assemble_now(c);
   CK(cudaGetLastError());
   return copy_lower(c, D, true);
 }
 
 static int factor_now(bd_ctx* c) {
-  bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
-  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+  assemble_now(c);
   CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
-  bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, c->stream);
+  if (c->precision == BD_PREC_MIXED) {
+    bdk::potrf_mixed(c->m, c->A32, c->lda32, c->PS, c->W, c->negpiv, c->d_err, c->stream);
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (derr) return set_error(BD_ERR_CUDA, "factor: a tensor-core kernel timed out");
+  } else {
+    bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, c->stream);
+  }
   CK(cudaGetLastError());
   return BD_OK;
 }
@@ -530,7 +591,8 @@ extern "C" int bd_noise_displacement(bd_ctx* c, const double* p, double* rd) {
   int rc = factor_now(c);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
+  if (c->precision == BD_PREC_MIXED) bdk::trmv32(c->m, c->A32, c->lda32, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
+  else bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
   CK(cudaMemcpyAsync(rd, c->rd, (size_t)c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return BD_OK;

@@ -1,0 +1,358 @@
+// Mixed-precision Cholesky of the RPY tensor on the sm_103a tensor cores.
+//
+// Right-looking blocked factorisation with 128-wide panels on an FP32
+// column-major matrix:
+//   k_diag32    FP32 Cholesky of the 128 x 128 diagonal block in shared
+//               memory (a negative pivot is replaced by its absolute value
+//               and counted, as func.cpp:827-833 does) and the inverse of the
+//               factor, W = L_kk^-1.
+//   k_panel32   L_ik = A_ik W^T for every 128-row tile below the block (FP32
+//               SIMT), written back and split into three BF16 slices
+//               (hi + mid + lo = the FP32 value exactly), stored pre-swizzled
+//               in the 128-byte-swizzle K-major layout the MMA reads.
+//   k_tc_syrk   trailing update A_IJ -= L_I L_J^T of one 128 x 128 tile per
+//               CTA: both operands' slices are brought into shared memory by
+//               bulk-async copies, six BF16 products (hi.hi, hi.mid, mid.hi,
+//               hi.lo, mid.mid, lo.hi) accumulate in one FP32 tensor-memory
+//               accumulator (tcgen05.mma, M = N = 128, K = 16 per
+//               instruction), and the epilogue reads the accumulator with
+//               tcgen05.ld and updates the FP32 tile.  The dropped products
+//               are below 2^-24 of the kept ones: FP32-class accuracy.
+// Every mbarrier wait is bounded; on a timeout the kernel records an error
+// code, frees its tensor memory and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "bd_internal.h"
+#include "dev_physics.cuh"
+#include "sm100_ptx.cuh"
+
+namespace {
+
+constexpr int kT = 128;                 // tile / panel width
+constexpr int kSliceBytes = kT * kT * 2;  // one BF16 slice of a 128 x 128 tile (two 64-column halves)
+constexpr int kHalfBytes = kSliceBytes / 2;
+constexpr int kTileSlices = 3;
+constexpr int kTileBytes = kTileSlices * kSliceBytes;  // 96 KB per 128-row panel tile
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// byte offset of element (row r, column k) inside one pre-swizzled slice
+__device__ __forceinline__ uint32_t swz_off(int r, int k) {
+  int half = k >> 6, kk = k & 63;
+  return half * kHalfBytes + (r >> 3) * 1024 + (r & 7) * 128 + ((((kk >> 3) ^ (r & 7)) & 7) << 4) + (kk & 7) * 2;
+}
+
+// ------------------------------------------------------------ RPY (FP32 storage)
+__global__ void __launch_bounds__(256) k_rpy32(int nD, const double* __restrict__ r, const double* __restrict__ rad,
+                                               double a1, double a2, float* __restrict__ A, int lda) {
+  using namespace bdp;
+  int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj > bi) return;
+  int i = bi * 32 + threadIdx.x;
+  if (i >= nD) return;
+  V3 ri = ld3(r + 3 * i);
+  double radi = rad[i];
+  for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
+    int j = bj * 32 + jj;
+    if (j >= nD || j > i) continue;
+    if (j == i) {
+      for (int l = 0; l < 3; l++)
+        for (int k = l; k < 3; k++) A[(size_t)(3 * j + l) * lda + 3 * i + k] = (k == l) ? (float)(a1 / radi) : 0.f;
+      continue;
+    }
+    V3 rj = ld3(r + 3 * j);
+    V3 sij{ri.x - rj.x, ri.y - rj.y, ri.z - rj.z};
+    double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
+    double s = sqrt(ssq);
+    double radj = rad[j];
+    for (int l = 0; l < 3; l++) {
+      float* col = A + (size_t)(3 * j + l) * lda + 3 * i;
+      for (int k = 0; k < 3; k++) col[k] = (float)rpy_elem(sij, ssq, s, radi, radj, a1, a2, k, l);
+    }
+  }
+}
+
+// ------------------------------------------------------------ diagonal block
+__global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int kb, float* W, int* negpiv) {
+  extern __shared__ float sm32[];
+  float (*S)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);
+  float (*X)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32 + kT * (kT + 1));
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kb * kb; e += blockDim.x) {
+    int c = e / kb, rr = e - c * kb;
+    S[rr][c] = (rr >= c) ? A[(size_t)(k0 + c) * lda + k0 + rr] : 0.f;
+  }
+  __syncthreads();
+  for (int c = 0; c < kb; c++) {
+    if (tid == 0) {
+      float f = S[c][c];
+      if (f < 0.f) {
+        f = -f;
+        atomicAdd(negpiv, 1);
+      }
+      S[c][c] = sqrtf(f);
+    }
+    __syncthreads();
+    float piv = S[c][c];
+    for (int rr = c + 1 + tid; rr < kb; rr += blockDim.x) S[rr][c] = S[rr][c] / piv;
+    __syncthreads();
+    int rem = kb - c - 1;
+    for (int e = tid; e < rem * rem; e += blockDim.x) {
+      int q = e / rem, rr = e - q * rem;
+      int col = c + 1 + q, row = c + 1 + rr;
+      if (row >= col) S[row][col] = fmaf(-S[row][c], S[col][c], S[row][col]);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < kb * kb; e += blockDim.x) {
+    int c = e / kb, rr = e - c * kb;
+    if (rr >= c) A[(size_t)(k0 + c) * lda + k0 + rr] = S[rr][c];
+  }
+  // W = L^-1 (lower): column t by forward substitution, one thread per column
+  for (int t = tid; t < kT; t += blockDim.x) {
+    for (int i = 0; i < kT; i++) X[i][t] = 0.f;
+    if (t < kb) {
+      X[t][t] = 1.f / S[t][t];
+      for (int i = t + 1; i < kb; i++) {
+        float s = 0.f;
+        for (int q = t; q < i; q++) s = fmaf(S[i][q], X[q][t], s);
+        X[i][t] = -s / S[i][i];
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < kT * kT; e += blockDim.x) W[e] = X[e / kT][e % kT];  // row-major
+}
+
+// ------------------------------------------------------------ panel
+// L_ik = A_ik W^T for the 128-row tile `tile` (row0 = tile*128); writes L
+// back (FP32) and its three BF16 slices, pre-swizzled, to PS + tile*96KB.
+__global__ void __launch_bounds__(256) k_panel32(float* A, int lda, int m, int k0, int kb, const float* __restrict__ W,
+                                                 int tile0, unsigned char* PS) {
+  extern __shared__ float sm32[];
+  float (*As)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);            // [row][q]
+  float (*Ws)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32 + kT * (kT + 1));  // [c][q]
+  const int tile = tile0 + blockIdx.x;
+  const int row0 = tile * kT;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kT * kT; e += blockDim.x) {
+    int q = e / kT, rr = e - q * kT;  // column-major walk: coalesced
+    int gr = row0 + rr;
+    As[rr][q] = (gr < m && q < kb) ? A[(size_t)(k0 + q) * lda + gr] : 0.f;
+    Ws[e / kT][e % kT] = W[e];
+  }
+  __syncthreads();
+  const int tr = (tid >> 4) * 8, tc = (tid & 15) * 8;
+  float acc[8][8];
+#pragma unroll
+  for (int a = 0; a < 8; a++)
+#pragma unroll
+    for (int b = 0; b < 8; b++) acc[a][b] = 0.f;
+  for (int q = 0; q < kT; q++) {
+    float av[8], wv[8];
+#pragma unroll
+    for (int a = 0; a < 8; a++) av[a] = As[tr + a][q];
+#pragma unroll
+    for (int b = 0; b < 8; b++) wv[b] = Ws[tc + b][q];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+      for (int b = 0; b < 8; b++) acc[a][b] = fmaf(av[a], wv[b], acc[a][b]);
+  }
+  unsigned char* ps = PS + (size_t)tile * kTileBytes;
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    int c = tc + b;
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      int r = tr + a, gr = row0 + r;
+      float x = (gr < m && c < kb) ? acc[a][b] : 0.f;
+      if (gr < m && c < kb) A[(size_t)(k0 + c) * lda + gr] = x;
+      __nv_bfloat16 h = __float2bfloat16_rn(x);
+      float r1 = x - __bfloat162float(h);
+      __nv_bfloat16 md = __float2bfloat16_rn(r1);
+      float r2 = r1 - __bfloat162float(md);
+      __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+      uint32_t off = swz_off(r, c);
+      *reinterpret_cast<__nv_bfloat16*>(ps + off) = h;
+      *reinterpret_cast<__nv_bfloat16*>(ps + kSliceBytes + off) = md;
+      *reinterpret_cast<__nv_bfloat16*>(ps + 2 * kSliceBytes + off) = lo;
+    }
+  }
+}
+
+// ------------------------------------------------------------ tensor-core trailing update
+constexpr int kSyrkThreads = 128;
+constexpr size_t kSyrkSmem = 2 * (size_t)kTileBytes + 1024 + 64;
+
+__global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(float* A, int lda, int m, int kpanel, int nt,
+                                                            const unsigned char* __restrict__ PS, int* err) {
+  extern __shared__ unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  unsigned char* sA = sm;
+  unsigned char* sB = sm + kTileBytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * kTileBytes);  // [0] loads, [1] mma
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+  // tile (I, J), kpanel < J <= I < nt, from the linear block index
+  const int rel = blockIdx.x;
+  int Ip = (int)((sqrtf(8.f * (float)rel + 1.f) - 1.f) * 0.5f);
+  while ((Ip + 1) * (Ip + 2) / 2 <= rel) Ip++;
+  while (Ip * (Ip + 1) / 2 > rel) Ip--;
+  const int Jp = rel - Ip * (Ip + 1) / 2;
+  const int I = kpanel + 1 + Ip, J = kpanel + 1 + Jp;
+  const bool diag = (I == J);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    sm100::mbar_init(&bars[0], 1);
+    sm100::mbar_init(&bars[1], 1);
+    sm100::fence_mbar_init();
+  }
+  if (warp == 0) sm100::tmem_alloc(tslot, 128);
+  sm100::tc_fence_before();
+  __syncthreads();
+  sm100::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  uint32_t* okflag = tslot + 1;
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = diag ? kTileBytes : 2 * kTileBytes;
+    sm100::mbar_arrive_expect_tx(&bars[0], bytes);
+    const unsigned char* gA = PS + (size_t)I * kTileBytes;
+    const unsigned char* gB = PS + (size_t)J * kTileBytes;
+    for (int s = 0; s < kTileSlices; s++) sm100::bulk_g2s(sA + s * kSliceBytes, gA + s * kSliceBytes, kSliceBytes, &bars[0]);
+    if (!diag)
+      for (int s = 0; s < kTileSlices; s++) sm100::bulk_g2s(sB + s * kSliceBytes, gB + s * kSliceBytes, kSliceBytes, &bars[0]);
+    bool ok = sm100::mbar_wait(&bars[0], 0, kWaitLimit);
+    if (ok) {
+      sm100::tc_fence_after();
+      const unsigned char* bB = diag ? sA : sB;
+      const uint32_t idesc = sm100::idesc_bf16_f32(128, 128);
+      // (A slice, B slice) products, smallest first
+      const int pa[6] = {2, 1, 0, 1, 0, 0};
+      const int pb[6] = {0, 1, 2, 0, 1, 0};
+      uint32_t accum = 0;
+      for (int t = 0; t < 6; t++) {
+        for (int h = 0; h < 2; h++) {
+          for (int kk = 0; kk < 4; kk++) {
+            uint32_t aaddr = sm100::smem_u32(sA + pa[t] * kSliceBytes + h * kHalfBytes) + kk * 32;
+            uint32_t baddr = sm100::smem_u32(bB + pb[t] * kSliceBytes + h * kHalfBytes) + kk * 32;
+            sm100::mma_bf16(tmem, sm100::desc_kmajor_sw128(aaddr), sm100::desc_kmajor_sw128(baddr), idesc, accum);
+            accum = 1;
+          }
+        }
+      }
+      sm100::mma_commit(&bars[1]);
+    } else {
+      atomicExch(err, 1);
+      // let the copies still in flight land before the CTA exits
+      (void)sm100::mbar_wait(&bars[0], 0, kWaitLimit);
+    }
+    *okflag = ok ? 1u : 0u;
+  }
+  __syncthreads();
+  const bool loaded = *okflag != 0;
+  const bool mma_done = loaded && sm100::mbar_wait(&bars[1], 0, kWaitLimit);
+  const int all_ok = __syncthreads_and(mma_done ? 1 : 0);
+  if (all_ok) {
+    sm100::tc_fence_after();
+    const int i = 32 * warp + lane;
+    const int gi = I * kT + i;
+    for (int c = 0; c < 4; c++) {
+      float v[32];
+      sm100::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        int gj = J * kT + 32 * c + j;
+        if (gi < m && gj < m && (!diag || gi >= gj)) {
+          float* p = A + (size_t)gj * lda + gi;
+          *p = *p - v[j];
+        }
+      }
+    }
+  } else if (threadIdx.x == 0 && loaded) {
+    atomicExch(err, 2);
+  }
+  sm100::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) sm100::tmem_dealloc(tmem, 128);
+}
+
+// ------------------------------------------------------------ L p (FP32 factor)
+__global__ void __launch_bounds__(256) k_trmv32_part(int m, const float* __restrict__ A, int lda,
+                                                     const double* __restrict__ p, double s2dt,
+                                                     double* __restrict__ part, int chunk) {
+  int i = blockIdx.x * 256 + threadIdx.x;
+  int kc = blockIdx.y;
+  int k0 = kc * chunk, k1 = min(k0 + chunk, m);
+  double s = 0.0;
+  if (i < m) {
+    int kend = min(k1, i + 1);
+    for (int k = k0; k < kend; k++) s = fma((double)A[(size_t)k * lda + i], p[k], s);
+  }
+  if (i < m) part[(size_t)kc * m + i] = s2dt * s;
+}
+
+__global__ void k_trmv32_sum(int m, int nchunk, const double* __restrict__ part, double* __restrict__ rd) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunk; c++) s = s + part[(size_t)c * m + i];
+  rd[i] = s;
+}
+
+}  // namespace
+
+namespace bdk {
+
+size_t mixed_panel_bytes(int m) { return (size_t)cdiv(m, kT) * kTileBytes; }
+int mixed_pad(int m) { return cdiv(m, kT) * kT; }
+
+static bool g_attr_done = false;
+
+int set_mixed_attributes() {
+  if (g_attr_done) return 0;
+  cudaError_t e = cudaFuncSetAttribute(k_tc_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSyrkSmem);
+  if (e != cudaSuccess) return 1;
+  size_t two = 2 * (size_t)kT * (kT + 1) * sizeof(float);
+  e = cudaFuncSetAttribute(k_diag32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)two);
+  if (e != cudaSuccess) return 1;
+  e = cudaFuncSetAttribute(k_panel32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)two);
+  if (e != cudaSuccess) return 1;
+  g_attr_done = true;
+  return 0;
+}
+
+void rpy_assemble32(int nD, const double* r_all, const double* rad, double a1, double a2, float* A, int lda,
+                    cudaStream_t st) {
+  int nt = cdiv(nD, 32);
+  k_rpy32<<<dim3(nt, nt), dim3(32, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
+}
+
+// Returns the number of kernel launches.
+int potrf_mixed(int m, float* A, int lda, unsigned char* PS, float* W, int* negpiv, int* err, cudaStream_t st) {
+  const int nt = cdiv(m, kT);
+  const size_t two = 2 * (size_t)kT * (kT + 1) * sizeof(float);
+  int L = 0;
+  for (int k = 0; k < nt; k++) {
+    const int k0 = k * kT, kb = (m - k0 < kT) ? m - k0 : kT;
+    k_diag32<<<1, 256, two, st>>>(A, lda, k0, kb, W, negpiv);
+    L++;
+    const int below = nt - k - 1;
+    if (below <= 0) break;
+    k_panel32<<<below, 256, two, st>>>(A, lda, m, k0, kb, W, k + 1, PS);
+    const int pairs = below * (below + 1) / 2;
+    k_tc_syrk<<<pairs, kSyrkThreads, kSyrkSmem, st>>>(A, lda, m, k, nt, PS, err);
+    L += 2;
+  }
+  return L;
+}
+
+void trmv32(int m, const float* A, int lda, const double* p, double s2dt, double* rd, double* part, cudaStream_t st) {
+  const int chunk = 512;
+  int nchunk = cdiv(m, chunk);
+  k_trmv32_part<<<dim3(cdiv(m, 256), nchunk), 256, 0, st>>>(m, A, lda, p, s2dt, part, chunk);
+  k_trmv32_sum<<<cdiv(m, 256), 256, 0, st>>>(m, nchunk, part, rd);
+}
+
+}  // namespace bdk

@@ -38,3 +38,18 @@ def test_cfg1_step_finite_and_deterministic(cfg1):
         assert np.all(np.isfinite(x)) and np.array_equal(x, b.get(k))
     d = a.get("r") - cfg1.state["r"]
     assert 0 < np.abs(d).max() < 1.0   # nm per ps step
+
+
+def test_cfg1_mixed_vs_fp64_displacement(cfg1):
+    """At the benchmark size the mixed step's displacement stays within
+    1e-6 (relative, max norm) of the FP64 step's."""
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context, Noise
+    rr, p = Noise(77).step(0, cfg1.arrays["r_var"], cfg1.m)
+    a, b = Context(cfg1, precision=PREC_FP64), Context(cfg1, precision=PREC_MIXED)
+    a.step(rr, p)
+    b.step(rr, p)
+    assert b.negative_pivots() == 0
+    for k in ("r", "r_t", "r_lh"):
+        d64 = a.get(k) - cfg1.state[k]
+        dm = b.get(k) - cfg1.state[k]
+        assert np.abs(dm - d64).max() <= 1e-6 * np.abs(d64).max(), k

@@ -1,0 +1,63 @@
+"""Mixed-precision path (BD_PREC_MIXED): FP32 storage, FP32 diagonal blocks
+and tensor-core (tcgen05, BF16 three-way split) trailing updates.
+
+Accuracy is stated against the FP64 oracle: the factor to 1e-5 relative
+(FP32 class, |L_mixed - L| / |L|), the noise displacement rd and the step's
+displacement to 1e-6 relative (max |x - ref| / max |ref|), the bound the
+mixed step is specified to meet."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", params=golden_names())
+def case(request):
+    fib, z = load_golden(request.param)
+    return request.param, fib, z
+
+
+def test_mixed_factor_matches_fp64(case):
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
+    name, fib, z = case
+    L64 = Context(fib, precision=PREC_FP64).cholesky()
+    cm = Context(fib, precision=PREC_MIXED)
+    Lm = cm.cholesky()
+    assert cm.negative_pivots() == 0
+    assert np.all(np.triu(Lm, 1) == 0.0)
+    assert rel_err(Lm, L64) <= 1e-5
+    p = np.random.default_rng(5).normal(size=fib.m)
+    rd64 = Context(fib, precision=PREC_FP64).noise_displacement(p)
+    assert rel_err(cm.noise_displacement(p), rd64) <= 1e-6
+
+
+def test_mixed_step_displacement(case):
+    from brownian_dynamics_cuda_gb300 import PREC_MIXED, Context
+    from oracle.pyoracle import Oracle
+    name, fib, z = case
+    o = Oracle(fib)
+    c = Context(fib, precision=PREC_MIXED)
+    r0 = {k: fib.state[k] for k in ("r", "r_t", "r_lh")}
+    for s in range(int(z["steps"])):
+        rr, p = z[f"noise{s}_rr"], z[f"noise{s}_p"]
+        o.step(rr, p)
+        c.step(rr, p)
+        for k in ("r", "r_t", "r_lh"):
+            ref = o.get(k)
+            if ref.size:
+                assert rel_err(c.get(k) - r0[k], ref - r0[k]) <= 1e-6, (s, k)
+        r0 = {k: o.get(k) for k in ("r", "r_t", "r_lh")}
+        # continue both from the oracle's state so errors do not compound
+        for k in ("r", "a", "b", "c", "r_t", "r_lh"):
+            c.set(k, o.get(k))
+
+
+def test_mixed_graph_matches_eager(case):
+    from brownian_dynamics_cuda_gb300 import PREC_MIXED, Context
+    name, fib, z = case
+    a, b = Context(fib, precision=PREC_MIXED, use_graph=True), Context(fib, precision=PREC_MIXED)
+    rr, p = z["noise0_rr"], z["noise0_p"]
+    assert a.step(rr, p) == b.step(rr, p)
+    assert np.array_equal(a.get("r"), b.get("r")) and np.array_equal(a.get("r_t"), b.get("r_t"))
