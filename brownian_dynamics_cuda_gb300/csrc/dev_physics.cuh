@@ -149,4 +149,36 @@ __device__ __forceinline__ double rpy_elem(const V3& sij, double ssq, double s, 
   return (a1 / se) * (3.0 * sk * sl / (32.0 * se * sqrt(ssq)));
 }
 
+// The full 3 x 3 block (same per-element expressions as rpy_elem, shared
+// subexpressions evaluated once): out[k][l].
+__device__ __forceinline__ void rpy_block(const V3& sij, double ssq, double s, double radi, double radj, double a1,
+                                          double a2, double (&out)[3][3]) {
+  const double sv[3] = {sij.x, sij.y, sij.z};
+  if (s >= radi + radj) {
+    double f = (radi * radi + radj * radj) / ssq;
+    double f1 = 1.0 + f / 3, f2 = 1.0 - f;
+    double as = a2 / s;
+#pragma unroll
+    for (int k = 0; k < 3; k++) out[k][k] = as * (f1 + f2 * sv[k] * sv[k] / ssq);
+    double o10 = as * (f2 * sv[1] * sv[0] / ssq);
+    double o20 = as * (f2 * sv[2] * sv[0] / ssq);
+    double o21 = as * (f2 * sv[2] * sv[1] / ssq);
+    out[1][0] = out[0][1] = o10;
+    out[2][0] = out[0][2] = o20;
+    out[2][1] = out[1][2] = o21;
+    return;
+  }
+  double se = pow((radi * radi * radi + radj * radj * radj) / 2.0, 1.0 / 3);
+  double as = a1 / se;
+  double rs = sqrt(ssq);
+#pragma unroll
+  for (int k = 0; k < 3; k++) out[k][k] = as * (1.0 - 9.0 * rs / (32 * se) + 3.0 * sv[k] * sv[k] / (32.0 * se * rs));
+  double o10 = as * (3.0 * sv[1] * sv[0] / (32.0 * se * rs));
+  double o20 = as * (3.0 * sv[2] * sv[0] / (32.0 * se * rs));
+  double o21 = as * (3.0 * sv[2] * sv[1] / (32.0 * se * rs));
+  out[1][0] = out[0][1] = o10;
+  out[2][0] = out[0][2] = o20;
+  out[2][1] = out[1][2] = o21;
+}
+
 }  // namespace bdp

@@ -241,11 +241,13 @@ __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const 
     double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
     double s = sqrt(ssq);
     double radj = M.rad_all[j];
+    double Db[3][3];
+    rpy_block(sij, ssq, s, radi, radj, M.a1, M.a2, Db);
     for (int l = 0; l < 3; l++) {
       double fl = f[l];
-      s0 = s0 + M.del * rpy_elem(sij, ssq, s, radi, radj, M.a1, M.a2, 0, l) * fl;
-      s1 = s1 + M.del * rpy_elem(sij, ssq, s, radi, radj, M.a1, M.a2, 1, l) * fl;
-      s2 = s2 + M.del * rpy_elem(sij, ssq, s, radi, radj, M.a1, M.a2, 2, l) * fl;
+      s0 = s0 + M.del * Db[0][l] * fl;
+      s1 = s1 + M.del * Db[1][l] * fl;
+      s2 = s2 + M.del * Db[2][l] * fl;
     }
   }
   for (int o = 16; o > 0; o >>= 1) {

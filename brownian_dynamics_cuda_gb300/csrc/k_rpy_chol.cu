@@ -46,9 +46,11 @@ __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ 
     double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
     double s = sqrt(ssq);
     double radj = rad[j];
+    double Db[3][3];
+    rpy_block(sij, ssq, s, radi, radj, a1, a2, Db);
     for (int l = 0; l < 3; l++) {
       double* col = A + (size_t)(3 * j + l) * lda + 3 * i;
-      for (int k = 0; k < 3; k++) col[k] = rpy_elem(sij, ssq, s, radi, radj, a1, a2, k, l);
+      for (int k = 0; k < 3; k++) col[k] = Db[k][l];
     }
   }
 }

@@ -4,10 +4,9 @@
 // column-major matrix:
 //   k_diag32    FP32 Cholesky of the 128 x 128 diagonal block in shared
 //               memory (a negative pivot is replaced by its absolute value
-//               and counted, as func.cpp:827-833 does) and the inverse of the
-//               factor, W = L_kk^-1.
-//   k_panel32   L_ik = A_ik W^T for every 128-row tile below the block (FP32
-//               SIMT), written back and split into three BF16 slices
+//               and counted, as func.cpp:827-833 does).
+//   k_panel32   L_ik = A_ik L_kk^-T by forward substitution for every 128-row
+//               tile below the block (FP32), written back and split into three BF16 slices
 //               (hi + mid + lo = the FP32 value exactly), stored pre-swizzled
 //               in the 128-byte-swizzle K-major layout the MMA reads.
 //   k_tc_syrk   trailing update A_IJ -= L_I L_J^T of one 128 x 128 tile per
@@ -67,18 +66,19 @@ __global__ void __launch_bounds__(256) k_rpy32(int nD, const double* __restrict_
     double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
     double s = sqrt(ssq);
     double radj = rad[j];
+    double Db[3][3];
+    rpy_block(sij, ssq, s, radi, radj, a1, a2, Db);
     for (int l = 0; l < 3; l++) {
       float* col = A + (size_t)(3 * j + l) * lda + 3 * i;
-      for (int k = 0; k < 3; k++) col[k] = (float)rpy_elem(sij, ssq, s, radi, radj, a1, a2, k, l);
+      for (int k = 0; k < 3; k++) col[k] = (float)Db[k][l];
     }
   }
 }
 
 // ------------------------------------------------------------ diagonal block
-__global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int kb, float* W, int* negpiv) {
+__global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int kb, int* negpiv) {
   extern __shared__ float sm32[];
   float (*S)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);
-  float (*X)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32 + kT * (kT + 1));
   const int tid = threadIdx.x;
   for (int e = tid; e < kb * kb; e += blockDim.x) {
     int c = e / kb, rr = e - c * kb;
@@ -110,76 +110,54 @@ __global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int k
     int c = e / kb, rr = e - c * kb;
     if (rr >= c) A[(size_t)(k0 + c) * lda + k0 + rr] = S[rr][c];
   }
-  // W = L^-1 (lower): column t by forward substitution, one thread per column
-  for (int t = tid; t < kT; t += blockDim.x) {
-    for (int i = 0; i < kT; i++) X[i][t] = 0.f;
-    if (t < kb) {
-      X[t][t] = 1.f / S[t][t];
-      for (int i = t + 1; i < kb; i++) {
-        float s = 0.f;
-        for (int q = t; q < i; q++) s = fmaf(S[i][q], X[q][t], s);
-        X[i][t] = -s / S[i][i];
-      }
-    }
-  }
-  __syncthreads();
-  for (int e = tid; e < kT * kT; e += blockDim.x) W[e] = X[e / kT][e % kT];  // row-major
 }
 
 // ------------------------------------------------------------ panel
-// L_ik = A_ik W^T for the 128-row tile `tile` (row0 = tile*128); writes L
-// back (FP32) and its three BF16 slices, pre-swizzled, to PS + tile*96KB.
-__global__ void __launch_bounds__(256) k_panel32(float* A, int lda, int m, int k0, int kb, const float* __restrict__ W,
-                                                 int tile0, unsigned char* PS) {
+// Rows of the 128-row tile `tile` (row0 = tile*128) solve X L_kk^T = A_ik by
+// forward substitution (one thread per row, the factor in shared memory;
+// backward stable, unlike multiplying by an explicit inverse); the result
+// L_ik is written back (FP32) and split into three BF16 slices stored
+// pre-swizzled at PS + tile*96KB.
+__global__ void __launch_bounds__(128) k_panel32(float* A, int lda, int m, int k0, int kb, int tile0,
+                                                 unsigned char* PS) {
   extern __shared__ float sm32[];
-  float (*As)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);            // [row][q]
-  float (*Ws)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32 + kT * (kT + 1));  // [c][q]
+  float (*Lk)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);               // [c][q] factor
+  float (*X)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32 + kT * (kT + 1));  // [row][q]
   const int tile = tile0 + blockIdx.x;
   const int row0 = tile * kT;
   const int tid = threadIdx.x;
   for (int e = tid; e < kT * kT; e += blockDim.x) {
     int q = e / kT, rr = e - q * kT;  // column-major walk: coalesced
     int gr = row0 + rr;
-    As[rr][q] = (gr < m && q < kb) ? A[(size_t)(k0 + q) * lda + gr] : 0.f;
-    Ws[e / kT][e % kT] = W[e];
+    X[rr][q] = (gr < m && q < kb) ? A[(size_t)(k0 + q) * lda + gr] : 0.f;
+    Lk[rr][q] = (rr >= q && rr < kb && q < kb) ? A[(size_t)(k0 + q) * lda + k0 + rr] : 0.f;
   }
   __syncthreads();
-  const int tr = (tid >> 4) * 8, tc = (tid & 15) * 8;
-  float acc[8][8];
-#pragma unroll
-  for (int a = 0; a < 8; a++)
-#pragma unroll
-    for (int b = 0; b < 8; b++) acc[a][b] = 0.f;
-  for (int q = 0; q < kT; q++) {
-    float av[8], wv[8];
-#pragma unroll
-    for (int a = 0; a < 8; a++) av[a] = As[tr + a][q];
-#pragma unroll
-    for (int b = 0; b < 8; b++) wv[b] = Ws[tc + b][q];
-#pragma unroll
-    for (int a = 0; a < 8; a++)
-#pragma unroll
-      for (int b = 0; b < 8; b++) acc[a][b] = fmaf(av[a], wv[b], acc[a][b]);
-  }
-  unsigned char* ps = PS + (size_t)tile * kTileBytes;
-#pragma unroll
-  for (int b = 0; b < 8; b++) {
-    int c = tc + b;
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-      int r = tr + a, gr = row0 + r;
-      float x = (gr < m && c < kb) ? acc[a][b] : 0.f;
-      if (gr < m && c < kb) A[(size_t)(k0 + c) * lda + gr] = x;
-      __nv_bfloat16 h = __float2bfloat16_rn(x);
-      float r1 = x - __bfloat162float(h);
-      __nv_bfloat16 md = __float2bfloat16_rn(r1);
-      float r2 = r1 - __bfloat162float(md);
-      __nv_bfloat16 lo = __float2bfloat16_rn(r2);
-      uint32_t off = swz_off(r, c);
-      *reinterpret_cast<__nv_bfloat16*>(ps + off) = h;
-      *reinterpret_cast<__nv_bfloat16*>(ps + kSliceBytes + off) = md;
-      *reinterpret_cast<__nv_bfloat16*>(ps + 2 * kSliceBytes + off) = lo;
+  {
+    const int t = tid;
+    for (int c = 0; c < kb; c++) {
+      float v = X[t][c];
+      for (int q = 0; q < c; q++) v = fmaf(-X[t][q], Lk[c][q], v);
+      X[t][c] = v / Lk[c][c];
     }
+  }
+  __syncthreads();
+  unsigned char* ps = PS + (size_t)tile * kTileBytes;
+  for (int e = tid; e < kT * kT; e += blockDim.x) {
+    int c = e / kT, r = e - c * kT;
+    int gr = row0 + r;
+    bool in = gr < m && c < kb;
+    float x = in ? X[r][c] : 0.f;
+    if (in) A[(size_t)(k0 + c) * lda + gr] = x;
+    __nv_bfloat16 h = __float2bfloat16_rn(x);
+    float r1 = x - __bfloat162float(h);
+    __nv_bfloat16 md = __float2bfloat16_rn(r1);
+    float r2 = r1 - __bfloat162float(md);
+    __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+    uint32_t off = swz_off(r, c);
+    *reinterpret_cast<__nv_bfloat16*>(ps + off) = h;
+    *reinterpret_cast<__nv_bfloat16*>(ps + kSliceBytes + off) = md;
+    *reinterpret_cast<__nv_bfloat16*>(ps + 2 * kSliceBytes + off) = lo;
   }
 }
 
@@ -336,11 +314,11 @@ int potrf_mixed(int m, float* A, int lda, unsigned char* PS, float* W, int* negp
   int L = 0;
   for (int k = 0; k < nt; k++) {
     const int k0 = k * kT, kb = (m - k0 < kT) ? m - k0 : kT;
-    k_diag32<<<1, 256, two, st>>>(A, lda, k0, kb, W, negpiv);
+    k_diag32<<<1, 256, two / 2, st>>>(A, lda, k0, kb, negpiv);
     L++;
     const int below = nt - k - 1;
     if (below <= 0) break;
-    k_panel32<<<below, 256, two, st>>>(A, lda, m, k0, kb, W, k + 1, PS);
+    k_panel32<<<below, 128, two, st>>>(A, lda, m, k0, kb, k + 1, PS);
     const int pairs = below * (below + 1) / 2;
     k_tc_syrk<<<pairs, kSyrkThreads, kSyrkSmem, st>>>(A, lda, m, k, nt, PS, err);
     L += 2;
