@@ -78,6 +78,23 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
+def max_over_ranks(x: float) -> float:
+    """Max of a per-rank scalar over the process group (identity without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(ms_per_step_max: float, world: int) -> float:
+    """Whole-job replica-steps/s: every rank advances its own fiber one step."""
+    return world * 1000.0 / ms_per_step_max
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -184,13 +201,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         barrier()
         clocks = clk.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1000.0 / ms
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = replica_rate(ms, world)
     launches = ctx.launch_count() * args.steps
     # e2e: reference-facing call with host buffers (noise H2D, r_lh D2H every
     # step, full state D2H on sampling steps every 100 steps)
@@ -210,12 +222,7 @@ def run_ours(args):
         e2e_ctx.step_reference(i, 1 << 30, freq, rr_h[i], p_h[i], out)
     torch.cuda.synchronize()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     h2d = (n3 + m) * 8
     d2h = 8 + 3 * fib.sizes["n_LH"] * 8 + (4 * n3 + 3 * fib.sizes["n_tail"]) * 8 / freq
     # roofline of the dominant phase: the Cholesky factorisation, m^3/3 flops

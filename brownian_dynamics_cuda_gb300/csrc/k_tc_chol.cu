@@ -84,28 +84,22 @@ __global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int k
     int c = e / kb, rr = e - c * kb;
     S[rr][c] = (rr >= c) ? A[(size_t)(k0 + c) * lda + k0 + rr] : 0.f;
   }
-  __syncthreads();
+  // thread t owns row r = t % 128 and, of that row, the columns of parity h = t / 128
+  const int r = tid & (kT - 1), h = tid >> 7;
   for (int c = 0; c < kb; c++) {
-    if (tid == 0) {
-      float f = S[c][c];
-      if (f < 0.f) {
-        f = -f;
-        atomicAdd(negpiv, 1);
-      }
-      S[c][c] = sqrtf(f);
+    __syncthreads();
+    float d = S[c][c];
+    if (tid == 0 && d < 0.f) atomicAdd(negpiv, 1);
+    const float piv = sqrtf(fabsf(d));
+    if (h == 0 && r > c && r < kb) S[r][c] = S[r][c] / piv;
+    __syncthreads();
+    if (tid == 0) S[c][c] = piv;
+    if (r > c && r < kb) {
+      const float lrc = S[r][c];
+      for (int q = c + 1 + h; q <= r; q += 2) S[r][q] = fmaf(-lrc, S[q][c], S[r][q]);
     }
-    __syncthreads();
-    float piv = S[c][c];
-    for (int rr = c + 1 + tid; rr < kb; rr += blockDim.x) S[rr][c] = S[rr][c] / piv;
-    __syncthreads();
-    int rem = kb - c - 1;
-    for (int e = tid; e < rem * rem; e += blockDim.x) {
-      int q = e / rem, rr = e - q * rem;
-      int col = c + 1 + q, row = c + 1 + rr;
-      if (row >= col) S[row][col] = fmaf(-S[row][c], S[col][c], S[row][col]);
-    }
-    __syncthreads();
   }
+  __syncthreads();
   for (int e = tid; e < kb * kb; e += blockDim.x) {
     int c = e / kb, rr = e - c * kb;
     if (rr >= c) A[(size_t)(k0 + c) * lda + k0 + rr] = S[rr][c];
@@ -136,9 +130,16 @@ __global__ void __launch_bounds__(128) k_panel32(float* A, int lda, int m, int k
   {
     const int t = tid;
     for (int c = 0; c < kb; c++) {
-      float v = X[t][c];
-      for (int q = 0; q < c; q++) v = fmaf(-X[t][q], Lk[c][q], v);
-      X[t][c] = v / Lk[c][c];
+      float s0 = X[t][c], s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      int q = 0;
+      for (; q + 3 < c; q += 4) {
+        s0 = fmaf(-X[t][q], Lk[c][q], s0);
+        s1 = fmaf(-X[t][q + 1], Lk[c][q + 1], s1);
+        s2 = fmaf(-X[t][q + 2], Lk[c][q + 2], s2);
+        s3 = fmaf(-X[t][q + 3], Lk[c][q + 3], s3);
+      }
+      for (; q < c; q++) s0 = fmaf(-X[t][q], Lk[c][q], s0);
+      X[t][c] = ((s0 + s1) + (s2 + s3)) / Lk[c][c];
     }
   }
   __syncthreads();
@@ -236,16 +237,22 @@ __global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(float* A, int lda, 
     sm100::tc_fence_after();
     const int i = 32 * warp + lane;
     const int gi = I * kT + i;
+    const bool row_ok = gi < m;
     for (int c = 0; c < 4; c++) {
-      float v[32];
+      float old[32], v[32];
+      const int gj0 = J * kT + 32 * c;
+      // all loads of the chunk first (independent), then the subtracts and stores
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const int gj = gj0 + j;
+        const bool ok2 = row_ok && gj < m && (!diag || gi >= gj);
+        old[j] = ok2 ? A[(size_t)gj * lda + gi] : 0.f;
+      }
       sm100::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);
 #pragma unroll
       for (int j = 0; j < 32; j++) {
-        int gj = J * kT + 32 * c + j;
-        if (gi < m && gj < m && (!diag || gi >= gj)) {
-          float* p = A + (size_t)gj * lda + gi;
-          *p = *p - v[j];
-        }
+        const int gj = gj0 + j;
+        if (row_ok && gj < m && (!diag || gi >= gj)) A[(size_t)gj * lda + gi] = old[j] - v[j];
       }
     }
   } else if (threadIdx.x == 0 && loaded) {
