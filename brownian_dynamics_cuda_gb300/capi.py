@@ -100,6 +100,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_dev_potrf.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     L.bd_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.bd_launch_count.argtypes = [C.c_void_p, _ip]
+    L.bd_kernel_time.argtypes = [C.c_void_p, C.POINTER(C.c_float), _ip, _dp]
     L.bd_negative_pivots.argtypes = [C.c_void_p, _ip]
     _lib = L
     return L
@@ -348,6 +349,12 @@ class Context:
         out = (C.c_float * 9)()
         _check(self._L.bd_phase_times(self._h, out))
         return np.array(list(out))
+
+    def kernel_time(self) -> tuple[float, int, float]:
+        """(total ms, launches, tensor flop) of the tensor-core update in the last timed step."""
+        ms, n, fl = C.c_float(), C.c_int(), C.c_double()
+        _check(self._L.bd_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(fl)))
+        return ms.value, n.value, fl.value
 
     def launch_count(self) -> int:
         v = C.c_int()

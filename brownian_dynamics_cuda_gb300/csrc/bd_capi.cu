@@ -82,11 +82,9 @@ struct bd_ctx {
   DevScratch S{};
   void* arena_base = nullptr;
   double* A = nullptr;   // m x lda, column-major; holds D then L (FP64 path)
-  float* A32 = nullptr;  // mixed path: FP32 storage, leading dim lda32
   unsigned char* PS = nullptr;  // mixed path: BF16 panel slices
-  float* W = nullptr;           // mixed path: inverse of the diagonal block
   int* d_err = nullptr;         // device error code of the tensor-core kernels
-  int m = 0, lda = 0, lda32 = 0;
+  int m = 0, lda = 0;
   double *r_all = nullptr, *rd = nullptr, *p = nullptr, *rr = nullptr, *rd_part = nullptr, *energy = nullptr;
   int* negpiv = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -94,6 +92,8 @@ struct bd_ctx {
   int host_negpiv = 0;
   cudaEvent_t ev[10] = {};
   bool timing = false;
+  std::vector<cudaEvent_t> kev;   // per-launch events around the tensor-core update (timing steps only)
+  double kflop = 0.0;
   // host copies for the drop-in paths
   std::vector<int> h_type;
 };
@@ -141,19 +141,22 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   bool rebuild = (c->step_count % c->freq_rp) == 0;
   const bool mixed = c->precision == BD_PREC_MIXED;
   if (rebuild) {
-    if (mixed) bdk::rpy_assemble32(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A32, c->lda32, st);
-    else bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st);
+    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st);
     L++;
   }
   record(c, 1);
   if (rebuild) {
     CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
-    if (mixed) L += bdk::potrf_mixed(c->m, c->A32, c->lda32, c->PS, c->W, c->negpiv, c->d_err, st);
+    if (mixed) {
+      const bool kt = c->timing && !c->kev.empty();
+      c->kflop = 0.0;
+      L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, kt ? c->kev.data() : nullptr,
+                            kt ? &c->kflop : nullptr);
+    }
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
   }
   record(c, 2);
-  if (mixed) bdk::trmv32(c->m, c->A32, c->lda32, d_p, M.s2dt, c->rd, c->rd_part, st);
-  else bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
+  bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
   L += 2;
   record(c, 3);
   L += bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
@@ -290,22 +293,16 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   addD(3 * (size_t)M.n_D); addD(c->m); addD(c->m); addD(3 * n); addD(bdk::trmv_scratch_doubles(c->m)); addD(1); addI(1);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
+  if (c->precision != BD_PREC_MIXED && c->precision != BD_PREC_FP64)
+    return fail(set_error(BD_ERR_ARG, "bd_create: unknown precision"));
+  e = cudaMalloc((void**)&c->A, (size_t)c->m * c->lda * sizeof(double));
+  if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
   if (c->precision == BD_PREC_MIXED) {
     if (bdk::set_mixed_attributes()) return fail(set_error(BD_ERR_CUDA, "bd_create: kernel attributes (shared memory)"));
-    c->lda32 = bdk::mixed_pad(c->m);
-    e = cudaMalloc((void**)&c->A32, (size_t)c->lda32 * c->lda32 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->PS, bdk::mixed_panel_bytes(c->m));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->W, 128 * 128 * sizeof(float));
+    e = cudaMalloc((void**)&c->PS, bdk::mixed_panel_bytes(c->m));
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
     if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
-    if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
-        cudaMemset(c->A32, 0, (size_t)c->lda32 * c->lda32 * sizeof(float)) != cudaSuccess)
-      return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
-  } else if (c->precision == BD_PREC_FP64) {
-    e = cudaMalloc((void**)&c->A, (size_t)c->m * c->lda * sizeof(double));
-    if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
-  } else {
-    return fail(set_error(BD_ERR_ARG, "bd_create: unknown precision"));
+    if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
   }
   Arena ar{(char*)c->arena_base, tot, 0};
   int *d_type = ar.take<int>(n), *d_core_rank = ar.take<int>(n), *d_core_bead = ar.take<int>(nc),
@@ -403,6 +400,10 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
       return fail(rc);
   }
   for (int k = 0; k < 10; k++) cudaEventCreate(&c->ev[k]);
+  if (c->precision == BD_PREC_MIXED) {
+    c->kev.resize(2 * (size_t)bdk::mixed_tiles(c->m));
+    for (auto& ev : c->kev) cudaEventCreate(&ev);
+  }
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_CUDA, (std::string("bd_create: ") + cudaGetErrorString(e)).c_str()));
   e = cudaGetLastError();
@@ -417,10 +418,9 @@ extern "C" int bd_destroy(bd_ctx* c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (int k = 0; k < 10; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (auto ev : c->kev) cudaEventDestroy(ev);
   if (c->A) cudaFree(c->A);
-  if (c->A32) cudaFree(c->A32);
   if (c->PS) cudaFree(c->PS);
-  if (c->W) cudaFree(c->W);
   if (c->d_err) cudaFree(c->d_err);
   if (c->arena_base) cudaFree(c->arena_base);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -524,19 +524,10 @@ extern "C" int bd_forces(bd_ctx* c, double* F, double* T, double* tF, double* lF
 }
 
 static int copy_lower(bd_ctx* c, double* out, bool mirror) {
-  std::vector<double> h;
-  int lda = c->lda;
-  if (c->precision == BD_PREC_MIXED) {
-    lda = c->lda32;
-    std::vector<float> f((size_t)c->m * lda);
-    CK(cudaMemcpyAsync(f.data(), c->A32, f.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    h.assign(f.begin(), f.end());
-  } else {
-    h.resize((size_t)c->m * c->lda);
-    CK(cudaMemcpyAsync(h.data(), c->A, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-  }
+  const int lda = c->lda;
+  std::vector<double> h((size_t)c->m * lda);
+  CK(cudaMemcpyAsync(h.data(), c->A, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   const int m = c->m;
   for (int i = 0; i < m; i++)
     for (int j = 0; j < m; j++) {
@@ -550,10 +541,7 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
 
 static void assemble_now(bd_ctx* c) {
   bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
-  if (c->precision == BD_PREC_MIXED)
-    bdk::rpy_assemble32(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A32, c->lda32, c->stream);
-  else
-    bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
 }
 
 extern "C" int bd_diffusion_tensor(bd_ctx* c, double* D) {
@@ -567,7 +555,7 @@ static int factor_now(bd_ctx* c) {
   assemble_now(c);
   CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
   if (c->precision == BD_PREC_MIXED) {
-    bdk::potrf_mixed(c->m, c->A32, c->lda32, c->PS, c->W, c->negpiv, c->d_err, c->stream);
+    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream);
     int derr = 0;
     CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -591,8 +579,7 @@ extern "C" int bd_noise_displacement(bd_ctx* c, const double* p, double* rd) {
   int rc = factor_now(c);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  if (c->precision == BD_PREC_MIXED) bdk::trmv32(c->m, c->A32, c->lda32, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
-  else bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
+  bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
   CK(cudaMemcpyAsync(rd, c->rd, (size_t)c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return BD_OK;
@@ -667,6 +654,24 @@ extern "C" int bd_phase_times(bd_ctx* c, float* out9) {
   CK(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < 8; k++) cudaEventElapsedTime(&out9[k], c->ev[k], c->ev[k + 1]);
   cudaEventElapsedTime(&out9[8], c->ev[0], c->ev[8]);
+  return BD_OK;
+}
+
+extern "C" int bd_kernel_time(bd_ctx* c, float* total_ms, int* launches, double* tensor_flop) {
+  if (!c || !total_ms || !launches) return set_error(BD_ERR_ARG, "bd_kernel_time: null argument");
+  *total_ms = 0.f;
+  *launches = 0;
+  if (tensor_flop) *tensor_flop = c->kflop;
+  if (c->precision != BD_PREC_MIXED || !c->timing) return BD_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  const int nt = bdk::mixed_tiles(c->m);
+  for (int k = 0; k + 1 < nt; k++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->kev[2 * k], c->kev[2 * k + 1]) == cudaSuccess) {
+      *total_ms += ms;
+      (*launches)++;
+    }
+  }
   return BD_OK;
 }
 

@@ -119,14 +119,15 @@ void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, dou
 int potrf_fp64(int m, double* A, int lda, double* rd_acc, const double* p, double s2dt, int* d_negpiv,
                cudaStream_t st);
 size_t trmv_scratch_doubles(int m);
-// k_tc_chol.cu (mixed precision: FP32 storage, tcgen05 trailing updates)
+// k_tc_chol.cu (mixed precision: FP64 storage, FP32-class arithmetic, tcgen05 trailing updates)
 size_t mixed_panel_bytes(int m);
-int mixed_pad(int m);
 int set_mixed_attributes();
-void rpy_assemble32(int nD, const double* r_all, const double* rad, double a1, double a2, float* A, int lda,
-                    cudaStream_t st);
-int potrf_mixed(int m, float* A, int lda, unsigned char* PS, float* W, int* negpiv, int* err, cudaStream_t st);
-void trmv32(int m, const float* A, int lda, const double* p, double s2dt, double* rd, double* part, cudaStream_t st);
+// syrk_ev (optional): 2 events per panel recorded around each tensor-core
+// update launch; syrk_flop accumulates the tensor work those launches issue.
+int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
+                cudaEvent_t* syrk_ev = nullptr, double* syrk_flop = nullptr);
+int mixed_tiles(int m);
+
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
                    cudaStream_t st);
 }  // namespace bdk

@@ -107,6 +107,44 @@ __device__ __forceinline__ V3 pair_f1(double q1, double q2, double eps, double k
   return V3{clamp09(t * (c1.x - c2.x) / d), clamp09(t * (c1.y - c2.y) / d), clamp09(t * (c1.z - c2.z) / d)};
 }
 
+__device__ __forceinline__ float clamp09f(float v) { return fminf(fmaxf(v, -0.9f), 0.9f); }
+
+// Mixed-precision form of pair_f1 for the tensor-core step: the separation
+// is formed in FP64 (large absolute coordinates cost nothing), the rest of
+// the pair in FP32 (sqrt, exp, powers of sigma/d by multiplication), and the
+// result is widened back for FP64 accumulation.  Same formulas as pair_f1.
+template <bool DH, bool LJ>
+__device__ __forceinline__ V3 pair_f1_mx(double q1, double q2, double eps, double kappa, double kev, double sig,
+                                         const V3& c1, const V3& c2, double* E) {
+  const float dx = (float)(c1.x - c2.x), dy = (float)(c1.y - c2.y), dz = (float)(c1.z - c2.z);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const float d = sqrtf(d2);
+  float t = 0.f;
+  if (DH && d < 7.f) {
+    const float kap = (float)kappa;
+    const float qq = (float)(q1 * q2 / (4 * kPi * eps));
+    const float ex = expf(-kap * d);
+    t = qq * (kap * d + 1.f) * ex / d2;
+    if (E) *E = *E + (double)(qq * ex / d);
+  }
+  if (LJ && d < 4.f) {
+    const float sr = (float)sig / d, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+    const float kv = (float)kev;
+    t = t - kv * (6.f * sr6 - 12.f * sr12) / d;
+    if (E) *E = *E + (double)(kv * (sr12 - sr6));
+  }
+  const float w = t / d;
+  return V3{(double)clamp09f(w * dx), (double)clamp09f(w * dy), (double)clamp09f(w * dz)};
+}
+
+// Dispatch on the step's precision.
+template <bool DH, bool LJ, bool MX>
+__device__ __forceinline__ V3 pairF(double q1, double q2, double eps, double kappa, double kev, double sig,
+                                    const V3& c1, const V3& c2, double* E) {
+  if constexpr (MX) return pair_f1_mx<DH, LJ>(q1, q2, eps, kappa, kev, sig, c1, c2, E);
+  else return pair_f1<DH, LJ>(q1, q2, eps, kappa, kev, sig, c1, c2, E);
+}
+
 // func.cpp:374-394: torque about the body frame from a force at pf
 __device__ __forceinline__ V3 torque_abs(const V3& F, const V3& pf, const V3& pc, const V3& a, const V3& b,
                                          const V3& c) {
@@ -179,6 +217,31 @@ __device__ __forceinline__ void rpy_block(const V3& sij, double ssq, double s, d
   out[1][0] = out[0][1] = o10;
   out[2][0] = out[0][2] = o20;
   out[2][1] = out[1][2] = o21;
+}
+
+// FP32 form of rpy_block for the mixed-precision drift (separation given in
+// FP32, already formed in FP64).
+__device__ __forceinline__ void rpy_block_f(float sx, float sy, float sz, float radi, float radj, float a1, float a2,
+                                            float (&out)[3][3]) {
+  const float sv[3] = {sx, sy, sz};
+  const float ssq = sx * sx + sy * sy + sz * sz;
+  const float s = sqrtf(ssq);
+  if (s >= radi + radj) {
+    const float f = (radi * radi + radj * radj) / ssq;
+    const float f1 = 1.f + f / 3.f, f2 = 1.f - f;
+    const float as = a2 / s, w = as * f2 / ssq;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+      for (int l = 0; l < 3; l++) out[k][l] = w * sv[k] * sv[l] + (k == l ? as * f1 : 0.f);
+    return;
+  }
+  const float se = cbrtf((radi * radi * radi + radj * radj * radj) / 2.f);
+  const float as = a1 / se, w = as * 3.f / (32.f * se * s);
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int l = 0; l < 3; l++) out[k][l] = w * sv[k] * sv[l] + (k == l ? as * (1.f - 9.f * s / (32.f * se)) : 0.f);
 }
 
 }  // namespace bdp

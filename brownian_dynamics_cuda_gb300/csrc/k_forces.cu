@@ -251,6 +251,7 @@ __global__ void k_chain_bonded(DevModel M, DevState X, double* Fm, double* Tm, d
 // Core/core (func.cpp:1489-1566): one CTA per core pair I < J.
 constexpr int kCCThreads = 256;
 
+template <bool MX>
 __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X, double* slots) {
   extern __shared__ double sm[];
   int I = blockIdx.x, J = blockIdx.y;
@@ -279,38 +280,73 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
   const double* cq = M.core_q;
   const double ke = M.k_e, kap = M.debye, kex = M.k_ex, sg = M.sCC;
   double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
-    int k = p / Nq, l = p - k * Nq;
-    V3 pk = ld3(si_ + 3 * k), pl = ld3(sj_ + 3 * l);
-    V3 z{pk.x - pl.x, pk.y - pl.y, pk.z - pl.z};
-    double dd = sqrt(z.x * z.x + z.y * z.y + z.z * z.z);
-    double mi = 1.0 / dd;
-    z = V3{mi * z.x, mi * z.y, mi * z.z};
-    double ex = exp(-kap * dd);
-    double g1 = ke * cq[k] * cq[l] * ex * (kap * dd + 1.0) / (dd * dd);
-    v[9] = v[9] + (ke * cq[l] * cq[k] / dd) * ex;
-    double gsum[2] = {g1, 0.0};
-    int ng = 1;
-    if (dd <= 8.0) {
-      gsum[1] = kex * ((12.0 / sg) * pow((sg / dd), 13) - (6.0 / sg) * pow((sg / dd), 7));
-      v[9] = v[9] + kex * (pow(sg / dd, 12) - pow(sg / dd, 6));
-      ng = 2;
+  if constexpr (MX) {
+    const float kapf = (float)kap, kexf = (float)kex, sgf = (float)sg;
+    const float aix = (float)ai.x, aiy = (float)ai.y, aiz = (float)ai.z, bix = (float)bi.x, biy = (float)bi.y,
+                biz = (float)bi.z, cix = (float)ci.x, ciy = (float)ci.y, ciz = (float)ci.z;
+    const float ajx = (float)aj.x, ajy = (float)aj.y, ajz = (float)aj.z, bjx = (float)bj.x, bjy = (float)bj.y,
+                bjz = (float)bj.z, cjx = (float)cj.x, cjy = (float)cj.y, cjz = (float)cj.z;
+    for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
+      int k = p / Nq, l = p - k * Nq;
+      float zx = (float)(si_[3 * k] - sj_[3 * l]), zy = (float)(si_[3 * k + 1] - sj_[3 * l + 1]),
+            zz = (float)(si_[3 * k + 2] - sj_[3 * l + 2]);
+      float dd = sqrtf(zx * zx + zy * zy + zz * zz);
+      float mi = 1.f / dd;
+      zx *= mi; zy *= mi; zz *= mi;
+      float ex = expf(-kapf * dd);
+      float qkl = (float)(ke * cq[k] * cq[l]);
+      float g = qkl * ex * (kapf * dd + 1.f) / (dd * dd);
+      float e = qkl * ex / dd;
+      if (dd <= 8.f) {
+        float sr = sgf / dd, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+        g += kexf * (12.f * sr12 - 6.f * sr6) / dd;
+        e += kexf * (sr12 - sr6);
+      }
+      v[9] += (double)e;
+      v[0] += (double)(g * zx); v[1] += (double)(g * zy); v[2] += (double)(g * zz);
+      const float cpk0 = (float)cp[3 * k], cpk1 = (float)cp[3 * k + 1], cpk2 = (float)cp[3 * k + 2];
+      const float cpl0 = (float)cp[3 * l], cpl1 = (float)cp[3 * l + 1], cpl2 = (float)cp[3 * l + 2];
+      float fa = g * (aix * zx + aiy * zy + aiz * zz), fb = g * (bix * zx + biy * zy + biz * zz),
+            fc = g * (cix * zx + ciy * zy + ciz * zz);
+      v[3] += (double)(fc * cpk1 - fb * cpk2); v[4] += (double)(fa * cpk2 - fc * cpk0); v[5] += (double)(fb * cpk0 - fa * cpk1);
+      fa = -g * (ajx * zx + ajy * zy + ajz * zz); fb = -g * (bjx * zx + bjy * zy + bjz * zz);
+      fc = -g * (cjx * zx + cjy * zy + cjz * zz);
+      v[6] += (double)(fc * cpl1 - fb * cpl2); v[7] += (double)(fa * cpl2 - fc * cpl0); v[8] += (double)(fb * cpl0 - fa * cpl1);
     }
-    for (int q = 0; q < ng; q++) {
-      double gg = gsum[q];
-      v[0] = v[0] + gg * z.x; v[1] = v[1] + gg * z.y; v[2] = v[2] + gg * z.z;
-      double fa = gg * (ai.x * z.x + ai.y * z.y + ai.z * z.z);
-      double fb = gg * (bi.x * z.x + bi.y * z.y + bi.z * z.z);
-      double fc = gg * (ci.x * z.x + ci.y * z.y + ci.z * z.z);
-      v[3] = v[3] + (fc * cp[3 * k + 1] - fb * cp[3 * k + 2]);
-      v[4] = v[4] + (fa * cp[3 * k + 2] - fc * cp[3 * k]);
-      v[5] = v[5] + (fb * cp[3 * k] - fa * cp[3 * k + 1]);
-      fa = -gg * (aj.x * z.x + aj.y * z.y + aj.z * z.z);
-      fb = -gg * (bj.x * z.x + bj.y * z.y + bj.z * z.z);
-      fc = -gg * (cj.x * z.x + cj.y * z.y + cj.z * z.z);
-      v[6] = v[6] + (fc * cp[3 * l + 1] - fb * cp[3 * l + 2]);
-      v[7] = v[7] + (fa * cp[3 * l + 2] - fc * cp[3 * l]);
-      v[8] = v[8] + (fb * cp[3 * l] - fa * cp[3 * l + 1]);
+  } else {
+  for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
+      int k = p / Nq, l = p - k * Nq;
+      V3 pk = ld3(si_ + 3 * k), pl = ld3(sj_ + 3 * l);
+      V3 z{pk.x - pl.x, pk.y - pl.y, pk.z - pl.z};
+      double dd = sqrt(z.x * z.x + z.y * z.y + z.z * z.z);
+      double mi = 1.0 / dd;
+      z = V3{mi * z.x, mi * z.y, mi * z.z};
+      double ex = exp(-kap * dd);
+      double g1 = ke * cq[k] * cq[l] * ex * (kap * dd + 1.0) / (dd * dd);
+      v[9] = v[9] + (ke * cq[l] * cq[k] / dd) * ex;
+      double gsum[2] = {g1, 0.0};
+      int ng = 1;
+      if (dd <= 8.0) {
+        gsum[1] = kex * ((12.0 / sg) * pow((sg / dd), 13) - (6.0 / sg) * pow((sg / dd), 7));
+        v[9] = v[9] + kex * (pow(sg / dd, 12) - pow(sg / dd, 6));
+        ng = 2;
+      }
+      for (int q = 0; q < ng; q++) {
+        double gg = gsum[q];
+        v[0] = v[0] + gg * z.x; v[1] = v[1] + gg * z.y; v[2] = v[2] + gg * z.z;
+        double fa = gg * (ai.x * z.x + ai.y * z.y + ai.z * z.z);
+        double fb = gg * (bi.x * z.x + bi.y * z.y + bi.z * z.z);
+        double fc = gg * (ci.x * z.x + ci.y * z.y + ci.z * z.z);
+        v[3] = v[3] + (fc * cp[3 * k + 1] - fb * cp[3 * k + 2]);
+        v[4] = v[4] + (fa * cp[3 * k + 2] - fc * cp[3 * k]);
+        v[5] = v[5] + (fb * cp[3 * k] - fa * cp[3 * k + 1]);
+        fa = -gg * (aj.x * z.x + aj.y * z.y + aj.z * z.z);
+        fb = -gg * (bj.x * z.x + bj.y * z.y + bj.z * z.z);
+        fc = -gg * (cj.x * z.x + cj.y * z.y + cj.z * z.z);
+        v[6] = v[6] + (fc * cp[3 * l + 1] - fb * cp[3 * l + 2]);
+        v[7] = v[7] + (fa * cp[3 * l + 2] - fc * cp[3 * l]);
+        v[8] = v[8] + (fb * cp[3 * l] - fa * cp[3 * l + 1]);
+      }
     }
   }
   bsum<10>(v, red);
@@ -320,6 +356,7 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
 
 // DNA/core (func.cpp:1355-1488): one warp per (linker bead d, core J).
 // Slot: force on the DNA bead (3), torque on the core (3), energy.
+template <bool MX>
 __global__ void k_dna_core(DevModel M, DevState X, double* slots) {
   int lane = threadIdx.x & 31;
   int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -341,33 +378,65 @@ __global__ void k_dna_core(DevModel M, DevState X, double* slots) {
   const double* cp = M.core_pos;
   const double ke = M.k_e, kap = M.debye, kex = M.k_ex, sg = M.sDC, ql = M.q_l;
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
+  if constexpr (MX) {
+    const float kapf = (float)kap, kexf = (float)kex, sgf = (float)sg;
+    const float acx = (float)ac.x, acy = (float)ac.y, acz = (float)ac.z, bcx = (float)bc.x, bcy = (float)bc.y,
+                bcz = (float)bc.z, ccx = (float)cc.x, ccy = (float)cc.y, ccz = (float)cc.z;
+    for (int k = lane; k < M.Nq; k += 32) {
+      V3 s = body(rc, ac, bc, cc, cp + 3 * k);
+      float zx = (float)(rd_.x - s.x), zy = (float)(rd_.y - s.y), zz = (float)(rd_.z - s.z);
+      float dd = sqrtf(zx * zx + zy * zy + zz * zz);
+      float mi = 1.f / dd;
+      zx *= mi; zy *= mi; zz *= mi;
+      double q = M.core_q[k];
+      float g = 0.f, e = 0.f;
+      if (adj) {
+        float ex = expf(-kapf * dd);
+        float qq = (float)(ke * ql * q);
+        g = qq * ex * (kapf * dd + 1.f) / (dd * dd);
+        e = qq * ex / dd;
+      }
+      if (dd <= 8.f && q > 0) {
+        float sr = sgf / dd, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+        g += kexf * (12.f * sr12 - 6.f * sr6) / dd;
+        e += kexf * (sr12 - sr6);
+      }
+      v[6] += (double)e;
+      v[0] += (double)(g * zx); v[1] += (double)(g * zy); v[2] += (double)(g * zz);
+      const float c0 = (float)cp[3 * k], c1 = (float)cp[3 * k + 1], c2 = (float)cp[3 * k + 2];
+      float fa = -g * (acx * zx + acy * zy + acz * zz), fb = -g * (bcx * zx + bcy * zy + bcz * zz),
+            fc = -g * (ccx * zx + ccy * zy + ccz * zz);
+      v[3] += (double)(fc * c1 - fb * c2); v[4] += (double)(fa * c2 - fc * c0); v[5] += (double)(fb * c0 - fa * c1);
+    }
+  } else {
   for (int k = lane; k < M.Nq; k += 32) {
-    V3 s = body(rc, ac, bc, cc, cp + 3 * k);
-    V3 z{rd_.x - s.x, rd_.y - s.y, rd_.z - s.z};
-    double dd = sqrt(z.x * z.x + z.y * z.y + z.z * z.z);
-    double mi = 1.0 / dd;
-    z = V3{mi * z.x, mi * z.y, mi * z.z};
-    double q = M.core_q[k];
-    double gs[2];
-    int ng = 0;
-    if (adj) {
-      double ex = exp(-kap * dd);
-      gs[ng++] = ke * ql * q * ex * (kap * dd + 1.0) / (dd * dd);
-      v[6] = v[6] + (ke * ql * q / dd) * ex;
-    }
-    if (dd <= 8.0 && q > 0) {
-      gs[ng++] = kex * ((12.0 / sg) * pow((sg / dd), 13) - (6.0 / sg) * pow((sg / dd), 7));
-      v[6] = v[6] + kex * (pow(sg / dd, 12) - pow(sg / dd, 6));
-    }
-    for (int t = 0; t < ng; t++) {
-      double g1 = gs[t];
-      v[0] = v[0] + g1 * z.x; v[1] = v[1] + g1 * z.y; v[2] = v[2] + g1 * z.z;
-      double fa = -g1 * (ac.x * z.x + ac.y * z.y + ac.z * z.z);
-      double fb = -g1 * (bc.x * z.x + bc.y * z.y + bc.z * z.z);
-      double fc = -g1 * (cc.x * z.x + cc.y * z.y + cc.z * z.z);
-      v[3] = v[3] + (fc * cp[3 * k + 1] - fb * cp[3 * k + 2]);
-      v[4] = v[4] + (fa * cp[3 * k + 2] - fc * cp[3 * k]);
-      v[5] = v[5] + (fb * cp[3 * k] - fa * cp[3 * k + 1]);
+      V3 s = body(rc, ac, bc, cc, cp + 3 * k);
+      V3 z{rd_.x - s.x, rd_.y - s.y, rd_.z - s.z};
+      double dd = sqrt(z.x * z.x + z.y * z.y + z.z * z.z);
+      double mi = 1.0 / dd;
+      z = V3{mi * z.x, mi * z.y, mi * z.z};
+      double q = M.core_q[k];
+      double gs[2];
+      int ng = 0;
+      if (adj) {
+        double ex = exp(-kap * dd);
+        gs[ng++] = ke * ql * q * ex * (kap * dd + 1.0) / (dd * dd);
+        v[6] = v[6] + (ke * ql * q / dd) * ex;
+      }
+      if (dd <= 8.0 && q > 0) {
+        gs[ng++] = kex * ((12.0 / sg) * pow((sg / dd), 13) - (6.0 / sg) * pow((sg / dd), 7));
+        v[6] = v[6] + kex * (pow(sg / dd, 12) - pow(sg / dd, 6));
+      }
+      for (int t = 0; t < ng; t++) {
+        double g1 = gs[t];
+        v[0] = v[0] + g1 * z.x; v[1] = v[1] + g1 * z.y; v[2] = v[2] + g1 * z.z;
+        double fa = -g1 * (ac.x * z.x + ac.y * z.y + ac.z * z.z);
+        double fb = -g1 * (bc.x * z.x + bc.y * z.y + bc.z * z.z);
+        double fc = -g1 * (cc.x * z.x + cc.y * z.y + cc.z * z.z);
+        v[3] = v[3] + (fc * cp[3 * k + 1] - fb * cp[3 * k + 2]);
+        v[4] = v[4] + (fa * cp[3 * k + 2] - fc * cp[3 * k]);
+        v[5] = v[5] + (fb * cp[3 * k] - fa * cp[3 * k + 1]);
+      }
     }
   }
   for (int q = 0; q < 7; q++) v[q] = wsum(v[q]);
@@ -379,6 +448,7 @@ __global__ void k_dna_core(DevModel M, DevState X, double* slots) {
 // (func.cpp:2524-2586): one warp per (I, L).  Slot: force on I (3), torque
 // on I (3), torque on L (3), energy.  Pairs beyond the 7 nm cut-off add
 // exact zeros, so far object pairs are skipped.
+template <bool MX>
 __global__ void k_ghead_core(DevModel M, DevState X, double* slots) {
   int lane = threadIdx.x & 31;
   int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -401,7 +471,7 @@ __global__ void k_ghead_core(DevModel M, DevState X, double* slots) {
     int jm = p / Nq, m = p - jm * Nq;
     V3 g = ld3(X.gpos + 3 * (I * ng + jm));
     V3 z = body(rl, al, bl, cl, M.core_pos + 3 * m);
-    V3 f1 = pair_f1<true, true>(M.LH_q[jm], M.core_q[m], eps, M.debye, M.k_ex, M.LH_vdw_hc[jm], g, z, &v[9]);
+    V3 f1 = pairF<true, true, MX>(M.LH_q[jm], M.core_q[m], eps, M.debye, M.k_ex, M.LH_vdw_hc[jm], g, z, &v[9]);
     V3 f2{-f1.x, -f1.y, -f1.z};
     v[0] = v[0] + f1.x; v[1] = v[1] + f1.y; v[2] = v[2] + f1.z;
     V3 t1 = torque_rel(f1, M.LH_g_pos + 3 * jm, ai, bi, ci);
@@ -420,6 +490,7 @@ __global__ void k_ghead_core(DevModel M, DevState X, double* slots) {
 // energy share.
 constexpr int kGatherThreads = 256;
 
+template <bool MX>
 __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, DevState X, const double* Fm,
                                                                 const double* Tm, const double* Ech,
                                                                 DevScratch S, DevForces out, double* Eout) {
@@ -440,6 +511,20 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
         V3 ri = ld3(X.r + 3 * i);
         double d = sqrt((rj.x - ri.x) * (rj.x - ri.x) + (rj.y - ri.y) * (rj.y - ri.y) + (rj.z - ri.z) * (rj.z - ri.z));
         if (d > 25.0) continue;
+        if constexpr (MX) {
+          float zx = (float)(rj.x - ri.x), zy = (float)(rj.y - ri.y), zz = (float)(rj.z - ri.z);
+          float df = sqrtf(zx * zx + zy * zy + zz * zz), mi = 1.f / df;
+          float kap = (float)M.debyell, ex = expf(-kap * df), qf = (float)(M.k_e * qq);
+          float g = qf * ex * (kap * df + 1.f) / (df * df), e = qf * ex / df;
+          if (df <= 8.f) {
+            float sr = (float)M.sDD / df, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+            g += (float)M.k_ex * (12.f * sr12 - 6.f * sr6) / df;
+            e += (float)M.k_ex * (sr12 - sr6);
+          }
+          if (j < i) E = E + (double)e;
+          F.x += (double)(g * zx * mi); F.y += (double)(g * zy * mi); F.z += (double)(g * zz * mi);
+          continue;
+        }
         double mi = 1.0 / d;
         V3 z{mi * (rj.x - ri.x), mi * (rj.y - ri.y), mi * (rj.z - ri.z)};
         double g1 = M.k_e * qq * exp(-M.debyell * d) * (M.debyell * d + 1.0) / (d * d);
@@ -455,16 +540,16 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
     }
     // tails on this DNA bead (func.cpp:1898-1917); energy on the tail side
     for (int t = tid; t < M.n_tail; t += nt)
-      acc(F, pair_f1<true, true>(M.q_l, M.t_q[t], eps, M.debye, M.k_ex, M.sTL, rj, ld3(X.r_t + 3 * t), nullptr));
+      acc(F, pairF<true, true, MX>(M.q_l, M.t_q[t], eps, M.debye, M.k_ex, M.sTL, rj, ld3(X.r_t + 3 * t), nullptr));
     // LH beads on this DNA bead (func.cpp:2249-2279); energy on the LH side
     for (int b = tid; b < M.n_LH; b += nt) {
       int p = lh_param(M, b);
-      acc(F, pair_f1<true, true>(M.q_l, M.LH_q[p], eps, M.debye, M.k_ex, M.LH_vdw_hl[p], rj, ld3(X.r_lh + 3 * b), nullptr));
+      acc(F, pairF<true, true, MX>(M.q_l, M.LH_q[p], eps, M.debye, M.k_ex, M.LH_vdw_hl[p], rj, ld3(X.r_lh + 3 * b), nullptr));
     }
     // globular heads on this DNA bead (func.cpp:2481-2522); energy on the core side
     for (int s = tid; s < M.n_lhcore * M.n_lh_g; s += nt) {
       int m = s % M.n_lh_g;
-      acc(F, pair_f1<true, true>(M.q_l, M.LH_q[m], eps, M.debye, M.k_ex, M.LH_vdw_hl[m], rj, ld3(X.gpos + 3 * s), nullptr));
+      acc(F, pairF<true, true, MX>(M.q_l, M.LH_q[m], eps, M.debye, M.k_ex, M.LH_vdw_hl[m], rj, ld3(X.gpos + 3 * s), nullptr));
     }
   } else {
     const int J = M.core_rank[j];
@@ -476,14 +561,14 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
         int m = s / M.n, l = s - m * M.n;
         if (M.type[l] != 0) continue;
         V3 g = ld3(X.gpos + 3 * (lc * ng + m));
-        V3 f1 = pair_f1<true, true>(M.LH_q[m], M.q_l, eps, M.debye, M.k_ex, M.LH_vdw_hl[m], g, ld3(X.r + 3 * l), &E);
+        V3 f1 = pairF<true, true, MX>(M.LH_q[m], M.q_l, eps, M.debye, M.k_ex, M.LH_vdw_hl[m], g, ld3(X.r + 3 * l), &E);
         acc(F, f1);
         acc(T, torque_rel(f1, M.LH_g_pos + 3 * m, aj, bj, cj));
       }
       for (int s = tid; s < ng * M.n_tail; s += nt) {  // func.cpp:2403-2476
         int m = s / M.n_tail, t = s - m * M.n_tail;
         V3 g = ld3(X.gpos + 3 * (lc * ng + m));
-        V3 f1 = pair_f1<true, true>(M.LH_q[m], M.t_q[t], eps, M.debye, M.k_ex, M.LH_vdw_ht[m], g, ld3(X.r_t + 3 * t), &E);
+        V3 f1 = pairF<true, true, MX>(M.LH_q[m], M.t_q[t], eps, M.debye, M.k_ex, M.LH_vdw_ht[m], g, ld3(X.r_t + 3 * t), &E);
         acc(F, f1);
         acc(T, torque_rel(f1, M.LH_g_pos + 3 * m, aj, bj, cj));
       }
@@ -492,7 +577,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
         if (b / M.nlh == lc) continue;
         int p2 = lh_param(M, b);
         V3 g = ld3(X.gpos + 3 * (lc * ng + m));
-        V3 f1 = pair_f1<true, true>(M.LH_q[m], M.LH_q[p2], eps, M.debye, M.k_ex, (M.LH_vdw_hh[m] + M.LH_vdw_hh[p2]) / 2,
+        V3 f1 = pairF<true, true, MX>(M.LH_q[m], M.LH_q[p2], eps, M.debye, M.k_ex, (M.LH_vdw_hh[m] + M.LH_vdw_hh[p2]) / 2,
                                     g, ld3(X.r_lh + 3 * b), &E);
         acc(F, f1);
         acc(T, torque_rel(f1, M.LH_g_pos + 3 * m, aj, bj, cj));
@@ -504,7 +589,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
         V3 g = ld3(X.gpos + 3 * (lc * ng + m));
         V3 g2 = ld3(X.gpos + 3 * (K * ng + m1));
         double e = 0.0;
-        V3 f1 = pair_f1<true, true>(M.LH_q[m], M.LH_q[m1], eps, M.debye, M.k_ex, (M.LH_vdw_hh[m] + M.LH_vdw_hh[m1]) / 2, g,
+        V3 f1 = pairF<true, true, MX>(M.LH_q[m], M.LH_q[m1], eps, M.debye, M.k_ex, (M.LH_vdw_hh[m] + M.LH_vdw_hh[m1]) / 2, g,
                                     g2, &e);
         if (lc < K) E = E + e;
         acc(F, f1);
@@ -552,13 +637,13 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
       V3 rt = ld3(X.r_t + 3 * t0);
       for (int b = tid; b < M.n_LH; b += nt) {
         int p = lh_param(M, b);
-        V3 f2 = pair_f1<true, true>(M.t_q[t0], M.LH_q[p], eps, M.debye, M.k_ex, M.LH_vdw_ht[p], rt, ld3(X.r_lh + 3 * b), nullptr);
+        V3 f2 = pairF<true, true, MX>(M.t_q[t0], M.LH_q[p], eps, M.debye, M.k_ex, M.LH_vdw_ht[p], rt, ld3(X.r_lh + 3 * b), nullptr);
         acc(F, f2);
         acc(T, torque_abs(f2, rt, rj, aj, bj, cj));
       }
       for (int s = tid; s < M.n_lhcore * M.n_lh_g; s += nt) {
         int m = s % M.n_lh_g;
-        V3 f2 = pair_f1<true, true>(M.t_q[t0], M.LH_q[m], eps, M.debye, M.k_ex, M.LH_vdw_ht[m], rt, ld3(X.gpos + 3 * s), nullptr);
+        V3 f2 = pairF<true, true, MX>(M.t_q[t0], M.LH_q[m], eps, M.debye, M.k_ex, M.LH_vdw_ht[m], rt, ld3(X.gpos + 3 * s), nullptr);
         acc(F, f2);
         acc(T, torque_abs(f2, rt, rj, aj, bj, cj));
       }
@@ -620,6 +705,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
 
 // ------------------------------------------------------------ tails
 // One warp per tail bead (func.cpp:1809-1917, 2343-2476 for the LH side).
+template <bool MX>
 __global__ void k_tail_gather(DevModel M, DevState X, DevForces out, double* Eout) {
   int lane = threadIdx.x & 31;
   int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -660,23 +746,23 @@ __global__ void k_tail_gather(DevModel M, DevState X, DevForces out, double* Eou
     int lo = t < u ? t : u, hi = t < u ? u : t;
     if (!(grp[lo] != grp[hi] || hi > lo + 2)) continue;
     double e = 0.0;
-    acc(F, pair_f1<true, false>(M.t_q[t], M.t_q[u], eps, M.debye, 0.0, 0.0, rt, ld3(X.r_t + 3 * u), &e));
+    acc(F, pairF<true, false, MX>(M.t_q[t], M.t_q[u], eps, M.debye, 0.0, 0.0, rt, ld3(X.r_t + 3 * u), &e));
     if (t < u) E = E + e;
   }
   // linker DNA (func.cpp:1898-1917); energy here
   for (int q = lane; q < M.n_dna; q += 32) {
     int j = M.dna_bead[q];
-    acc(F, pair_f1<true, true>(M.t_q[t], M.q_l, eps, M.debye, M.k_ex, M.sTL, rt, ld3(X.r + 3 * j), &E));
+    acc(F, pairF<true, true, MX>(M.t_q[t], M.q_l, eps, M.debye, M.k_ex, M.sTL, rt, ld3(X.r + 3 * j), &E));
   }
   if (M.t_fix[t] == 0) {
     // LH beads and globular heads act on free tail beads (energies on their side)
     for (int b = lane; b < M.n_LH; b += 32) {
       int p = lh_param(M, b);
-      acc(F, pair_f1<true, true>(M.t_q[t], M.LH_q[p], eps, M.debye, M.k_ex, M.LH_vdw_ht[p], rt, ld3(X.r_lh + 3 * b), nullptr));
+      acc(F, pairF<true, true, MX>(M.t_q[t], M.LH_q[p], eps, M.debye, M.k_ex, M.LH_vdw_ht[p], rt, ld3(X.r_lh + 3 * b), nullptr));
     }
     for (int s = lane; s < M.n_lhcore * M.n_lh_g; s += 32) {
       int m = s % M.n_lh_g;
-      acc(F, pair_f1<true, true>(M.t_q[t], M.LH_q[m], eps, M.debye, M.k_ex, M.LH_vdw_ht[m], rt, ld3(X.gpos + 3 * s), nullptr));
+      acc(F, pairF<true, true, MX>(M.t_q[t], M.LH_q[m], eps, M.debye, M.k_ex, M.LH_vdw_ht[m], rt, ld3(X.gpos + 3 * s), nullptr));
     }
   }
   F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
@@ -688,6 +774,7 @@ __global__ void k_tail_gather(DevModel M, DevState X, DevForces out, double* Eou
 
 // ------------------------------------------------------------ LH beads
 // One warp per mobile LH bead (func.cpp:2109-2398, 2588-2644, 2725-2777).
+template <bool MX>
 __global__ void k_lh_gather(DevModel M, DevState X, DevForces out, double* Eout) {
   int lane = threadIdx.x & 31;
   int bI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -740,25 +827,25 @@ __global__ void k_lh_gather(DevModel M, DevState X, DevForces out, double* Eout)
     if (bI / nlh == u / nlh) {
       int lo = bI < u ? bI : u, hi = bI < u ? u : bI;
       if (!(hi > lo + 1)) continue;
-      acc(F, pair_f1<false, true>(0.0, 0.0, eps, M.debye, M.k_ex, sig, rb, ld3(X.r_lh + 3 * u), &e));
+      acc(F, pairF<false, true, MX>(0.0, 0.0, eps, M.debye, M.k_ex, sig, rb, ld3(X.r_lh + 3 * u), &e));
     } else {
-      acc(F, pair_f1<true, true>(M.LH_q[pb], M.LH_q[pu], eps, M.debye, M.k_ex, sig, rb, ld3(X.r_lh + 3 * u), &e));
+      acc(F, pairF<true, true, MX>(M.LH_q[pb], M.LH_q[pu], eps, M.debye, M.k_ex, sig, rb, ld3(X.r_lh + 3 * u), &e));
     }
     if (bI < u) E = E + e;
   }
   // linker DNA and tails (func.cpp:2249-2398); energies here
   for (int q = lane; q < M.n_dna; q += 32) {
     int j = M.dna_bead[q];
-    acc(F, pair_f1<true, true>(M.LH_q[pb], M.q_l, eps, M.debye, M.k_ex, M.LH_vdw_hl[pb], rb, ld3(X.r + 3 * j), &E));
+    acc(F, pairF<true, true, MX>(M.LH_q[pb], M.q_l, eps, M.debye, M.k_ex, M.LH_vdw_hl[pb], rb, ld3(X.r + 3 * j), &E));
   }
   for (int t = lane; t < M.n_tail; t += 32)
-    acc(F, pair_f1<true, true>(M.LH_q[pb], M.t_q[t], eps, M.debye, M.k_ex, M.LH_vdw_ht[pb], rb, ld3(X.r_t + 3 * t), &E));
+    acc(F, pairF<true, true, MX>(M.LH_q[pb], M.t_q[t], eps, M.debye, M.k_ex, M.LH_vdw_ht[pb], rb, ld3(X.r_t + 3 * t), &E));
   // globular heads of the other LHs (func.cpp:2588-2644); energy on the core
   const int own = bI / nlh;
   for (int s = lane; s < M.n_lhcore * M.n_lh_g; s += 32) {
     int K = s / M.n_lh_g, m = s - K * M.n_lh_g;
     if (K == own) continue;
-    acc(F, pair_f1<true, true>(M.LH_q[pb], M.LH_q[m], eps, M.debye, M.k_ex, (M.LH_vdw_hh[m] + M.LH_vdw_hh[pb]) / 2, rb,
+    acc(F, pairF<true, true, MX>(M.LH_q[pb], M.LH_q[m], eps, M.debye, M.k_ex, (M.LH_vdw_hh[m] + M.LH_vdw_hh[pb]) / 2, rb,
                                ld3(X.gpos + 3 * s), nullptr));
   }
   F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
@@ -782,7 +869,6 @@ __global__ void k_energy(int n0, const double* e0, double* E) {
 namespace bdk {
 
 int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mixed, cudaStream_t st) {
-  (void)mixed;
   // energy layout in S.ebuf: [0,n) chain, [n, n+n_tail) tails, then LH
   double* Ech = S.ebuf;
   double* Et = S.ebuf + M.n;
@@ -791,19 +877,27 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   double* Fm = S.ebuf + 2 * M.n + M.n_tail + M.n_LH; // [3n]
   double* Tm = Fm + 3 * M.n;                          // [3n]
   int L = 0;
+#define KSEL(name) (mixed ? name<true> : name<false>)
+  auto k_core_coreX = KSEL(k_core_core);
+  auto k_dna_coreX = KSEL(k_dna_core);
+  auto k_ghead_coreX = KSEL(k_ghead_core);
+  auto k_tail_gatherX = KSEL(k_tail_gather);
+  auto k_lh_gatherX = KSEL(k_lh_gather);
+  auto k_chain_gatherX = KSEL(k_chain_gather);
+#undef KSEL
   if (M.n_lhcore > 0) { k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X); L++; }
   k_chain_bonded<<<cdiv(M.n, 128), 128, 0, st>>>(M, X, Fm, Tm, Ebond);
   L++;
   if (M.n_c > 1) {
     size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
-    k_core_core<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+    k_core_coreX<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
     L++;
   }
-  if (M.n_dna > 0 && M.n_c > 0) { k_dna_core<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc); L++; }
-  if (M.n_lhcore > 0) { k_ghead_core<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc); L++; }
-  if (M.n_tail > 0) { k_tail_gather<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et); L++; }
-  if (M.n_LH > 0) { k_lh_gather<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El); L++; }
-  k_chain_gather<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
+  if (M.n_dna > 0 && M.n_c > 0) { k_dna_coreX<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc); L++; }
+  if (M.n_lhcore > 0) { k_ghead_coreX<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc); L++; }
+  if (M.n_tail > 0) { k_tail_gatherX<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et); L++; }
+  if (M.n_LH > 0) { k_lh_gatherX<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El); L++; }
+  k_chain_gatherX<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
   k_energy<<<1, 256, 0, st>>>(M.n + M.n_tail + M.n_LH, S.ebuf, out.E);
   return L + 2;
 }

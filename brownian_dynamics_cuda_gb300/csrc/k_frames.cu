@@ -212,6 +212,7 @@ __global__ void k_rotate(DevModel M, const double* __restrict__ T, const double*
 // D_ss the RPY block of the bead's own species (chain, tails or LH).
 // The lanes split the partner loop; partial sums are combined in a fixed
 // butterfly order so the result is deterministic.
+template <bool MX>
 __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const double* __restrict__ Fc,
                             const double* __restrict__ Ft, const double* __restrict__ Fl, const double* __restrict__ rd,
                             const double* __restrict__ r0, const double* __restrict__ rt0,
@@ -227,27 +228,48 @@ __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const 
   V3 ri = ld3(r_all + 3 * i);
   double radi = M.rad_all[i];
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-  for (int j = lo + lane; j < hi; j += 32) {
-    const double* f = F + 3 * (j - lo);
-    if (j == i) {
-      double d = M.a1 / radi;
-      s0 = s0 + M.del * d * f[0];
-      s1 = s1 + M.del * d * f[1];
-      s2 = s2 + M.del * d * f[2];
-      continue;
+  if constexpr (MX) {
+    const float a1f = (float)M.a1, a2f = (float)M.a2, radf = (float)radi, delf = (float)M.del;
+    for (int j = lo + lane; j < hi; j += 32) {
+      const double* f = F + 3 * (j - lo);
+      float Db[3][3];
+      if (j == i) {
+        const float d = a1f / radf;
+        s0 += (double)(delf * d * (float)f[0]);
+        s1 += (double)(delf * d * (float)f[1]);
+        s2 += (double)(delf * d * (float)f[2]);
+        continue;
+      }
+      rpy_block_f((float)(ri.x - r_all[3 * j]), (float)(ri.y - r_all[3 * j + 1]), (float)(ri.z - r_all[3 * j + 2]), radf,
+                  (float)M.rad_all[j], a1f, a2f, Db);
+      const float fx = (float)f[0], fy = (float)f[1], fz = (float)f[2];
+      s0 += (double)(delf * (Db[0][0] * fx + Db[0][1] * fy + Db[0][2] * fz));
+      s1 += (double)(delf * (Db[1][0] * fx + Db[1][1] * fy + Db[1][2] * fz));
+      s2 += (double)(delf * (Db[2][0] * fx + Db[2][1] * fy + Db[2][2] * fz));
     }
-    V3 rj = ld3(r_all + 3 * j);
-    V3 sij{ri.x - rj.x, ri.y - rj.y, ri.z - rj.z};
-    double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
-    double s = sqrt(ssq);
-    double radj = M.rad_all[j];
-    double Db[3][3];
-    rpy_block(sij, ssq, s, radi, radj, M.a1, M.a2, Db);
-    for (int l = 0; l < 3; l++) {
-      double fl = f[l];
-      s0 = s0 + M.del * Db[0][l] * fl;
-      s1 = s1 + M.del * Db[1][l] * fl;
-      s2 = s2 + M.del * Db[2][l] * fl;
+  } else {
+  for (int j = lo + lane; j < hi; j += 32) {
+      const double* f = F + 3 * (j - lo);
+      if (j == i) {
+        double d = M.a1 / radi;
+        s0 = s0 + M.del * d * f[0];
+        s1 = s1 + M.del * d * f[1];
+        s2 = s2 + M.del * d * f[2];
+        continue;
+      }
+      V3 rj = ld3(r_all + 3 * j);
+      V3 sij{ri.x - rj.x, ri.y - rj.y, ri.z - rj.z};
+      double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
+      double s = sqrt(ssq);
+      double radj = M.rad_all[j];
+      double Db[3][3];
+      rpy_block(sij, ssq, s, radi, radj, M.a1, M.a2, Db);
+      for (int l = 0; l < 3; l++) {
+        double fl = f[l];
+        s0 = s0 + M.del * Db[0][l] * fl;
+        s1 = s1 + M.del * Db[1][l] * fl;
+        s2 = s2 + M.del * Db[2][l] * fl;
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -305,9 +327,9 @@ void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream
 // hold X's positions (the tensor is evaluated at the start configuration).
 void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const DevForces& Fo, const double* rr,
                       const double* rd, const double* r_all, int mixed, cudaStream_t st) {
-  (void)mixed;
   k_rotate<<<cdiv(M.n, 128), 128, 0, st>>>(M, Fo.T, rr, X.a, X.b, X.c, Y.a, Y.b, Y.c);
-  k_translate<<<cdiv(M.n_D * 32, 256), 256, 0, st>>>(M, r_all, Fo.F, Fo.tF, Fo.lF, rd, X.r, X.r_t, X.r_lh, Y.r,
+  auto kt = mixed ? k_translate<true> : k_translate<false>;
+  kt<<<cdiv(M.n_D * 32, 256), 256, 0, st>>>(M, r_all, Fo.F, Fo.tF, Fo.lF, rd, X.r, X.r_t, X.r_lh, Y.r,
                                                       Y.r_t, Y.r_lh);
 }
 

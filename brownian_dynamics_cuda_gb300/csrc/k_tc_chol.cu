@@ -1,10 +1,13 @@
 // Mixed-precision Cholesky of the RPY tensor on the sm_103a tensor cores.
 //
-// Right-looking blocked factorisation with 128-wide panels on an FP32
-// column-major matrix:
-//   k_diag32    FP32 Cholesky of the 128 x 128 diagonal block in shared
-//               memory (a negative pivot is replaced by its absolute value
-//               and counted, as func.cpp:827-833 does).
+// Right-looking blocked factorisation with 128-wide panels.  The matrix is
+// stored in FP64 (column-major), so each trailing update is rounded at FP64
+// however many panels precede it; the arithmetic is FP32-class:
+//   k_diag32    Cholesky of the 128 x 128 diagonal block in shared memory,
+//               left-looking (each element is one FP32 dot product and one
+//               rounding of its FP64 value, not one rounding per column as a
+//               right-looking FP32 update would do); a negative pivot is
+//               replaced by its absolute value and counted (func.cpp:827-833).
 //   k_panel32   L_ik = A_ik L_kk^-T by forward substitution for every 128-row
 //               tile below the block (FP32), written back and split into three BF16 slices
 //               (hi + mid + lo = the FP32 value exactly), stored pre-swizzled
@@ -15,8 +18,8 @@
 //               hi.lo, mid.mid, lo.hi) accumulate in one FP32 tensor-memory
 //               accumulator (tcgen05.mma, M = N = 128, K = 16 per
 //               instruction), and the epilogue reads the accumulator with
-//               tcgen05.ld and updates the FP32 tile.  The dropped products
-//               are below 2^-24 of the kept ones: FP32-class accuracy.
+//               tcgen05.ld and updates the FP64 tile.  The dropped products
+//               are below 2^-24 of the kept ones: FP32-class products.
 // Every mbarrier wait is bounded; on a timeout the kernel records an error
 // code, frees its tensor memory and returns.
 #include <cuda_bf16.h>
@@ -43,66 +46,48 @@ __device__ __forceinline__ uint32_t swz_off(int r, int k) {
   return half * kHalfBytes + (r >> 3) * 1024 + (r & 7) * 128 + ((((kk >> 3) ^ (r & 7)) & 7) << 4) + (kk & 7) * 2;
 }
 
-// ------------------------------------------------------------ RPY (FP32 storage)
-__global__ void __launch_bounds__(256) k_rpy32(int nD, const double* __restrict__ r, const double* __restrict__ rad,
-                                               double a1, double a2, float* __restrict__ A, int lda) {
-  using namespace bdp;
-  int bi = blockIdx.y, bj = blockIdx.x;
-  if (bj > bi) return;
-  int i = bi * 32 + threadIdx.x;
-  if (i >= nD) return;
-  V3 ri = ld3(r + 3 * i);
-  double radi = rad[i];
-  for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
-    int j = bj * 32 + jj;
-    if (j >= nD || j > i) continue;
-    if (j == i) {
-      for (int l = 0; l < 3; l++)
-        for (int k = l; k < 3; k++) A[(size_t)(3 * j + l) * lda + 3 * i + k] = (k == l) ? (float)(a1 / radi) : 0.f;
-      continue;
-    }
-    V3 rj = ld3(r + 3 * j);
-    V3 sij{ri.x - rj.x, ri.y - rj.y, ri.z - rj.z};
-    double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
-    double s = sqrt(ssq);
-    double radj = rad[j];
-    double Db[3][3];
-    rpy_block(sij, ssq, s, radi, radj, a1, a2, Db);
-    for (int l = 0; l < 3; l++) {
-      float* col = A + (size_t)(3 * j + l) * lda + 3 * i;
-      for (int k = 0; k < 3; k++) col[k] = (float)Db[k][l];
-    }
-  }
-}
-
 // ------------------------------------------------------------ diagonal block
-__global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int kb, int* negpiv) {
+__global__ void __launch_bounds__(256) k_diag32(double* A, int lda, int k0, int kb, int* negpiv) {
   extern __shared__ float sm32[];
-  float (*S)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);
+  float (*S)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);   // [row][col]; lower part holds L as it forms
+  __shared__ float diag_s[1];
   const int tid = threadIdx.x;
   for (int e = tid; e < kb * kb; e += blockDim.x) {
     int c = e / kb, rr = e - c * kb;
-    S[rr][c] = (rr >= c) ? A[(size_t)(k0 + c) * lda + k0 + rr] : 0.f;
-  }
-  // thread t owns row r = t % 128 and, of that row, the columns of parity h = t / 128
-  const int r = tid & (kT - 1), h = tid >> 7;
-  for (int c = 0; c < kb; c++) {
-    __syncthreads();
-    float d = S[c][c];
-    if (tid == 0 && d < 0.f) atomicAdd(negpiv, 1);
-    const float piv = sqrtf(fabsf(d));
-    if (h == 0 && r > c && r < kb) S[r][c] = S[r][c] / piv;
-    __syncthreads();
-    if (tid == 0) S[c][c] = piv;
-    if (r > c && r < kb) {
-      const float lrc = S[r][c];
-      for (int q = c + 1 + h; q <= r; q += 2) S[r][q] = fmaf(-lrc, S[q][c], S[r][q]);
-    }
+    S[rr][c] = (rr >= c) ? (float)A[(size_t)(k0 + c) * lda + k0 + rr] : 0.f;
   }
   __syncthreads();
+  // column c: every row r >= c forms s = A[r][c] - sum_{q<c} L[r][q] L[c][q]
+  // as one dot product (four partial sums), then L[c][c] = sqrt(|s_cc|) and
+  // L[r][c] = s_rc / L[c][c]
+  const int r = tid;
+  for (int c = 0; c < kb; c++) {
+    float sv = 0.f;
+    if (r >= c && r < kb) {
+      float s0 = S[r][c], s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      int q = 0;
+      for (; q + 3 < c; q += 4) {
+        s0 = fmaf(-S[r][q], S[c][q], s0);
+        s1 = fmaf(-S[r][q + 1], S[c][q + 1], s1);
+        s2 = fmaf(-S[r][q + 2], S[c][q + 2], s2);
+        s3 = fmaf(-S[r][q + 3], S[c][q + 3], s3);
+      }
+      for (; q < c; q++) s0 = fmaf(-S[r][q], S[c][q], s0);
+      sv = (s0 + s1) + (s2 + s3);
+      if (r == c) {
+        if (sv < 0.f) atomicAdd(negpiv, 1);
+        diag_s[0] = sqrtf(fabsf(sv));
+      }
+    }
+    __syncthreads();
+    const float piv = diag_s[0];
+    if (r == c) S[c][c] = piv;
+    else if (r > c && r < kb) S[r][c] = sv / piv;
+    __syncthreads();
+  }
   for (int e = tid; e < kb * kb; e += blockDim.x) {
     int c = e / kb, rr = e - c * kb;
-    if (rr >= c) A[(size_t)(k0 + c) * lda + k0 + rr] = S[rr][c];
+    if (rr >= c) A[(size_t)(k0 + c) * lda + k0 + rr] = (double)S[rr][c];
   }
 }
 
@@ -112,7 +97,7 @@ __global__ void __launch_bounds__(256) k_diag32(float* A, int lda, int k0, int k
 // backward stable, unlike multiplying by an explicit inverse); the result
 // L_ik is written back (FP32) and split into three BF16 slices stored
 // pre-swizzled at PS + tile*96KB.
-__global__ void __launch_bounds__(128) k_panel32(float* A, int lda, int m, int k0, int kb, int tile0,
+__global__ void __launch_bounds__(128) k_panel32(double* A, int lda, int m, int k0, int kb, int tile0,
                                                  unsigned char* PS) {
   extern __shared__ float sm32[];
   float (*Lk)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);               // [c][q] factor
@@ -123,8 +108,8 @@ __global__ void __launch_bounds__(128) k_panel32(float* A, int lda, int m, int k
   for (int e = tid; e < kT * kT; e += blockDim.x) {
     int q = e / kT, rr = e - q * kT;  // column-major walk: coalesced
     int gr = row0 + rr;
-    X[rr][q] = (gr < m && q < kb) ? A[(size_t)(k0 + q) * lda + gr] : 0.f;
-    Lk[rr][q] = (rr >= q && rr < kb && q < kb) ? A[(size_t)(k0 + q) * lda + k0 + rr] : 0.f;
+    X[rr][q] = (gr < m && q < kb) ? (float)A[(size_t)(k0 + q) * lda + gr] : 0.f;
+    Lk[rr][q] = (rr >= q && rr < kb && q < kb) ? (float)A[(size_t)(k0 + q) * lda + k0 + rr] : 0.f;
   }
   __syncthreads();
   {
@@ -149,7 +134,7 @@ __global__ void __launch_bounds__(128) k_panel32(float* A, int lda, int m, int k
     int gr = row0 + r;
     bool in = gr < m && c < kb;
     float x = in ? X[r][c] : 0.f;
-    if (in) A[(size_t)(k0 + c) * lda + gr] = x;
+    if (in) A[(size_t)(k0 + c) * lda + gr] = (double)x;
     __nv_bfloat16 h = __float2bfloat16_rn(x);
     float r1 = x - __bfloat162float(h);
     __nv_bfloat16 md = __float2bfloat16_rn(r1);
@@ -166,7 +151,7 @@ __global__ void __launch_bounds__(128) k_panel32(float* A, int lda, int m, int k
 constexpr int kSyrkThreads = 128;
 constexpr size_t kSyrkSmem = 2 * (size_t)kTileBytes + 1024 + 64;
 
-__global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(float* A, int lda, int m, int kpanel, int nt,
+__global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(double* A, int lda, int m, int kpanel, int nt,
                                                             const unsigned char* __restrict__ PS, int* err) {
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -239,20 +224,21 @@ __global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(float* A, int lda, 
     const int gi = I * kT + i;
     const bool row_ok = gi < m;
     for (int c = 0; c < 4; c++) {
-      float old[32], v[32];
+      double old[32];
+      float v[32];
       const int gj0 = J * kT + 32 * c;
       // all loads of the chunk first (independent), then the subtracts and stores
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const int gj = gj0 + j;
         const bool ok2 = row_ok && gj < m && (!diag || gi >= gj);
-        old[j] = ok2 ? A[(size_t)gj * lda + gi] : 0.f;
+        old[j] = ok2 ? A[(size_t)gj * lda + gi] : 0.0;
       }
       sm100::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const int gj = gj0 + j;
-        if (row_ok && gj < m && (!diag || gi >= gj)) A[(size_t)gj * lda + gi] = old[j] - v[j];
+        if (row_ok && gj < m && (!diag || gi >= gj)) A[(size_t)gj * lda + gi] = old[j] - (double)v[j];
       }
     }
   } else if (threadIdx.x == 0 && loaded) {
@@ -263,35 +249,12 @@ __global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(float* A, int lda, 
   if (warp == 0) sm100::tmem_dealloc(tmem, 128);
 }
 
-// ------------------------------------------------------------ L p (FP32 factor)
-__global__ void __launch_bounds__(256) k_trmv32_part(int m, const float* __restrict__ A, int lda,
-                                                     const double* __restrict__ p, double s2dt,
-                                                     double* __restrict__ part, int chunk) {
-  int i = blockIdx.x * 256 + threadIdx.x;
-  int kc = blockIdx.y;
-  int k0 = kc * chunk, k1 = min(k0 + chunk, m);
-  double s = 0.0;
-  if (i < m) {
-    int kend = min(k1, i + 1);
-    for (int k = k0; k < kend; k++) s = fma((double)A[(size_t)k * lda + i], p[k], s);
-  }
-  if (i < m) part[(size_t)kc * m + i] = s2dt * s;
-}
-
-__global__ void k_trmv32_sum(int m, int nchunk, const double* __restrict__ part, double* __restrict__ rd) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  double s = 0.0;
-  for (int c = 0; c < nchunk; c++) s = s + part[(size_t)c * m + i];
-  rd[i] = s;
-}
-
 }  // namespace
 
 namespace bdk {
 
 size_t mixed_panel_bytes(int m) { return (size_t)cdiv(m, kT) * kTileBytes; }
-int mixed_pad(int m) { return cdiv(m, kT) * kT; }
+int mixed_tiles(int m) { return cdiv(m, kT); }
 
 static bool g_attr_done = false;
 
@@ -308,36 +271,27 @@ int set_mixed_attributes() {
   return 0;
 }
 
-void rpy_assemble32(int nD, const double* r_all, const double* rad, double a1, double a2, float* A, int lda,
-                    cudaStream_t st) {
-  int nt = cdiv(nD, 32);
-  k_rpy32<<<dim3(nt, nt), dim3(32, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
-}
-
 // Returns the number of kernel launches.
-int potrf_mixed(int m, float* A, int lda, unsigned char* PS, float* W, int* negpiv, int* err, cudaStream_t st) {
+int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
+                cudaEvent_t* syrk_ev, double* syrk_flop) {
   const int nt = cdiv(m, kT);
   const size_t two = 2 * (size_t)kT * (kT + 1) * sizeof(float);
   int L = 0;
   for (int k = 0; k < nt; k++) {
     const int k0 = k * kT, kb = (m - k0 < kT) ? m - k0 : kT;
-    k_diag32<<<1, 256, two / 2, st>>>(A, lda, k0, kb, negpiv);
+    k_diag32<<<1, kT, two / 2, st>>>(A, lda, k0, kb, negpiv);
     L++;
     const int below = nt - k - 1;
     if (below <= 0) break;
     k_panel32<<<below, 128, two, st>>>(A, lda, m, k0, kb, k + 1, PS);
     const int pairs = below * (below + 1) / 2;
+    if (syrk_ev) cudaEventRecord(syrk_ev[2 * k], st);
     k_tc_syrk<<<pairs, kSyrkThreads, kSyrkSmem, st>>>(A, lda, m, k, nt, PS, err);
+    if (syrk_ev) cudaEventRecord(syrk_ev[2 * k + 1], st);
+    if (syrk_flop) *syrk_flop += 6.0 * 2.0 * kT * kT * kT * pairs;  // BF16 tensor work issued
     L += 2;
   }
   return L;
-}
-
-void trmv32(int m, const float* A, int lda, const double* p, double s2dt, double* rd, double* part, cudaStream_t st) {
-  const int chunk = 512;
-  int nchunk = cdiv(m, chunk);
-  k_trmv32_part<<<dim3(cdiv(m, 256), nchunk), 256, 0, st>>>(m, A, lda, p, s2dt, part, chunk);
-  k_trmv32_sum<<<cdiv(m, 256), 256, 0, st>>>(m, nchunk, part, rd);
 }
 
 }  // namespace bdk

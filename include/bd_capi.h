@@ -190,6 +190,11 @@ int bd_dev_potrf(bd_ctx* ctx, int m, double* d_A, int lda, int precision, int* d
 /* Timing of the last step's phases on the device (ms): rpy chol rd forces1
  * update1 frames forces2 update2 total.  Valid after a step with use_graph=0. */
 int bd_phase_times(bd_ctx* ctx, float* out9);
+/* Mixed path: total device time (CUDA events on the context's stream) of
+ * the tensor-core trailing-update launches of the last step run with
+ * timing enabled (see bd_phase_times), their number, and the BF16 tensor
+ * work they issued (flop). */
+int bd_kernel_time(bd_ctx* ctx, float* total_ms, int* launches, double* tensor_flop);
 /* Count of kernel launches issued by the last bd_step (graph nodes count once each). */
 int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
