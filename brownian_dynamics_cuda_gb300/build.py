@@ -31,6 +31,7 @@ UNITS = [
     ("k_forces.cu", ["-fmad=false"]),
     ("k_rpy_chol.cu", ["-fmad=false"]),
     ("k_tc_chol.cu", []),
+    ("k_noalloc.cu", ["-fmad=false"]),
 ]
 
 

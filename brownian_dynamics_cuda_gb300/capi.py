@@ -98,6 +98,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_set_state.argtypes = [C.c_void_p, C.c_char_p, _dp]
     L.bd_dev_rpy.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_int]
     L.bd_dev_potrf.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.bd_noise_displacement_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_void_p,
+                                                C.c_void_p]
     L.bd_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.bd_launch_count.argtypes = [C.c_void_p, _ip]
     L.bd_kernel_time.argtypes = [C.c_void_p, C.POINTER(C.c_float), _ip, _dp]

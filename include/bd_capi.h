@@ -187,6 +187,24 @@ int bd_dev_rpy(bd_ctx* ctx, int n_beads, const double* d_r, const double* d_rad,
                double* d_D, int lda);
 int bd_dev_potrf(bd_ctx* ctx, int m, double* d_A, int lda, int precision, int* d_info);
 
+/* Allocation-free noise displacement: rd = s2dt * L p for a lower factor L
+ * (column-major, leading dim lda) that the caller owns on the device, with
+ * p and rd caller-owned device vectors of length m; stream-ordered on
+ * `stream` (a cudaStream_t, NULL for the default stream).
+ * No counterpart in the reference: it serves hosts that cannot let a
+ * library call cudaMalloc/cudaFree (their device memory belongs to their own
+ * pool allocator, or an allocation - which may synchronise the device -
+ * would stall their step loop).  It calls no allocating routine: its
+ * partial sums live in a fixed 4 MiB device array inside the library, so
+ * m must not exceed 16384 (BD_ERR_ARG otherwise).  The first call on a
+ * device looks that array's device address up (cudaGetSymbolAddress, with
+ * the device current) and caches it; make that first call before any stream
+ * capture.  All calls share the array: calls whose kernels overlap on the
+ * GPU race and must be ordered by the caller.  Nothing in the array needs
+ * to start at zero. */
+int bd_noise_displacement_noalloc(int m, const double* d_L, int lda, const double* d_p, double s2dt, double* d_rd,
+                                  void* stream);
+
 /* Timing of the last step's phases on the device (ms): rpy chol rd forces1
  * update1 frames forces2 update2 total.  Valid after a step with use_graph=0. */
 int bd_phase_times(bd_ctx* ctx, float* out9);
