@@ -117,6 +117,46 @@ def fp64_peak_tflops() -> float:
     return 2.0 * n ** 3 / best / 1e12
 
 
+def fp64_comparison(fib, rr_d, p_d, host, args, local, stream) -> dict:
+    """Plain FP64 step (CUDA graph, same fiber, same noise) timed like the
+    headline, and the relative displacement error of one mixed step against
+    one FP64 step from the same state: max |dr_mixed - dr_fp64| / max |dr_fp64|
+    over r, r_t and r_lh."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
+    steps = max(2, min(args.steps, 5))
+    c64 = Context(fib, precision=PREC_FP64, use_graph=True, device=local, stream=stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            c64.step_device(rr_d[i].data_ptr(), p_d[i].data_ptr())
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            c64.step_device(rr_d[args.warmup + i % args.steps].data_ptr(), p_d[args.warmup + i % args.steps].data_ptr())
+        e1.record(stream)
+        stream.synchronize()
+    ms64 = e0.elapsed_time(e1) / steps
+    c64.close()
+    a = Context(fib, precision=PREC_FP64, device=local)
+    b = Context(fib, precision=PREC_MIXED, device=local)
+    rr, p = host[0]
+    a.step(rr, p)
+    b.step(rr, p)
+    num = den = 0.0
+    for k in ("r", "r_t", "r_lh"):
+        if fib.state[k].size == 0:
+            continue
+        d64 = a.get(k) - fib.state[k]
+        dm = b.get(k) - fib.state[k]
+        num = max(num, float(np.abs(dm - d64).max()))
+        den = max(den, float(np.abs(d64).max()))
+    a.close()
+    b.close()
+    return {"fp64_steps_per_s": 1000.0 / ms64, "fp64_ms_per_step": ms64, "fp64_steps_timed": steps,
+            "rel_displacement_err": num / den, "tolerance": 1e-6}
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -270,6 +310,14 @@ def run_ours(args):
                 "useful_fp32_equiv_tflops": flop_k / 6.0 / (ms_k * 1e-3) / 1e12 if ms_k > 0 else None,
                 "chol_phase_ms": chol_ms}
         roof["frac"] = roof["achieved"] / peak if roof["achieved"] else None
+    # the plain FP64 step on the same fiber and noise: the metric's reference
+    # point, and the mixed step's displacement error against it
+    vs64 = None
+    if prec == PREC_MIXED:
+        vs64 = fp64_comparison(fib, rr_d, p_d, host, args, local, stream)
+        if world > 1:
+            vs64["fp64_steps_per_s"] = replica_rate(max_over_ranks(1000.0 / vs64["fp64_steps_per_s"]), world)
+        vs64["speedup_vs_fp64"] = value / vs64["fp64_steps_per_s"]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         s = cpu_sample(fib, 1)
@@ -285,7 +333,7 @@ def run_ours(args):
                                                                          (m * m * 8 / 1e9)},
                 "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+                "gpu_launches": launches, "clocks": clocks, "roofline": roof, "vs_fp64": vs64,
                 "phases_ms": dict(zip(names, [round(float(x), 4) for x in phases])),
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
@@ -301,7 +349,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     if args.impl == "reference":
