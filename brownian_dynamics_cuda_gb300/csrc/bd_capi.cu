@@ -93,7 +93,9 @@ struct bd_ctx {
   cudaEvent_t ev[10] = {};
   bool timing = false;
   std::vector<cudaEvent_t> kev;   // per-launch events around the tensor-core update (timing steps only)
+  int kev_pairs = 0;
   double kflop = 0.0;
+  bdk::MixedAux aux;               // mixed path: lookahead stream and events
   // host copies for the drop-in paths
   std::vector<int> h_type;
 };
@@ -150,8 +152,9 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
     if (mixed) {
       const bool kt = c->timing && !c->kev.empty();
       c->kflop = 0.0;
-      L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, kt ? c->kev.data() : nullptr,
-                            kt ? &c->kflop : nullptr);
+      c->kev_pairs = 0;
+      L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, c->aux, kt ? c->kev.data() : nullptr,
+                            kt ? &c->kev_pairs : nullptr, kt ? &c->kflop : nullptr);
     }
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
   }
@@ -303,6 +306,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
     if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
+    if (bdk::mixed_aux_create(&c->aux)) return fail(set_error(BD_ERR_CUDA, "bd_create: lookahead stream/events"));
   }
   Arena ar{(char*)c->arena_base, tot, 0};
   int *d_type = ar.take<int>(n), *d_core_rank = ar.take<int>(n), *d_core_bead = ar.take<int>(nc),
@@ -419,6 +423,7 @@ extern "C" int bd_destroy(bd_ctx* c) {
   for (int k = 0; k < 10; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (auto ev : c->kev) cudaEventDestroy(ev);
+  bdk::mixed_aux_destroy(&c->aux);
   if (c->A) cudaFree(c->A);
   if (c->PS) cudaFree(c->PS);
   if (c->d_err) cudaFree(c->d_err);
@@ -448,7 +453,8 @@ static int run_step(bd_ctx* c, const double* d_rr, const double* d_p) {
       cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (rc) return rc;
       if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_step: graph capture failed");
-      e = cudaGraphInstantiate(&c->graph, g, 0);
+      // per-node priorities: the lookahead panels run ahead of the bulk update
+      e = cudaGraphInstantiate(&c->graph, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_step: graph instantiation failed");
     }
@@ -555,7 +561,7 @@ static int factor_now(bd_ctx* c) {
   assemble_now(c);
   CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
   if (c->precision == BD_PREC_MIXED) {
-    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream);
+    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream, c->aux);
     int derr = 0;
     CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -664,8 +670,7 @@ extern "C" int bd_kernel_time(bd_ctx* c, float* total_ms, int* launches, double*
   if (tensor_flop) *tensor_flop = c->kflop;
   if (c->precision != BD_PREC_MIXED || !c->timing) return BD_OK;
   CK(cudaStreamSynchronize(c->stream));
-  const int nt = bdk::mixed_tiles(c->m);
-  for (int k = 0; k + 1 < nt; k++) {
+  for (int k = 0; k < c->kev_pairs; k++) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->kev[2 * k], c->kev[2 * k + 1]) == cudaSuccess) {
       *total_ms += ms;

@@ -46,101 +46,167 @@ __device__ __forceinline__ uint32_t swz_off(int r, int k) {
   return half * kHalfBytes + (r >> 3) * 1024 + (r & 7) * 128 + ((((kk >> 3) ^ (r & 7)) & 7) << 4) + (kk & 7) * 2;
 }
 
-// ------------------------------------------------------------ diagonal block
-__global__ void __launch_bounds__(256) k_diag32(double* A, int lda, int k0, int kb, int* negpiv) {
-  extern __shared__ float sm32[];
-  float (*S)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);   // [row][col]; lower part holds L as it forms
-  __shared__ float diag_s[1];
-  const int tid = threadIdx.x;
-  for (int e = tid; e < kb * kb; e += blockDim.x) {
-    int c = e / kb, rr = e - c * kb;
-    S[rr][c] = (rr >= c) ? (float)A[(size_t)(k0 + c) * lda + k0 + rr] : 0.f;
-  }
-  __syncthreads();
-  // column c: every row r >= c forms s = A[r][c] - sum_{q<c} L[r][q] L[c][q]
-  // as one dot product (four partial sums), then L[c][c] = sqrt(|s_cc|) and
-  // L[r][c] = s_rc / L[c][c]
-  const int r = tid;
-  for (int c = 0; c < kb; c++) {
-    float sv = 0.f;
-    if (r >= c && r < kb) {
-      float s0 = S[r][c], s1 = 0.f, s2 = 0.f, s3 = 0.f;
-      int q = 0;
-      for (; q + 3 < c; q += 4) {
-        s0 = fmaf(-S[r][q], S[c][q], s0);
-        s1 = fmaf(-S[r][q + 1], S[c][q + 1], s1);
-        s2 = fmaf(-S[r][q + 2], S[c][q + 2], s2);
-        s3 = fmaf(-S[r][q + 3], S[c][q + 3], s3);
-      }
-      for (; q < c; q++) s0 = fmaf(-S[r][q], S[c][q], s0);
-      sv = (s0 + s1) + (s2 + s3);
-      if (r == c) {
-        if (sv < 0.f) atomicAdd(negpiv, 1);
-        diag_s[0] = sqrtf(fabsf(sv));
-      }
+// ------------------------------------------------------------ diagonal block + panel
+// One launch per panel k.  Every CTA loads the 128 x 128 diagonal block and
+// factors it in shared memory (the factor is recomputed by each CTA instead
+// of being passed between launches); CTA 0 writes L_kk back, CTA b >= 1
+// solves the 128-row tile k + b:  X L_kk^T = A_ik.
+//
+// Both factorisations work on 32-column blocks, left-looking across blocks:
+// block column j first takes  S[r][c] -= sum_{q < 32 j} S[r][q] L[c][q]  as
+// one FP32 dot product per element (register-tiled 4 x 4 per thread), then
+// the 32 x 32 diagonal block is factored by one warp in registers and the
+// rows below it are solved by forward substitution, one row per thread.
+// A negative pivot is replaced by its absolute value and counted
+// (func.cpp:827-833), by CTA 0 only.
+constexpr int kLd = 132;             // shared row stride (floats): 16-byte rows, conflict-free 4-wide loads
+constexpr int kDpThreads = 256;
+constexpr size_t kDpSmem = (2 * (size_t)kT * kLd + kT) * sizeof(float);
+
+// Out[r][c] -= sum_{q < c0} In[r][q] * Lf[c][q] for r in [r0, r1), c in
+// [c0, c0 + 32) (c < cend); lower-only (r >= c) when `lower`.
+__device__ __forceinline__ void dp_block_update(float (*S)[kLd], const float (*Lf)[kLd], int r0, int r1, int c0,
+                                                int cend, bool lower) {
+  const int t = threadIdx.x;
+  const int g = t & 7, rg = t >> 3;  // 8 column groups x 32 row groups
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
+  for (int q = 0; q < c0; q += 4) {
+    float4 xv[4], lv[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int r = r0 + rg + 32 * i;
+      xv[i] = (r < r1) ? *reinterpret_cast<const float4*>(&S[r][q]) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    __syncthreads();
-    const float piv = diag_s[0];
-    if (r == c) S[c][c] = piv;
-    else if (r > c && r < kb) S[r][c] = sv / piv;
-    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; j++) lv[j] = *reinterpret_cast<const float4*>(&Lf[c0 + g + 8 * j][q]);
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        acc[i][j] = fmaf(xv[i].x, lv[j].x, acc[i][j]);
+        acc[i][j] = fmaf(xv[i].y, lv[j].y, acc[i][j]);
+        acc[i][j] = fmaf(xv[i].z, lv[j].z, acc[i][j]);
+        acc[i][j] = fmaf(xv[i].w, lv[j].w, acc[i][j]);
+      }
   }
-  for (int e = tid; e < kb * kb; e += blockDim.x) {
-    int c = e / kb, rr = e - c * kb;
-    if (rr >= c) A[(size_t)(k0 + c) * lda + k0 + rr] = (double)S[rr][c];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int r = r0 + rg + 32 * i;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int c = c0 + g + 8 * j;
+      if (r < r1 && c < cend && (!lower || r >= c)) S[r][c] -= acc[i][j];
+    }
   }
 }
 
-// ------------------------------------------------------------ panel
-// Rows of the 128-row tile `tile` (row0 = tile*128) solve X L_kk^T = A_ik by
-// forward substitution (one thread per row, the factor in shared memory;
-// backward stable, unlike multiplying by an explicit inverse); the result
-// L_ik is written back (FP32) and split into three BF16 slices stored
-// pre-swizzled at PS + tile*96KB.
-__global__ void __launch_bounds__(128) k_panel32(double* A, int lda, int m, int k0, int kb, int tile0,
-                                                 unsigned char* PS) {
-  extern __shared__ float sm32[];
-  float (*Lk)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32);               // [c][q] factor
-  float (*X)[kT + 1] = reinterpret_cast<float (*)[kT + 1]>(sm32 + kT * (kT + 1));  // [row][q]
-  const int tile = tile0 + blockIdx.x;
+// Forward substitution of one row against the 32 x 32 block of Lf at (c0, c0):
+// x[c] = (b[c] - sum_{q < c} x[q] L[c0+c][c0+q]) / L[c0+c][c0+c], right-looking in registers.
+__device__ __forceinline__ void dp_row_solve(float* row, const float (*Lf)[kLd], const float* invd, int c0, int w) {
+  float x[32];
+#pragma unroll
+  for (int j = 0; j < 32; j++) x[j] = (j < w) ? row[j] : 0.f;
+#pragma unroll
+  for (int c = 0; c < 32; c++) {
+    x[c] *= invd[c0 + c];
+#pragma unroll
+    for (int j = c + 1; j < 32; j++) x[j] = fmaf(-x[c], Lf[c0 + j][c0 + c], x[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 32; j++)
+    if (j < w) row[j] = x[j];
+}
+
+__global__ void __launch_bounds__(kDpThreads, 1) k_dpanel(double* A, int lda, int m, int k0, int kb, int tile0,
+                                                         unsigned char* PS, int* negpiv) {
+  extern __shared__ float4 sm4[];
+  float (*Ls)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);
+  float (*X)[kLd] = reinterpret_cast<float (*)[kLd]>(reinterpret_cast<float*>(sm4) + kT * kLd);
+  float* invd = reinterpret_cast<float*>(sm4) + 2 * kT * kLd;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool is_diag = blockIdx.x == 0;
+  const int tile = tile0 + (int)blockIdx.x - 1;
   const int row0 = tile * kT;
-  const int tid = threadIdx.x;
-  for (int e = tid; e < kT * kT; e += blockDim.x) {
-    int q = e / kT, rr = e - q * kT;  // column-major walk: coalesced
-    int gr = row0 + rr;
-    X[rr][q] = (gr < m && q < kb) ? (float)A[(size_t)(k0 + q) * lda + gr] : 0.f;
-    Lk[rr][q] = (rr >= q && rr < kb && q < kb) ? (float)A[(size_t)(k0 + q) * lda + k0 + rr] : 0.f;
+  const int nrows = is_diag ? 0 : min(kT, m - row0);
+  for (int e = tid; e < kT * kT; e += kDpThreads) {
+    const int c = e >> 7, r = e & (kT - 1);  // column-major walk: coalesced global reads
+    Ls[r][c] = (r >= c && r < kb && c < kb) ? (float)A[(size_t)(k0 + c) * lda + k0 + r] : 0.f;
+    if (!is_diag) X[r][c] = (r < nrows && c < kb) ? (float)A[(size_t)(k0 + c) * lda + row0 + r] : 0.f;
   }
+  if (tid < kT) invd[tid] = 0.f;
   __syncthreads();
-  {
-    const int t = tid;
-    for (int c = 0; c < kb; c++) {
-      float s0 = X[t][c], s1 = 0.f, s2 = 0.f, s3 = 0.f;
-      int q = 0;
-      for (; q + 3 < c; q += 4) {
-        s0 = fmaf(-X[t][q], Lk[c][q], s0);
-        s1 = fmaf(-X[t][q + 1], Lk[c][q + 1], s1);
-        s2 = fmaf(-X[t][q + 2], Lk[c][q + 2], s2);
-        s3 = fmaf(-X[t][q + 3], Lk[c][q + 3], s3);
-      }
-      for (; q < c; q++) s0 = fmaf(-X[t][q], Lk[c][q], s0);
-      X[t][c] = ((s0 + s1) + (s2 + s3)) / Lk[c][c];
+  const int nb = (kb + 31) >> 5;
+  for (int jb = 0; jb < nb; jb++) {
+    const int c0 = 32 * jb, w = min(32, kb - c0);
+    if (jb > 0) {
+      dp_block_update(Ls, Ls, c0, kb, c0, c0 + w, true);
+      __syncthreads();
     }
+    if (warp == 0) {
+      float a[32];
+#pragma unroll
+      for (int j = 0; j < 32; j++) a[j] = (lane < w && j <= lane) ? Ls[c0 + lane][c0 + j] : 0.f;
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        if (c < w) {
+          const float d = __shfl_sync(0xffffffffu, a[c], c);
+          const float piv = sqrtf(fabsf(d));
+          const float inv = 1.f / piv;
+          if (lane == 0) {
+            invd[c0 + c] = inv;
+            if (is_diag && d < 0.f) atomicAdd(negpiv, 1);
+          }
+          if (lane == c) a[c] = piv;
+          else if (lane > c) a[c] *= inv;
+#pragma unroll
+          for (int j = c + 1; j < 32; j++) {
+            const float ljc = __shfl_sync(0xffffffffu, a[c], j);
+            a[j] = fmaf(-a[c], ljc, a[j]);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        if (lane < w && j <= lane) Ls[c0 + lane][c0 + j] = a[j];
+    }
+    __syncthreads();
+    const int rb = c0 + 32;
+    if (rb < kb && tid < kb - rb) dp_row_solve(&Ls[rb + tid][c0], Ls, invd, c0, w);
+    __syncthreads();
   }
-  __syncthreads();
+  if (is_diag) {
+    for (int e = tid; e < kb * kb; e += kDpThreads) {
+      const int c = e / kb, r = e - c * kb;
+      if (r >= c) A[(size_t)(k0 + c) * lda + k0 + r] = (double)Ls[r][c];
+    }
+    return;
+  }
+  for (int jb = 0; jb < nb; jb++) {
+    const int c0 = 32 * jb, w = min(32, kb - c0);
+    if (jb > 0) {
+      dp_block_update(X, Ls, 0, nrows, c0, c0 + w, false);
+      __syncthreads();
+    }
+    if (tid < nrows) dp_row_solve(&X[tid][c0], Ls, invd, c0, w);
+    __syncthreads();
+  }
+  // write L_ik back (FP64) and its three BF16 slices, pre-swizzled
   unsigned char* ps = PS + (size_t)tile * kTileBytes;
-  for (int e = tid; e < kT * kT; e += blockDim.x) {
-    int c = e / kT, r = e - c * kT;
-    int gr = row0 + r;
-    bool in = gr < m && c < kb;
-    float x = in ? X[r][c] : 0.f;
-    if (in) A[(size_t)(k0 + c) * lda + gr] = (double)x;
-    __nv_bfloat16 h = __float2bfloat16_rn(x);
-    float r1 = x - __bfloat162float(h);
-    __nv_bfloat16 md = __float2bfloat16_rn(r1);
-    float r2 = r1 - __bfloat162float(md);
-    __nv_bfloat16 lo = __float2bfloat16_rn(r2);
-    uint32_t off = swz_off(r, c);
+  for (int e = tid; e < kT * kT; e += kDpThreads) {
+    const int c = e >> 7, r = e & (kT - 1);
+    const bool in = r < nrows && c < kb;
+    const float x = in ? X[r][c] : 0.f;
+    if (in) A[(size_t)(k0 + c) * lda + row0 + r] = (double)x;
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    const __nv_bfloat16 md = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(md);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+    const uint32_t off = swz_off(r, c);
     *reinterpret_cast<__nv_bfloat16*>(ps + off) = h;
     *reinterpret_cast<__nv_bfloat16*>(ps + kSliceBytes + off) = md;
     *reinterpret_cast<__nv_bfloat16*>(ps + 2 * kSliceBytes + off) = lo;
@@ -151,7 +217,9 @@ __global__ void __launch_bounds__(128) k_panel32(double* A, int lda, int m, int 
 constexpr int kSyrkThreads = 128;
 constexpr size_t kSyrkSmem = 2 * (size_t)kTileBytes + 1024 + 64;
 
-__global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(double* A, int lda, int m, int kpanel, int nt,
+// Tiles: col_only -> (jlo + blockIdx.x, jlo); otherwise the lower triangle
+// of tiles (I, J) with jlo <= J <= I, from the linear block index.
+__global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(double* A, int lda, int m, int jlo, int col_only,
                                                             const unsigned char* __restrict__ PS, int* err) {
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -159,13 +227,18 @@ __global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(double* A, int lda,
   unsigned char* sB = sm + kTileBytes;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * kTileBytes);  // [0] loads, [1] mma
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
-  // tile (I, J), kpanel < J <= I < nt, from the linear block index
   const int rel = blockIdx.x;
-  int Ip = (int)((sqrtf(8.f * (float)rel + 1.f) - 1.f) * 0.5f);
-  while ((Ip + 1) * (Ip + 2) / 2 <= rel) Ip++;
-  while (Ip * (Ip + 1) / 2 > rel) Ip--;
-  const int Jp = rel - Ip * (Ip + 1) / 2;
-  const int I = kpanel + 1 + Ip, J = kpanel + 1 + Jp;
+  int Ip, Jp;
+  if (col_only) {
+    Ip = rel;
+    Jp = 0;
+  } else {
+    Ip = (int)((sqrtf(8.f * (float)rel + 1.f) - 1.f) * 0.5f);
+    while ((Ip + 1) * (Ip + 2) / 2 <= rel) Ip++;
+    while (Ip * (Ip + 1) / 2 > rel) Ip--;
+    Jp = rel - Ip * (Ip + 1) / 2;
+  }
+  const int I = jlo + Ip, J = jlo + Jp;
   const bool diag = (I == J);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -253,7 +326,9 @@ __global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(double* A, int lda,
 
 namespace bdk {
 
-size_t mixed_panel_bytes(int m) { return (size_t)cdiv(m, kT) * kTileBytes; }
+// two panel-slice buffers: panel k writes buffer k & 1 while the updates of
+// panel k - 1 still read the other
+size_t mixed_panel_bytes(int m) { return 2 * (size_t)cdiv(m, kT) * kTileBytes; }
 int mixed_tiles(int m) { return cdiv(m, kT); }
 
 static bool g_attr_done = false;
@@ -262,35 +337,88 @@ int set_mixed_attributes() {
   if (g_attr_done) return 0;
   cudaError_t e = cudaFuncSetAttribute(k_tc_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSyrkSmem);
   if (e != cudaSuccess) return 1;
-  size_t two = 2 * (size_t)kT * (kT + 1) * sizeof(float);
-  e = cudaFuncSetAttribute(k_diag32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)two);
-  if (e != cudaSuccess) return 1;
-  e = cudaFuncSetAttribute(k_panel32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)two);
+  e = cudaFuncSetAttribute(k_dpanel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDpSmem);
   if (e != cudaSuccess) return 1;
   g_attr_done = true;
   return 0;
 }
 
-// Returns the number of kernel launches.
+int mixed_aux_create(MixedAux* x) {
+  int lo = 0, hi = 0;
+  if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) return 1;
+  x->prio_hi = hi;
+  if (cudaStreamCreateWithPriority(&x->side, cudaStreamNonBlocking, lo) != cudaSuccess) return 1;
+  for (cudaEvent_t* e : {&x->ev_fork, &x->ev_panel, &x->ev_rest})
+    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return 1;
+  return 0;
+}
+
+void mixed_aux_destroy(MixedAux* x) {
+  for (cudaEvent_t* e : {&x->ev_fork, &x->ev_panel, &x->ev_rest})
+    if (*e) cudaEventDestroy(*e), *e = nullptr;
+  if (x->side) cudaStreamDestroy(x->side), x->side = nullptr;
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_prio(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, int prio,
+                        Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Right-looking with a lookahead of one panel, on two streams:
+//   st   : panel k (k_dpanel), then panel k's update of column k+1 (the
+//          next panel), at high priority;
+//   side : panel k's update of the tiles right of column k+1.
+// Panel k+1 is factored while the bulk of panel k's update runs.  Column
+// k+1 is also updated by the side stream's update of panel k-1, so st waits
+// for that one before updating the column; panel k+1's slices go to the
+// other buffer, whose last reader (the side update of panel k-1) is done by
+// then.  Returns the number of kernel launches.
 int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
-                cudaEvent_t* syrk_ev, double* syrk_flop) {
+                const MixedAux& aux, cudaEvent_t* kev, int* kev_pairs, double* kflop) {
   const int nt = cdiv(m, kT);
-  const size_t two = 2 * (size_t)kT * (kT + 1) * sizeof(float);
-  int L = 0;
+  const size_t buf = (size_t)nt * kTileBytes;
+  int L = 0, pairs = 0;
+  cudaEventRecord(aux.ev_fork, st);
+  cudaStreamWaitEvent(aux.side, aux.ev_fork, 0);
+  cudaEventRecord(aux.ev_rest, aux.side);
   for (int k = 0; k < nt; k++) {
     const int k0 = k * kT, kb = (m - k0 < kT) ? m - k0 : kT;
-    k_diag32<<<1, kT, two / 2, st>>>(A, lda, k0, kb, negpiv);
-    L++;
     const int below = nt - k - 1;
+    unsigned char* psk = PS + (size_t)(k & 1) * buf;
+    launch_prio(k_dpanel, below + 1, kDpThreads, kDpSmem, st, aux.prio_hi, A, lda, m, k0, kb, k + 1, psk, negpiv);
+    L++;
     if (below <= 0) break;
-    k_panel32<<<below, 128, two, st>>>(A, lda, m, k0, kb, k + 1, PS);
-    const int pairs = below * (below + 1) / 2;
-    if (syrk_ev) cudaEventRecord(syrk_ev[2 * k], st);
-    k_tc_syrk<<<pairs, kSyrkThreads, kSyrkSmem, st>>>(A, lda, m, k, nt, PS, err);
-    if (syrk_ev) cudaEventRecord(syrk_ev[2 * k + 1], st);
-    if (syrk_flop) *syrk_flop += 6.0 * 2.0 * kT * kT * kT * pairs;  // BF16 tensor work issued
-    L += 2;
+    cudaEventRecord(aux.ev_panel, st);
+    cudaStreamWaitEvent(st, aux.ev_rest, 0);
+    launch_prio(k_tc_syrk, below, kSyrkThreads, kSyrkSmem, st, aux.prio_hi, A, lda, m, k + 1, 1,
+                (const unsigned char*)psk, err);
+    L++;
+    const int rest = below - 1;
+    cudaStreamWaitEvent(aux.side, aux.ev_panel, 0);
+    if (rest > 0) {
+      const int tiles = rest * (rest + 1) / 2;
+      if (kev) cudaEventRecord(kev[2 * pairs], aux.side);
+      k_tc_syrk<<<tiles, kSyrkThreads, kSyrkSmem, aux.side>>>(A, lda, m, k + 2, 0, psk, err);
+      if (kev) cudaEventRecord(kev[2 * pairs + 1], aux.side);
+      pairs++;
+      if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles;  // BF16 tensor work issued
+      L++;
+    }
+    cudaEventRecord(aux.ev_rest, aux.side);
   }
+  cudaStreamWaitEvent(st, aux.ev_rest, 0);
+  if (kev_pairs) *kev_pairs = pairs;
   return L;
 }
 
