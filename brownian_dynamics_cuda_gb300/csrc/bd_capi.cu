@@ -95,7 +95,6 @@ struct bd_ctx {
   std::vector<cudaEvent_t> kev;   // per-launch events around the tensor-core update (timing steps only)
   int kev_pairs = 0;
   double kflop = 0.0;
-  bdk::MixedAux aux;               // mixed path: lookahead stream and events
   // host copies for the drop-in paths
   std::vector<int> h_type;
 };
@@ -153,7 +152,7 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
       const bool kt = c->timing && !c->kev.empty();
       c->kflop = 0.0;
       c->kev_pairs = 0;
-      L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, c->aux, kt ? c->kev.data() : nullptr,
+      L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, kt ? c->kev.data() : nullptr,
                             kt ? &c->kev_pairs : nullptr, kt ? &c->kflop : nullptr);
     }
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
@@ -306,7 +305,6 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
     if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
-    if (bdk::mixed_aux_create(&c->aux)) return fail(set_error(BD_ERR_CUDA, "bd_create: lookahead stream/events"));
   }
   Arena ar{(char*)c->arena_base, tot, 0};
   int *d_type = ar.take<int>(n), *d_core_rank = ar.take<int>(n), *d_core_bead = ar.take<int>(nc),
@@ -423,7 +421,6 @@ extern "C" int bd_destroy(bd_ctx* c) {
   for (int k = 0; k < 10; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (auto ev : c->kev) cudaEventDestroy(ev);
-  bdk::mixed_aux_destroy(&c->aux);
   if (c->A) cudaFree(c->A);
   if (c->PS) cudaFree(c->PS);
   if (c->d_err) cudaFree(c->d_err);
@@ -453,8 +450,7 @@ static int run_step(bd_ctx* c, const double* d_rr, const double* d_p) {
       cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (rc) return rc;
       if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_step: graph capture failed");
-      // per-node priorities: the lookahead panels run ahead of the bulk update
-      e = cudaGraphInstantiate(&c->graph, g, cudaGraphInstantiateFlagUseNodePriority);
+      e = cudaGraphInstantiate(&c->graph, g, 0);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_step: graph instantiation failed");
     }
@@ -561,7 +557,7 @@ static int factor_now(bd_ctx* c) {
   assemble_now(c);
   CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
   if (c->precision == BD_PREC_MIXED) {
-    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream, c->aux);
+    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream);
     int derr = 0;
     CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

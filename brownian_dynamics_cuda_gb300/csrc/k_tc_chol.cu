@@ -3,25 +3,26 @@
 // Right-looking blocked factorisation with 128-wide panels.  The matrix is
 // stored in FP64 (column-major), so each trailing update is rounded at FP64
 // however many panels precede it; the arithmetic is FP32-class:
-//   k_diag32    Cholesky of the 128 x 128 diagonal block in shared memory,
-//               left-looking (each element is one FP32 dot product and one
-//               rounding of its FP64 value, not one rounding per column as a
-//               right-looking FP32 update would do); a negative pivot is
-//               replaced by its absolute value and counted (func.cpp:827-833).
-//   k_panel32   L_ik = A_ik L_kk^-T by forward substitution for every 128-row
-//               tile below the block (FP32), written back and split into three BF16 slices
-//               (hi + mid + lo = the FP32 value exactly), stored pre-swizzled
-//               in the 128-byte-swizzle K-major layout the MMA reads.
-//   k_tc_syrk   trailing update A_IJ -= L_I L_J^T of one 128 x 128 tile per
-//               CTA: both operands' slices are brought into shared memory by
-//               bulk-async copies, six BF16 products (hi.hi, hi.mid, mid.hi,
-//               hi.lo, mid.mid, lo.hi) accumulate in one FP32 tensor-memory
-//               accumulator (tcgen05.mma, M = N = 128, K = 16 per
-//               instruction), and the epilogue reads the accumulator with
-//               tcgen05.ld and updates the FP64 tile.  The dropped products
-//               are below 2^-24 of the kept ones: FP32-class products.
-// Every mbarrier wait is bounded; on a timeout the kernel records an error
-// code, frees its tensor memory and returns.
+//   k_dpanel    one launch per panel: every CTA factors the 128 x 128
+//               diagonal block in shared memory (FP32, 32-column blocks,
+//               left-looking across blocks), CTA 0 writes it back and the
+//               others solve one 128-row tile each, L_ik = A_ik L_kk^-T, by
+//               forward substitution, write it back and split it into three
+//               BF16 slices (hi + mid + lo = the FP32 value exactly), stored
+//               pre-swizzled in the 128-byte-swizzle K-major layout the MMA
+//               reads; a negative pivot is replaced by its absolute value and
+//               counted (func.cpp:827-833).
+//   k_tc_rest   trailing update A_IJ -= L_I L_J^T, a run of tiles per CTA,
+//               warp-specialised: bulk-async operand copies, six BF16
+//               products (hi.hi, hi.mid, mid.hi, hi.lo, mid.mid, lo.hi) into
+//               one of two FP32 tensor-memory accumulators (tcgen05.mma,
+//               M = N = 128, K = 16 per instruction), tcgen05.ld epilogue
+//               into the FP64 tile.  The dropped products are below 2^-24 of
+//               the kept ones: FP32-class products.
+// A one-panel lookahead runs the next panel on a second stream while the
+// bulk update of the current one runs.  Every mbarrier wait is bounded; on
+// a timeout the kernel records an error code, frees its tensor memory and
+// returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -30,6 +31,8 @@
 #include "sm100_ptx.cuh"
 
 namespace {
+
+
 
 constexpr int kT = 128;                 // tile / panel width
 constexpr int kSliceBytes = kT * kT * 2;  // one BF16 slice of a 128 x 128 tile (two 64-column halves)
@@ -121,21 +124,41 @@ __device__ __forceinline__ void dp_row_solve(float* row, const float (*Lf)[kLd],
     if (j < w) row[j] = x[j];
 }
 
-__global__ void __launch_bounds__(kDpThreads, 1) k_dpanel(double* A, int lda, int m, int k0, int kb, int tile0,
-                                                         unsigned char* PS, int* negpiv) {
-  extern __shared__ float4 sm4[];
+// Runs in a CTA of kRestThreads threads; threads >= kDpThreads only take
+// part in the barriers.  `b` is the CTA's index among the panel CTAs.
+__device__ __forceinline__ void dpanel_body(float4* sm4, double* A, int lda, int m, int k0, int kb, int tile0,
+                                            int b, unsigned char* PS, int* negpiv) {
   float (*Ls)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);
   float (*X)[kLd] = reinterpret_cast<float (*)[kLd]>(reinterpret_cast<float*>(sm4) + kT * kLd);
   float* invd = reinterpret_cast<float*>(sm4) + 2 * kT * kLd;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool is_diag = blockIdx.x == 0;
-  const int tile = tile0 + (int)blockIdx.x - 1;
+  const bool work = tid < kDpThreads;
+  const bool is_diag = b == 0;
+  const int tile = tile0 + b - 1;
   const int row0 = tile * kT;
   const int nrows = is_diag ? 0 : min(kT, m - row0);
-  for (int e = tid; e < kT * kT; e += kDpThreads) {
-    const int c = e >> 7, r = e & (kT - 1);  // column-major walk: coalesced global reads
-    Ls[r][c] = (r >= c && r < kb && c < kb) ? (float)A[(size_t)(k0 + c) * lda + k0 + r] : 0.f;
-    if (!is_diag) X[r][c] = (r < nrows && c < kb) ? (float)A[(size_t)(k0 + c) * lda + row0 + r] : 0.f;
+  if (work) {
+    // column-major walk (a warp reads 32 consecutive rows of one column),
+    // 16 columns per batch so that 32 loads per thread are in flight
+    const int r = tid & (kT - 1), cq = tid >> 7;
+    const double* ga = A + (size_t)k0 * lda + k0 + r;
+    const double* gx = A + (size_t)k0 * lda + row0 + r;
+#pragma unroll 1
+    for (int i0 = 0; i0 < kT / 2; i0 += 16) {
+      double va[16], vx[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const int c = cq + 2 * (i0 + i);
+        va[i] = (r >= c && r < kb && c < kb) ? ga[(size_t)c * lda] : 0.0;
+        vx[i] = (!is_diag && r < nrows && c < kb) ? gx[(size_t)c * lda] : 0.0;
+      }
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const int c = cq + 2 * (i0 + i);
+        Ls[r][c] = (float)va[i];
+        X[r][c] = (float)vx[i];
+      }
+    }
   }
   if (tid < kT) invd[tid] = 0.f;
   __syncthreads();
@@ -143,7 +166,7 @@ __global__ void __launch_bounds__(kDpThreads, 1) k_dpanel(double* A, int lda, in
   for (int jb = 0; jb < nb; jb++) {
     const int c0 = 32 * jb, w = min(32, kb - c0);
     if (jb > 0) {
-      dp_block_update(Ls, Ls, c0, kb, c0, c0 + w, true);
+      if (work) dp_block_update(Ls, Ls, c0, kb, c0, c0 + w, true);
       __syncthreads();
     }
     if (warp == 0) {
@@ -179,147 +202,307 @@ __global__ void __launch_bounds__(kDpThreads, 1) k_dpanel(double* A, int lda, in
     __syncthreads();
   }
   if (is_diag) {
-    for (int e = tid; e < kb * kb; e += kDpThreads) {
-      const int c = e / kb, r = e - c * kb;
-      if (r >= c) A[(size_t)(k0 + c) * lda + k0 + r] = (double)Ls[r][c];
-    }
+    if (work)
+      for (int e = tid; e < kb * kb; e += kDpThreads) {
+        const int c = e / kb, r = e - c * kb;
+        if (r >= c) A[(size_t)(k0 + c) * lda + k0 + r] = (double)Ls[r][c];
+      }
     return;
   }
   for (int jb = 0; jb < nb; jb++) {
     const int c0 = 32 * jb, w = min(32, kb - c0);
     if (jb > 0) {
-      dp_block_update(X, Ls, 0, nrows, c0, c0 + w, false);
+      if (work) dp_block_update(X, Ls, 0, nrows, c0, c0 + w, false);
       __syncthreads();
     }
     if (tid < nrows) dp_row_solve(&X[tid][c0], Ls, invd, c0, w);
     __syncthreads();
   }
-  // write L_ik back (FP64) and its three BF16 slices, pre-swizzled
+  // write L_ik back (FP64) and its three BF16 slices, pre-swizzled: each
+  // thread takes one row and 8 consecutive columns, i.e. one 16-byte chunk
+  // of each slice (consecutive lanes: consecutive rows, coalesced FP64 stores)
   unsigned char* ps = PS + (size_t)tile * kTileBytes;
-  for (int e = tid; e < kT * kT; e += kDpThreads) {
-    const int c = e >> 7, r = e & (kT - 1);
-    const bool in = r < nrows && c < kb;
-    const float x = in ? X[r][c] : 0.f;
-    if (in) A[(size_t)(k0 + c) * lda + row0 + r] = (double)x;
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    const float r1 = x - __bfloat162float(h);
-    const __nv_bfloat16 md = __float2bfloat16_rn(r1);
-    const float r2 = r1 - __bfloat162float(md);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
-    const uint32_t off = swz_off(r, c);
-    *reinterpret_cast<__nv_bfloat16*>(ps + off) = h;
-    *reinterpret_cast<__nv_bfloat16*>(ps + kSliceBytes + off) = md;
-    *reinterpret_cast<__nv_bfloat16*>(ps + 2 * kSliceBytes + off) = lo;
+  double* gout = A + (size_t)k0 * lda + row0;
+#pragma unroll 1
+  for (int e = tid; work && e < kT * (kT / 8); e += kDpThreads) {
+    const int r = e & (kT - 1), c0 = (e >> 7) * 8;
+    const float4 x0 = *reinterpret_cast<const float4*>(&X[r][c0]);
+    const float4 x1 = *reinterpret_cast<const float4*>(&X[r][c0 + 4]);
+    const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+    uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const bool in = r < nrows && c0 + j < kb;
+      const float x = in ? xs[j] : 0.f;
+      if (in) gout[(size_t)(c0 + j) * lda + r] = (double)x;
+      // x = hi + mid + lo exactly (8 + 8 + 8 significant bits)
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      const float r1 = x - __bfloat162float(h);
+      const __nv_bfloat16 md = __float2bfloat16_rn(r1);
+      const float r2 = r1 - __bfloat162float(md);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+      const uint32_t sh = (j & 1) * 16;
+      if ((j & 1) == 0) hw[j >> 1] = mw[j >> 1] = lw[j >> 1] = 0u;
+      hw[j >> 1] |= (uint32_t)__bfloat16_as_ushort(h) << sh;
+      mw[j >> 1] |= (uint32_t)__bfloat16_as_ushort(md) << sh;
+      lw[j >> 1] |= (uint32_t)__bfloat16_as_ushort(lo) << sh;
+    }
+    const uint32_t off = swz_off(r, c0);
+    *reinterpret_cast<uint4*>(ps + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(ps + kSliceBytes + off) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+    *reinterpret_cast<uint4*>(ps + 2 * kSliceBytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
 }
 
 // ------------------------------------------------------------ tensor-core trailing update
-constexpr int kSyrkThreads = 128;
-constexpr size_t kSyrkSmem = 2 * (size_t)kTileBytes + 1024 + 64;
+// A_IJ -= L_I L_J^T for a run of up to `group` consecutive tiles per CTA
+// (row-major order over the tile triangle, so consecutive tiles share I and
+// the A operand stays in shared memory).  Warp-specialised, pipelined:
+//   warp 0 (one lane)  bulk-async copies: the three A slices when I changes,
+//                      the three B slices per tile in two K-halves (two
+//                      48 KB stages), and an L2 prefetch of the FP64 tile;
+//   warp 1 (one lane)  six BF16 products per K-half into one of two TMEM
+//                      accumulators (128 columns each), tcgen05.commit to
+//                      release stages, the accumulator and the A operand;
+//   warps 2-9          epilogue: tcgen05.ld of the accumulator (warp w reads
+//                      TMEM lanes 32 (w % 4) .. + 31, half of the columns),
+//                      release it, then the FP64 read-modify-write.
+// So the next tile's copies and MMAs run under the current tile's epilogue.
+// Every wait is bounded; a timeout records an error code and raises a
+// shared abort flag that ends every role's loop; copies still in flight
+// are waited for (bounded) and TMEM is freed before the CTA exits.
+#ifndef BD_REST_PREFETCH
+#define BD_REST_PREFETCH 0  // L2 prefetch of the FP64 tile ahead of the epilogue (measured slower)
+#endif
+#ifndef BD_REST_GROUP
+#define BD_REST_GROUP 0  // tiles per CTA; 0: from the tile count
+#endif
+constexpr int kRestThreads = 320;
+constexpr int kStageBytes = kTileSlices * kHalfBytes;  // one K-half of the three B slices
+constexpr size_t kRestSmem = (size_t)kTileBytes + 2 * kStageBytes + 1024 + 256;
+constexpr int kAccCols = 128;
 
-// Tiles: col_only -> (jlo + blockIdx.x, jlo); otherwise the lower triangle
-// of tiles (I, J) with jlo <= J <= I, from the linear block index.
-__global__ void __launch_bounds__(kSyrkThreads, 1) k_tc_syrk(double* A, int lda, int m, int jlo, int col_only,
-                                                            const unsigned char* __restrict__ PS, int* err) {
-  extern __shared__ unsigned char smraw[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
-  unsigned char* sA = sm;
-  unsigned char* sB = sm + kTileBytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * kTileBytes);  // [0] loads, [1] mma
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
-  const int rel = blockIdx.x;
-  int Ip, Jp;
+struct RestBars {
+  uint64_t fullA, emptyA, fullB[2], emptyB[2], accFull[2], accEmpty[2], done;
+};
+
+__device__ __forceinline__ void rest_tile(int t, int jlo, int col_only, int& I, int& J) {
   if (col_only) {
-    Ip = rel;
-    Jp = 0;
-  } else {
-    Ip = (int)((sqrtf(8.f * (float)rel + 1.f) - 1.f) * 0.5f);
-    while ((Ip + 1) * (Ip + 2) / 2 <= rel) Ip++;
-    while (Ip * (Ip + 1) / 2 > rel) Ip--;
-    Jp = rel - Ip * (Ip + 1) / 2;
+    I = jlo + t;
+    J = jlo;
+    return;
   }
-  const int I = jlo + Ip, J = jlo + Jp;
-  const bool diag = (I == J);
+  int Ip = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+  while ((Ip + 1) * (Ip + 2) / 2 <= t) Ip++;
+  while (Ip * (Ip + 1) / 2 > t) Ip--;
+  I = jlo + Ip;
+  J = jlo + (t - Ip * (Ip + 1) / 2);
+}
+
+// `cta` is the CTA's index among the update CTAs.
+__device__ __forceinline__ void rest_body(unsigned char* smraw, double* A, int lda, int m, int jlo, int col_only,
+                                          int ntiles, int group, int cta, const unsigned char* __restrict__ PS,
+                                          int* err) {
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  unsigned char* sA = sm;                 // 3 slices x 32 KB
+  unsigned char* sB = sm + kTileBytes;    // 2 stages x (3 slices x 16 KB)
+  RestBars* bars = reinterpret_cast<RestBars*>(sm + kTileBytes + 2 * kStageBytes);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t0 = cta * group, t1 = min(t0 + group, ntiles);
   if (threadIdx.x == 0) {
-    sm100::mbar_init(&bars[0], 1);
-    sm100::mbar_init(&bars[1], 1);
+    sm100::mbar_init(&bars->fullA, 1);
+    sm100::mbar_init(&bars->emptyA, 1);
+    for (int h = 0; h < 2; h++) {
+      sm100::mbar_init(&bars->fullB[h], 1);
+      sm100::mbar_init(&bars->emptyB[h], 1);
+      sm100::mbar_init(&bars->accFull[h], 1);
+      sm100::mbar_init(&bars->accEmpty[h], 8);
+    }
+    sm100::mbar_init(&bars->done, 1);
+    *abort_flag = 0;
     sm100::fence_mbar_init();
   }
-  if (warp == 0) sm100::tmem_alloc(tslot, 128);
+  if (warp == 1) sm100::tmem_alloc(tslot, 2 * kAccCols);
   sm100::tc_fence_before();
   __syncthreads();
   sm100::tc_fence_after();
   const uint32_t tmem = *tslot;
-  uint32_t* okflag = tslot + 1;
-  if (threadIdx.x == 0) {
-    const uint32_t bytes = diag ? kTileBytes : 2 * kTileBytes;
-    sm100::mbar_arrive_expect_tx(&bars[0], bytes);
-    const unsigned char* gA = PS + (size_t)I * kTileBytes;
-    const unsigned char* gB = PS + (size_t)J * kTileBytes;
-    for (int s = 0; s < kTileSlices; s++) sm100::bulk_g2s(sA + s * kSliceBytes, gA + s * kSliceBytes, kSliceBytes, &bars[0]);
-    if (!diag)
-      for (int s = 0; s < kTileSlices; s++) sm100::bulk_g2s(sB + s * kSliceBytes, gB + s * kSliceBytes, kSliceBytes, &bars[0]);
-    bool ok = sm100::mbar_wait(&bars[0], 0, kWaitLimit);
-    if (ok) {
-      sm100::tc_fence_after();
-      const unsigned char* bB = diag ? sA : sB;
-      const uint32_t idesc = sm100::idesc_bf16_f32(128, 128);
-      // (A slice, B slice) products, smallest first
-      const int pa[6] = {2, 1, 0, 1, 0, 0};
-      const int pb[6] = {0, 1, 2, 0, 1, 0};
-      uint32_t accum = 0;
-      for (int t = 0; t < 6; t++) {
-        for (int h = 0; h < 2; h++) {
-          for (int kk = 0; kk < 4; kk++) {
-            uint32_t aaddr = sm100::smem_u32(sA + pa[t] * kSliceBytes + h * kHalfBytes) + kk * 32;
-            uint32_t baddr = sm100::smem_u32(bB + pb[t] * kSliceBytes + h * kHalfBytes) + kk * 32;
-            sm100::mma_bf16(tmem, sm100::desc_kmajor_sw128(aaddr), sm100::desc_kmajor_sw128(baddr), idesc, accum);
-            accum = 1;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- producer
+      int curI = -1;
+      uint32_t nA = 0, nfill[2] = {0, 0};
+      bool ok = true;
+      for (int t = t0; t < t1 && ok; t++) {
+        int I, J;
+        rest_tile(t, jlo, col_only, I, J);
+        if (I != curI) {
+          if (nA > 0) ok = sm100::mbar_wait(&bars->emptyA, (nA - 1) & 1, kWaitLimit);
+          if (!ok || *abort_flag) break;
+          sm100::mbar_arrive_expect_tx(&bars->fullA, kTileBytes);
+          const unsigned char* g = PS + (size_t)I * kTileBytes;
+          for (int s2 = 0; s2 < kTileSlices; s2++)
+            sm100::bulk_g2s(sA + s2 * kSliceBytes, g + s2 * kSliceBytes, kSliceBytes, &bars->fullA);
+          curI = I;
+          nA++;
+        }
+        if (BD_REST_PREFETCH) {  // the FP64 tile's columns into L2 ahead of the epilogue
+          const int rows = min(kT, lda - I * kT);
+          const int jend = min(J * kT + kT, m);
+          for (int gj = J * kT; gj < jend; gj++)
+            sm100::prefetch_l2(A + (size_t)gj * lda + (size_t)I * kT, (uint32_t)rows * 8u);
+        }
+        for (int h = 0; h < 2 && ok; h++) {
+          if (nfill[h] > 0) ok = sm100::mbar_wait(&bars->emptyB[h], (nfill[h] - 1) & 1, kWaitLimit);
+          if (!ok || *abort_flag) {
+            ok = false;
+            break;
           }
+          if (I == J) {
+            sm100::mbar_arrive(&bars->fullB[h]);  // diagonal tile: B is the A operand
+          } else {
+            sm100::mbar_arrive_expect_tx(&bars->fullB[h], kStageBytes);
+            const unsigned char* g = PS + (size_t)J * kTileBytes + h * kHalfBytes;
+            for (int s2 = 0; s2 < kTileSlices; s2++)
+              sm100::bulk_g2s(sB + h * kStageBytes + s2 * kHalfBytes, g + s2 * kSliceBytes, kHalfBytes,
+                              &bars->fullB[h]);
+          }
+          nfill[h]++;
         }
       }
-      sm100::mma_commit(&bars[1]);
-    } else {
-      atomicExch(err, 1);
-      // let the copies still in flight land before the CTA exits
-      (void)sm100::mbar_wait(&bars[0], 0, kWaitLimit);
-    }
-    *okflag = ok ? 1u : 0u;
-  }
-  __syncthreads();
-  const bool loaded = *okflag != 0;
-  const bool mma_done = loaded && sm100::mbar_wait(&bars[1], 0, kWaitLimit);
-  const int all_ok = __syncthreads_and(mma_done ? 1 : 0);
-  if (all_ok) {
-    sm100::tc_fence_after();
-    const int i = 32 * warp + lane;
-    const int gi = I * kT + i;
-    const bool row_ok = gi < m;
-    for (int c = 0; c < 4; c++) {
-      double old[32];
-      float v[32];
-      const int gj0 = J * kT + 32 * c;
-      // all loads of the chunk first (independent), then the subtracts and stores
-#pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const int gj = gj0 + j;
-        const bool ok2 = row_ok && gj < m && (!diag || gi >= gj);
-        old[j] = ok2 ? A[(size_t)gj * lda + gi] : 0.0;
+      if (!ok) {
+        atomicExch(err, 3);
+        *abort_flag = 1;
       }
-      sm100::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);
+      // copies still in flight land before the CTA exits
+      for (int h = 0; h < 2; h++)
+        if (nfill[h] > 0) (void)sm100::mbar_wait(&bars->fullB[h], (nfill[h] - 1) & 1, kWaitLimit);
+      if (nA > 0) (void)sm100::mbar_wait(&bars->fullA, (nA - 1) & 1, kWaitLimit);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      const uint32_t idesc = sm100::idesc_bf16_f32(128, 128);
+      const int pa[6] = {2, 1, 0, 1, 0, 0};  // (A slice, B slice) products, smallest first
+      const int pb[6] = {0, 1, 2, 0, 1, 0};
+      int curI = -1;
+      uint32_t nA = 0;
+      bool ok = true;
+      int n = 0;
+      for (int t = t0; t < t1; t++, n++) {
+        int I, J;
+        rest_tile(t, jlo, col_only, I, J);
+        if (*abort_flag) break;
+        if (I != curI) {
+          ok = sm100::mbar_wait(&bars->fullA, nA & 1, kWaitLimit);
+          if (!ok) break;
+          curI = I;
+          nA++;
+        }
+        const int acc = n & 1;
+        if (n >= 2) {
+          ok = sm100::mbar_wait(&bars->accEmpty[acc], ((n >> 1) - 1) & 1, kWaitLimit);
+          if (!ok) break;
+        }
+        sm100::tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(acc * kAccCols);
+        for (int h = 0; h < 2 && ok; h++) {
+          ok = sm100::mbar_wait(&bars->fullB[h], n & 1, kWaitLimit);
+          if (!ok) break;
+          sm100::tc_fence_after();
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const int gj = gj0 + j;
-        if (row_ok && gj < m && (!diag || gi >= gj)) A[(size_t)gj * lda + gi] = old[j] - (double)v[j];
+          for (int p = 0; p < 6; p++) {
+            const uint32_t aaddr = sm100::smem_u32(sA + pa[p] * kSliceBytes + h * kHalfBytes);
+            const uint32_t baddr = (I == J) ? sm100::smem_u32(sA + pb[p] * kSliceBytes + h * kHalfBytes)
+                                            : sm100::smem_u32(sB + h * kStageBytes + pb[p] * kHalfBytes);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+              sm100::mma_bf16(d, sm100::desc_kmajor_sw128(aaddr + kk * 32), sm100::desc_kmajor_sw128(baddr + kk * 32),
+                              idesc, (h | p | kk) != 0);
+          }
+          sm100::mma_commit(&bars->emptyB[h]);
+        }
+        if (!ok) break;
+        sm100::mma_commit(&bars->accFull[acc]);
+        int In = -1, Jn;
+        if (t + 1 < t1) rest_tile(t + 1, jlo, col_only, In, Jn);
+        if (In != I) sm100::mma_commit(&bars->emptyA);
+      }
+      if (!ok) {
+        atomicExch(err, 4);
+        *abort_flag = 1;
+      }
+      // every MMA issued has finished before TMEM is freed
+      sm100::mma_commit(&bars->done);
+      (void)sm100::mbar_wait(&bars->done, 0, kWaitLimit);
+    }
+  } else {
+    // ---------------- epilogue
+    const int q = warp & 3, ch = (warp - 2) >> 2;
+    int n = 0;
+    for (int t = t0; t < t1; t++, n++) {
+      int I, J;
+      rest_tile(t, jlo, col_only, I, J);
+      const int acc = n & 1;
+      const bool ok = sm100::mbar_wait(&bars->accFull[acc], (n >> 1) & 1, kWaitLimit);
+      if (!ok || *abort_flag) {
+        if (!ok && lane == 0) {
+          atomicExch(err, 5);
+          *abort_flag = 1;
+        }
+        break;
+      }
+      sm100::tc_fence_after();
+      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * kAccCols + 64 * ch);
+      const int gi = I * kT + 32 * q + lane;
+      const bool diag = I == J;
+      const bool row_ok = gi < m;
+      // columns [jlim0, jlim1) of this thread's row are inside the matrix and the lower triangle
+      const int cbase = J * kT + 64 * ch;
+      const int jlim0 = diag ? max(0, gi - cbase + 1) : 64;  // diagonal tile: columns <= gi
+      const int jcnt = row_ok ? min(min(jlim0, 64), m - cbase) : 0;
+      double* colp = A + (size_t)cbase * lda + gi;
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        double old[32];
+        float v[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) old[j] = (32 * c + j < jcnt) ? colp[(size_t)(32 * c + j) * lda] : 0.0;
+        sm100::tmem_ld32(ta + 32 * c, v);
+        if (c == 1) {  // accumulator read out: hand it back to the MMA issuer
+          sm100::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) sm100::mbar_arrive(&bars->accEmpty[acc]);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (32 * c + j < jcnt) colp[(size_t)(32 * c + j) * lda] = old[j] - (double)v[j];
       }
     }
-  } else if (threadIdx.x == 0 && loaded) {
-    atomicExch(err, 2);
   }
   sm100::tc_fence_before();
   __syncthreads();
-  if (warp == 0) sm100::tmem_dealloc(tmem, 128);
+  if (warp == 1) sm100::tmem_dealloc(tmem, 2 * kAccCols);
+}
+
+// One launch per panel step: CTAs [0, ndp) factor panel pk (diagonal block
+// and the tiles below it, writing its slices to PSp); the remaining CTAs
+// apply an earlier panel's trailing update (tiles from jlo, slices PSu).
+// The two parts touch disjoint columns and slice buffers.
+__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(double* A, int lda, int m, int ndp, int pk0, int pkb,
+                                                              unsigned char* PSp, int* negpiv, int jlo, int col_only,
+                                                              int ntiles, int group,
+                                                              const unsigned char* __restrict__ PSu, int* err) {
+  extern __shared__ float4 smem4[];
+  if ((int)blockIdx.x < ndp) {
+    dpanel_body(smem4, A, lda, m, pk0, pkb, pk0 / kT + 1, (int)blockIdx.x, PSp, negpiv);
+    return;
+  }
+  rest_body(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group, (int)blockIdx.x - ndp,
+            PSu, err);
 }
 
 }  // namespace
@@ -335,91 +518,67 @@ static bool g_attr_done = false;
 
 int set_mixed_attributes() {
   if (g_attr_done) return 0;
-  cudaError_t e = cudaFuncSetAttribute(k_tc_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSyrkSmem);
-  if (e != cudaSuccess) return 1;
-  e = cudaFuncSetAttribute(k_dpanel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDpSmem);
+  static_assert(kDpSmem <= kRestSmem, "panel CTAs run inside the update kernel's shared memory");
+  cudaError_t e = cudaFuncSetAttribute(k_chol_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRestSmem);
   if (e != cudaSuccess) return 1;
   g_attr_done = true;
   return 0;
 }
 
-int mixed_aux_create(MixedAux* x) {
-  int lo = 0, hi = 0;
-  if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) return 1;
-  x->prio_hi = hi;
-  if (cudaStreamCreateWithPriority(&x->side, cudaStreamNonBlocking, lo) != cudaSuccess) return 1;
-  for (cudaEvent_t* e : {&x->ev_fork, &x->ev_panel, &x->ev_rest})
-    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return 1;
-  return 0;
+// Tiles per CTA of the bulk update: enough CTAs to fill the GPU about three
+// times over, at most 8 tiles each.
+static int rest_group(int tiles) {
+  if (BD_REST_GROUP > 0) return BD_REST_GROUP;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  int g = tiles / (3 * sms);
+  return g < 1 ? 1 : (g > 8 ? 8 : g);
 }
 
-void mixed_aux_destroy(MixedAux* x) {
-  for (cudaEvent_t* e : {&x->ev_fork, &x->ev_panel, &x->ev_rest})
-    if (*e) cudaEventDestroy(*e), *e = nullptr;
-  if (x->side) cudaStreamDestroy(x->side), x->side = nullptr;
-}
-
-template <typename... KArgs, typename... Args>
-static void launch_prio(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, int prio,
-                        Args... args) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributePriority;
-  at[0].val.priority = prio;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
-// Right-looking with a lookahead of one panel, on two streams:
-//   st   : panel k (k_dpanel), then panel k's update of column k+1 (the
-//          next panel), at high priority;
-//   side : panel k's update of the tiles right of column k+1.
-// Panel k+1 is factored while the bulk of panel k's update runs.  Column
-// k+1 is also updated by the side stream's update of panel k-1, so st waits
-// for that one before updating the column; panel k+1's slices go to the
-// other buffer, whose last reader (the side update of panel k-1) is done by
-// then.  Returns the number of kernel launches.
+// Right-looking with a lookahead of one panel, on one stream.  Step k:
+//   launch 1: panel k's update of column k+1 (the next panel's tiles);
+//   launch 2: panel k+1 (extra CTAs) together with panel k's update of the
+//             tiles right of column k+1.
+// Panel k+1 needs only column k+1, so it is factored inside the launch that
+// carries the bulk of panel k's update; the two parts write disjoint
+// columns, and panel k+1's slices go to the other buffer.  No two kernels
+// run at the same time.  Returns the number of kernel launches.
 int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
-                const MixedAux& aux, cudaEvent_t* kev, int* kev_pairs, double* kflop) {
+                cudaEvent_t* kev, int* kev_pairs, double* kflop) {
   const int nt = cdiv(m, kT);
   const size_t buf = (size_t)nt * kTileBytes;
   int L = 0, pairs = 0;
-  cudaEventRecord(aux.ev_fork, st);
-  cudaStreamWaitEvent(aux.side, aux.ev_fork, 0);
-  cudaEventRecord(aux.ev_rest, aux.side);
-  for (int k = 0; k < nt; k++) {
-    const int k0 = k * kT, kb = (m - k0 < kT) ? m - k0 : kT;
+  auto kb_of = [&](int k) { return (m - k * kT < kT) ? m - k * kT : kT; };
+  // panel 0 alone
+  k_chol_step<<<nt, kRestThreads, kRestSmem, st>>>(A, lda, m, nt, 0, kb_of(0), PS, negpiv, 0, 0, 0, 1, PS, err);
+  L++;
+  for (int k = 0; k + 1 < nt; k++) {
     const int below = nt - k - 1;
-    unsigned char* psk = PS + (size_t)(k & 1) * buf;
-    launch_prio(k_dpanel, below + 1, kDpThreads, kDpSmem, st, aux.prio_hi, A, lda, m, k0, kb, k + 1, psk, negpiv);
-    L++;
-    if (below <= 0) break;
-    cudaEventRecord(aux.ev_panel, st);
-    cudaStreamWaitEvent(st, aux.ev_rest, 0);
-    launch_prio(k_tc_syrk, below, kSyrkThreads, kSyrkSmem, st, aux.prio_hi, A, lda, m, k + 1, 1,
-                (const unsigned char*)psk, err);
+    const unsigned char* psk = PS + (size_t)(k & 1) * buf;
+    unsigned char* psn = PS + (size_t)((k + 1) & 1) * buf;
+    k_chol_step<<<below, kRestThreads, kRestSmem, st>>>(A, lda, m, 0, 0, 0, psn, negpiv, k + 1, 1, below, 1, psk,
+                                                         err);
     L++;
     const int rest = below - 1;
-    cudaStreamWaitEvent(aux.side, aux.ev_panel, 0);
-    if (rest > 0) {
-      const int tiles = rest * (rest + 1) / 2;
-      if (kev) cudaEventRecord(kev[2 * pairs], aux.side);
-      k_tc_syrk<<<tiles, kSyrkThreads, kSyrkSmem, aux.side>>>(A, lda, m, k + 2, 0, psk, err);
-      if (kev) cudaEventRecord(kev[2 * pairs + 1], aux.side);
-      pairs++;
-      if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles;  // BF16 tensor work issued
-      L++;
-    }
-    cudaEventRecord(aux.ev_rest, aux.side);
+    const int tiles = rest * (rest + 1) / 2;
+    const int group = tiles > 0 ? rest_group(tiles) : 1;
+    const int ndp = nt - k - 1;  // panel k+1: its diagonal block and the tiles below it
+    if (kev) cudaEventRecord(kev[2 * pairs], st);
+    k_chol_step<<<ndp + cdiv(tiles, group), kRestThreads, kRestSmem, st>>>(
+        A, lda, m, ndp, (k + 1) * kT, kb_of(k + 1), psn, negpiv, k + 2, 0, tiles, group, psk, err);
+    if (kev) cudaEventRecord(kev[2 * pairs + 1], st);
+    pairs++;
+    if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles;  // BF16 tensor work issued
+    L++;
   }
-  cudaStreamWaitEvent(st, aux.ev_rest, 0);
   if (kev_pairs) *kev_pairs = pairs;
   return L;
 }
 
 }  // namespace bdk
+

@@ -53,3 +53,18 @@ def test_cfg1_mixed_vs_fp64_displacement(cfg1):
         d64 = a.get(k) - cfg1.state[k]
         dm = b.get(k) - cfg1.state[k]
         assert np.abs(dm - d64).max() <= 1e-6 * np.abs(d64).max(), k
+
+
+def test_cfg1_mixed_factor_matches_fp64(cfg1):
+    """The tensor-core factor of the 3N = 11,700 tensor agrees with the FP64
+    factor tile by tile (FP32-class: within 2e-6 of max |L|), twice in a row
+    on one context (the second factorisation reuses the panel buffers)."""
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
+    L64 = Context(cfg1, precision=PREC_FP64).cholesky()
+    cm = Context(cfg1, precision=PREC_MIXED)
+    scale = np.abs(L64).max()
+    for _ in range(2):
+        Lm = cm.cholesky()
+        assert cm.negative_pivots() == 0
+        assert np.isfinite(Lm).all()
+        assert np.abs(Lm - L64).max() <= 2e-6 * scale
