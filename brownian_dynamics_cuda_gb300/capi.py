@@ -103,6 +103,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.bd_launch_count.argtypes = [C.c_void_p, _ip]
     L.bd_kernel_time.argtypes = [C.c_void_p, C.POINTER(C.c_float), _ip, _dp]
+    L.bd_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, _ip]
     L.bd_negative_pivots.argtypes = [C.c_void_p, _ip]
     _lib = L
     return L
@@ -357,6 +358,13 @@ class Context:
         ms, n, fl = C.c_float(), C.c_int(), C.c_double()
         _check(self._L.bd_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(fl)))
         return ms.value, n.value, fl.value
+
+    def kernel_times(self) -> np.ndarray:
+        """Per-launch ms of the tensor-core update launches of the last timed step."""
+        out = (C.c_float * 4096)()
+        n = C.c_int()
+        _check(self._L.bd_kernel_times(self._h, out, 4096, C.byref(n)))
+        return np.array(list(out)[:min(n.value, 4096)])
 
     def launch_count(self) -> int:
         v = C.c_int()

@@ -142,7 +142,7 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   bool rebuild = (c->step_count % c->freq_rp) == 0;
   const bool mixed = c->precision == BD_PREC_MIXED;
   if (rebuild) {
-    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st);
+    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed);
     L++;
   }
   record(c, 1);
@@ -158,7 +158,7 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
   }
   record(c, 2);
-  bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st);
+  bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st, mixed);
   L += 2;
   record(c, 3);
   L += bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
@@ -531,6 +531,13 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
   CK(cudaMemcpyAsync(h.data(), c->A, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   const int m = c->m;
+  if (c->precision == BD_PREC_MIXED) {  // double-float pairs (hi, lo) -> FP64
+    for (size_t e = 0; e < h.size(); e++) {
+      float f[2];
+      std::memcpy(f, &h[e], sizeof f);
+      h[e] = (double)f[0] + (double)f[1];
+    }
+  }
   for (int i = 0; i < m; i++)
     for (int j = 0; j < m; j++) {
       double v;
@@ -543,7 +550,8 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
 
 static void assemble_now(bd_ctx* c) {
   bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
-  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream);
+  bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream,
+                    c->precision == BD_PREC_MIXED);
 }
 
 extern "C" int bd_diffusion_tensor(bd_ctx* c, double* D) {
@@ -581,7 +589,8 @@ extern "C" int bd_noise_displacement(bd_ctx* c, const double* p, double* rd) {
   int rc = factor_now(c);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream);
+  bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream,
+                     c->precision == BD_PREC_MIXED);
   CK(cudaMemcpyAsync(rd, c->rd, (size_t)c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return BD_OK;
@@ -656,6 +665,20 @@ extern "C" int bd_phase_times(bd_ctx* c, float* out9) {
   CK(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < 8; k++) cudaEventElapsedTime(&out9[k], c->ev[k], c->ev[k + 1]);
   cudaEventElapsedTime(&out9[8], c->ev[0], c->ev[8]);
+  return BD_OK;
+}
+
+extern "C" int bd_kernel_times(bd_ctx* c, float* out_ms, int max, int* launches) {
+  if (!c || !launches || (max > 0 && !out_ms)) return set_error(BD_ERR_ARG, "bd_kernel_times: bad argument");
+  *launches = 0;
+  if (c->precision != BD_PREC_MIXED || !c->timing) return BD_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < c->kev_pairs; k++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->kev[2 * k], c->kev[2 * k + 1]) != cudaSuccess) ms = -1.f;
+    if (*launches < max) out_ms[*launches] = ms;
+    (*launches)++;
+  }
   return BD_OK;
 }
 

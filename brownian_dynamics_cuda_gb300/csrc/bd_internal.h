@@ -114,8 +114,9 @@ void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream
 // returns the number of kernels launched
 int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);
 // rpy_chol.cu
+// df: store each element as the double-float pair (hi, lo) of FP32 (mixed path)
 void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
-                  cudaStream_t st);
+                  cudaStream_t st, bool df = false);
 int potrf_fp64(int m, double* A, int lda, double* rd_acc, const double* p, double s2dt, int* d_negpiv,
                cudaStream_t st);
 size_t trmv_scratch_doubles(int m);
@@ -130,5 +131,5 @@ int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* 
 int mixed_tiles(int m);
 
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
-                   cudaStream_t st);
+                   cudaStream_t st, bool df = false);
 }  // namespace bdk

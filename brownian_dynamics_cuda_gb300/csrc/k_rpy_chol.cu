@@ -25,6 +25,19 @@ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 // ------------------------------------------------------------ RPY
 constexpr int kRpyTile = 32;
 
+// element store: FP64, or the double-float pair (hi, lo) of the mixed path
+template <bool DF>
+__device__ __forceinline__ void st_elem(double* A, size_t idx, double x) {
+  if (DF) {
+    const float hi = __double2float_rn(x);
+    const float lo = __double2float_rn(x - (double)hi);
+    reinterpret_cast<float2*>(A)[idx] = make_float2(hi, lo);
+  } else {
+    A[idx] = x;
+  }
+}
+
+template <bool DF>
 __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ r, const double* __restrict__ rad,
                                              double a1, double a2, double* __restrict__ A, int lda) {
   int bi = blockIdx.y, bj = blockIdx.x;
@@ -38,7 +51,7 @@ __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ 
     if (j >= nD || j > i) continue;
     if (j == i) {
       for (int l = 0; l < 3; l++)
-        for (int k = l; k < 3; k++) A[(size_t)(3 * j + l) * lda + 3 * i + k] = (k == l) ? a1 / radi : 0.0;
+        for (int k = l; k < 3; k++) st_elem<DF>(A, (size_t)(3 * j + l) * lda + 3 * i + k, (k == l) ? a1 / radi : 0.0);
       continue;
     }
     V3 rj = ld3(r + 3 * j);
@@ -49,8 +62,8 @@ __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ 
     double Db[3][3];
     rpy_block(sij, ssq, s, radi, radj, a1, a2, Db);
     for (int l = 0; l < 3; l++) {
-      double* col = A + (size_t)(3 * j + l) * lda + 3 * i;
-      for (int k = 0; k < 3; k++) col[k] = Db[k][l];
+      const size_t col = (size_t)(3 * j + l) * lda + 3 * i;
+      for (int k = 0; k < 3; k++) st_elem<DF>(A, col + k, Db[k][l]);
     }
   }
 }
@@ -199,6 +212,24 @@ __global__ void __launch_bounds__(kRdRows) k_trmv_part(int m, const double* __re
   if (i < m) part[(size_t)kc * m + i] = s;
 }
 
+// the same over the double-float factor of the mixed path
+__global__ void __launch_bounds__(kRdRows) k_trmv_part_df(int m, const float2* __restrict__ A, int lda,
+                                                          const double* __restrict__ p, double s2dt,
+                                                          double* __restrict__ part) {
+  int i = blockIdx.x * kRdRows + threadIdx.x;
+  int kc = blockIdx.y;
+  int k0 = kc * kRdChunk, k1 = min(k0 + kRdChunk, m);
+  double s = 0.0;
+  if (i < m) {
+    int kend = min(k1, i + 1);
+    for (int k = k0; k < kend; k++) {
+      const float2 a = A[(size_t)k * lda + i];
+      s = s + (s2dt * ((double)a.x + (double)a.y)) * p[k];
+    }
+  }
+  if (i < m) part[(size_t)kc * m + i] = s;
+}
+
 __global__ void k_trmv_sum(int m, int nchunk, const double* __restrict__ part, double* __restrict__ rd) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
@@ -212,9 +243,12 @@ __global__ void k_trmv_sum(int m, int nchunk, const double* __restrict__ part, d
 namespace bdk {
 
 void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
-                  cudaStream_t st) {
+                  cudaStream_t st, bool df) {
   int nt = cdiv(nD, kRpyTile);
-  k_rpy<<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
+  if (df)
+    k_rpy<true><<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
+  else
+    k_rpy<false><<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
 }
 
 int potrf_fp64(int m, double* A, int lda, double* /*rd_acc*/, const double* /*p*/, double /*s2dt*/, int* d_negpiv,
@@ -237,9 +271,13 @@ int potrf_fp64(int m, double* A, int lda, double* /*rd_acc*/, const double* /*p*
 size_t trmv_scratch_doubles(int m) { return (size_t)cdiv(m, kRdChunk) * m; }
 
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
-                   cudaStream_t st) {
+                   cudaStream_t st, bool df) {
   int nchunk = cdiv(m, kRdChunk);
-  k_trmv_part<<<dim3(cdiv(m, kRdRows), nchunk), kRdRows, 0, st>>>(m, A, lda, p, s2dt, part);
+  if (df)
+    k_trmv_part_df<<<dim3(cdiv(m, kRdRows), nchunk), kRdRows, 0, st>>>(m, reinterpret_cast<const float2*>(A), lda, p,
+                                                                       s2dt, part);
+  else
+    k_trmv_part<<<dim3(cdiv(m, kRdRows), nchunk), kRdRows, 0, st>>>(m, A, lda, p, s2dt, part);
   k_trmv_sum<<<cdiv(m, 256), 256, 0, st>>>(m, nchunk, part, rd);
 }
 

@@ -1,8 +1,10 @@
 // Mixed-precision Cholesky of the RPY tensor on the sm_103a tensor cores.
 //
 // Right-looking blocked factorisation with 128-wide panels.  The matrix is
-// stored in FP64 (column-major), so each trailing update is rounded at FP64
-// however many panels precede it; the arithmetic is FP32-class:
+// stored as double-float pairs (hi, lo) of FP32 (column-major, 8 bytes per
+// element, ~48 significant bits), so the trailing updates accumulate without
+// an FP32 rounding per panel and without FP64 arithmetic (GB300's FP64 rate
+// is ~2 operations per clock per SM); the arithmetic is FP32-class:
 //   k_dpanel    one launch per panel: every CTA factors the 128 x 128
 //               diagonal block in shared memory (FP32, 32-column blocks,
 //               left-looking across blocks), CTA 0 writes it back and the
@@ -17,7 +19,7 @@
 //               products (hi.hi, hi.mid, mid.hi, hi.lo, mid.mid, lo.hi) into
 //               one of two FP32 tensor-memory accumulators (tcgen05.mma,
 //               M = N = 128, K = 16 per instruction), tcgen05.ld epilogue
-//               into the FP64 tile.  The dropped products are below 2^-24 of
+//               subtracting into the double-float tile.  The dropped products are below 2^-24 of
 //               the kept ones: FP32-class products.
 // A one-panel lookahead runs the next panel on a second stream while the
 // bulk update of the current one runs.  Every mbarrier wait is bounded; on
@@ -47,6 +49,20 @@ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 __device__ __forceinline__ uint32_t swz_off(int r, int k) {
   int half = k >> 6, kk = k & 63;
   return half * kHalfBytes + (r >> 3) * 1024 + (r & 7) * 128 + ((((kk >> 3) ^ (r & 7)) & 7) << 4) + (kk & 7) * 2;
+}
+
+// (hi, lo) - v in double-float arithmetic: exact two-sums (Knuth), so the
+// stored value keeps ~48 significant bits through every trailing update
+// (no per-update FP32 rounding of the element) without any FP64 operation.
+__device__ __forceinline__ float2 df_sub(float2 a, float v) {
+  const float s = a.x - v;
+  const float bb = s - a.x;
+  float e = (a.x - (s - bb)) + (-v - bb);
+  e += a.y;
+  const float h = s + e;
+  const float b2 = h - s;
+  const float l = (s - (h - b2)) + (e - b2);
+  return make_float2(h, l);
 }
 
 // ------------------------------------------------------------ diagonal block + panel
@@ -126,7 +142,7 @@ __device__ __forceinline__ void dp_row_solve(float* row, const float (*Lf)[kLd],
 
 // Runs in a CTA of kRestThreads threads; threads >= kDpThreads only take
 // part in the barriers.  `b` is the CTA's index among the panel CTAs.
-__device__ __forceinline__ void dpanel_body(float4* sm4, double* A, int lda, int m, int k0, int kb, int tile0,
+__device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, int lda, int m, int k0, int kb, int tile0,
                                             int b, unsigned char* PS, int* negpiv) {
   float (*Ls)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);
   float (*X)[kLd] = reinterpret_cast<float (*)[kLd]>(reinterpret_cast<float*>(sm4) + kT * kLd);
@@ -141,22 +157,22 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, double* A, int lda, int
     // column-major walk (a warp reads 32 consecutive rows of one column),
     // 16 columns per batch so that 32 loads per thread are in flight
     const int r = tid & (kT - 1), cq = tid >> 7;
-    const double* ga = A + (size_t)k0 * lda + k0 + r;
-    const double* gx = A + (size_t)k0 * lda + row0 + r;
+    const float2* ga = A + (size_t)k0 * lda + k0 + r;
+    const float2* gx = A + (size_t)k0 * lda + row0 + r;
 #pragma unroll 1
     for (int i0 = 0; i0 < kT / 2; i0 += 16) {
-      double va[16], vx[16];
+      float2 va[16], vx[16];
 #pragma unroll
       for (int i = 0; i < 16; i++) {
         const int c = cq + 2 * (i0 + i);
-        va[i] = (r >= c && r < kb && c < kb) ? ga[(size_t)c * lda] : 0.0;
-        vx[i] = (!is_diag && r < nrows && c < kb) ? gx[(size_t)c * lda] : 0.0;
+        va[i] = (r >= c && r < kb && c < kb) ? ga[(size_t)c * lda] : make_float2(0.f, 0.f);
+        vx[i] = (!is_diag && r < nrows && c < kb) ? gx[(size_t)c * lda] : make_float2(0.f, 0.f);
       }
 #pragma unroll
       for (int i = 0; i < 16; i++) {
         const int c = cq + 2 * (i0 + i);
-        Ls[r][c] = (float)va[i];
-        X[r][c] = (float)vx[i];
+        Ls[r][c] = va[i].x + va[i].y;  // nearest FP32 of the stored double-float
+        X[r][c] = vx[i].x + vx[i].y;
       }
     }
   }
@@ -205,7 +221,7 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, double* A, int lda, int
     if (work)
       for (int e = tid; e < kb * kb; e += kDpThreads) {
         const int c = e / kb, r = e - c * kb;
-        if (r >= c) A[(size_t)(k0 + c) * lda + k0 + r] = (double)Ls[r][c];
+        if (r >= c) A[(size_t)(k0 + c) * lda + k0 + r] = make_float2(Ls[r][c], 0.f);
       }
     return;
   }
@@ -222,7 +238,7 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, double* A, int lda, int
   // thread takes one row and 8 consecutive columns, i.e. one 16-byte chunk
   // of each slice (consecutive lanes: consecutive rows, coalesced FP64 stores)
   unsigned char* ps = PS + (size_t)tile * kTileBytes;
-  double* gout = A + (size_t)k0 * lda + row0;
+  float2* gout = A + (size_t)k0 * lda + row0;
 #pragma unroll 1
   for (int e = tid; work && e < kT * (kT / 8); e += kDpThreads) {
     const int r = e & (kT - 1), c0 = (e >> 7) * 8;
@@ -234,7 +250,7 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, double* A, int lda, int
     for (int j = 0; j < 8; j++) {
       const bool in = r < nrows && c0 + j < kb;
       const float x = in ? xs[j] : 0.f;
-      if (in) gout[(size_t)(c0 + j) * lda + r] = (double)x;
+      if (in) gout[(size_t)(c0 + j) * lda + r] = make_float2(x, 0.f);
       // x = hi + mid + lo exactly (8 + 8 + 8 significant bits)
       const __nv_bfloat16 h = __float2bfloat16_rn(x);
       const float r1 = x - __bfloat162float(h);
@@ -300,7 +316,7 @@ __device__ __forceinline__ void rest_tile(int t, int jlo, int col_only, int& I, 
 }
 
 // `cta` is the CTA's index among the update CTAs.
-__device__ __forceinline__ void rest_body(unsigned char* smraw, double* A, int lda, int m, int jlo, int col_only,
+__device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int lda, int m, int jlo, int col_only,
                                           int ntiles, int group, int cta, const unsigned char* __restrict__ PS,
                                           int* err) {
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -464,13 +480,14 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, double* A, int l
       const int cbase = J * kT + 64 * ch;
       const int jlim0 = diag ? max(0, gi - cbase + 1) : 64;  // diagonal tile: columns <= gi
       const int jcnt = row_ok ? min(min(jlim0, 64), m - cbase) : 0;
-      double* colp = A + (size_t)cbase * lda + gi;
+      float2* colp = A + (size_t)cbase * lda + gi;
 #pragma unroll
       for (int c = 0; c < 2; c++) {
-        double old[32];
+        float2 old[32];
         float v[32];
 #pragma unroll
-        for (int j = 0; j < 32; j++) old[j] = (32 * c + j < jcnt) ? colp[(size_t)(32 * c + j) * lda] : 0.0;
+        for (int j = 0; j < 32; j++)
+          old[j] = (32 * c + j < jcnt) ? colp[(size_t)(32 * c + j) * lda] : make_float2(0.f, 0.f);
         sm100::tmem_ld32(ta + 32 * c, v);
         if (c == 1) {  // accumulator read out: hand it back to the MMA issuer
           sm100::tc_fence_before();
@@ -479,7 +496,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, double* A, int l
         }
 #pragma unroll
         for (int j = 0; j < 32; j++)
-          if (32 * c + j < jcnt) colp[(size_t)(32 * c + j) * lda] = old[j] - (double)v[j];
+          if (32 * c + j < jcnt) colp[(size_t)(32 * c + j) * lda] = df_sub(old[j], v[j]);
       }
     }
   }
@@ -492,7 +509,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, double* A, int l
 // and the tiles below it, writing its slices to PSp); the remaining CTAs
 // apply an earlier panel's trailing update (tiles from jlo, slices PSu).
 // The two parts touch disjoint columns and slice buffers.
-__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(double* A, int lda, int m, int ndp, int pk0, int pkb,
+__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(float2* A, int lda, int m, int ndp, int pk0, int pkb,
                                                               unsigned char* PSp, int* negpiv, int jlo, int col_only,
                                                               int ntiles, int group,
                                                               const unsigned char* __restrict__ PSu, int* err) {
@@ -548,8 +565,9 @@ static int rest_group(int tiles) {
 // carries the bulk of panel k's update; the two parts write disjoint
 // columns, and panel k+1's slices go to the other buffer.  No two kernels
 // run at the same time.  Returns the number of kernel launches.
-int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
+int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
                 cudaEvent_t* kev, int* kev_pairs, double* kflop) {
+  float2* A = reinterpret_cast<float2*>(A64);  // double-float storage, 8 bytes per element
   const int nt = cdiv(m, kT);
   const size_t buf = (size_t)nt * kTileBytes;
   int L = 0, pairs = 0;

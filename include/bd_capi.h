@@ -213,6 +213,9 @@ int bd_phase_times(bd_ctx* ctx, float* out9);
  * timing enabled (see bd_phase_times), their number, and the BF16 tensor
  * work they issued (flop). */
 int bd_kernel_time(bd_ctx* ctx, float* total_ms, int* launches, double* tensor_flop);
+/* The same launches one by one: out_ms[i] for i < min(max, launches), in
+ * panel order; *launches = their number. */
+int bd_kernel_times(bd_ctx* ctx, float* out_ms, int max, int* launches);
 /* Count of kernel launches issued by the last bd_step (graph nodes count once each). */
 int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */

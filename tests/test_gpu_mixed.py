@@ -1,5 +1,6 @@
-"""Mixed-precision path (BD_PREC_MIXED): FP32 storage, FP32 diagonal blocks
-and tensor-core (tcgen05, BF16 three-way split) trailing updates.
+"""Mixed-precision path (BD_PREC_MIXED): double-float (FP32 pair) tensor
+storage, FP32 diagonal blocks and tensor-core (tcgen05, BF16 three-way
+split) trailing updates.
 
 Accuracy is stated against the FP64 oracle: the factor to 1e-5 relative
 (FP32 class, |L_mixed - L| / |L|), the noise displacement rd and the step's
@@ -17,6 +18,15 @@ pytestmark = pytest.mark.gpu
 def case(request):
     fib, z = load_golden(request.param)
     return request.param, fib, z
+
+
+def test_mixed_tensor_storage(case):
+    """The double-float tensor holds the FP64 RPY tensor to ~2^-48."""
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
+    name, fib, z = case
+    D64 = Context(fib, precision=PREC_FP64).diffusion_tensor()
+    Dm = Context(fib, precision=PREC_MIXED).diffusion_tensor()
+    assert np.abs(Dm - D64).max() <= 1e-13 * np.abs(D64).max()
 
 
 def test_mixed_factor_matches_fp64(case):
