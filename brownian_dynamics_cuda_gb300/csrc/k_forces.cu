@@ -354,6 +354,104 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
     for (int q = 0; q < 10; q++) out[q] = v[q];
 }
 
+// Core/core, mixed path: the same slot (force on I, body-frame torques on I
+// and J, energy) with no FP64 arithmetic per charge pair.  Sites are set up
+// once per CTA in FP64 and stored in FP32 relative to the midpoint of the
+// two cores (|s| <= ~20 nm, so the FP32 separation carries ~1e-6 relative
+// error at 1 nm); the torques are summed in the world frame as
+// lever x f (lever = R cp) and turned into the body frame once at the end
+// (R^T (lever x f) = cp x (R^T f), the reference's form); sums are FP32 over
+// 32 pairs, then FP64.
+constexpr int kCCFlush = 32;
+
+__global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevState X, double* slots) {
+  extern __shared__ double sm[];
+  const int I = blockIdx.x, J = blockIdx.y;
+  double* out = slots + ((size_t)I * M.n_c + J) * 10;
+  if (I >= J) return;
+  const int i = M.core_bead[I], j = M.core_bead[J];
+  const V3 ri = ld3(X.r + 3 * i), rj = ld3(X.r + 3 * j);
+  const double d0 = sqrt((rj.x - ri.x) * (rj.x - ri.x) + (rj.y - ri.y) * (rj.y - ri.y) + (rj.z - ri.z) * (rj.z - ri.z));
+  if (d0 > 25.0 || !chain_ok(M, i) || !chain_ok(M, j)) {
+    if (threadIdx.x < 10) out[threadIdx.x] = 0.0;
+    return;
+  }
+  const int Nq = M.Nq;
+  // SoA: site (x, y, z), lever (x, y, z), charge; I then J
+  float* f = reinterpret_cast<float*>(sm);
+  float *sIx = f, *sIy = f + Nq, *sIz = f + 2 * Nq, *lIx = f + 3 * Nq, *lIy = f + 4 * Nq, *lIz = f + 5 * Nq,
+        *qI = f + 6 * Nq;
+  float *sJx = f + 7 * Nq, *sJy = f + 8 * Nq, *sJz = f + 9 * Nq, *lJx = f + 10 * Nq, *lJy = f + 11 * Nq,
+        *lJz = f + 12 * Nq, *qJ = f + 13 * Nq;
+  double* red = sm + (14 * Nq + 1) / 2;
+  const V3 ai = ld3(X.a + 3 * i), bi = ld3(X.b + 3 * i), ci = ld3(X.c + 3 * i);
+  const V3 aj = ld3(X.a + 3 * j), bj = ld3(X.b + 3 * j), cj = ld3(X.c + 3 * j);
+  const V3 mid{0.5 * (ri.x + rj.x), 0.5 * (ri.y + rj.y), 0.5 * (ri.z + rj.z)};
+  for (int k = threadIdx.x; k < Nq; k += blockDim.x) {
+    const double* p = M.core_pos + 3 * k;
+    const V3 li{ai.x * p[0] + bi.x * p[1] + ci.x * p[2], ai.y * p[0] + bi.y * p[1] + ci.y * p[2],
+                ai.z * p[0] + bi.z * p[1] + ci.z * p[2]};
+    const V3 lj{aj.x * p[0] + bj.x * p[1] + cj.x * p[2], aj.y * p[0] + bj.y * p[1] + cj.y * p[2],
+                aj.z * p[0] + bj.z * p[1] + cj.z * p[2]};
+    sIx[k] = (float)((ri.x - mid.x) + li.x); sIy[k] = (float)((ri.y - mid.y) + li.y); sIz[k] = (float)((ri.z - mid.z) + li.z);
+    sJx[k] = (float)((rj.x - mid.x) + lj.x); sJy[k] = (float)((rj.y - mid.y) + lj.y); sJz[k] = (float)((rj.z - mid.z) + lj.z);
+    lIx[k] = (float)li.x; lIy[k] = (float)li.y; lIz[k] = (float)li.z;
+    lJx[k] = (float)lj.x; lJy[k] = (float)lj.y; lJz[k] = (float)lj.z;
+    qI[k] = (float)(M.k_e * M.core_q[k]);
+    qJ[k] = (float)M.core_q[k];
+  }
+  __syncthreads();
+  const float kap = (float)M.debye, kex = (float)M.k_ex, sg = (float)M.sCC;
+  float a[10];
+  double v[10];
+#pragma unroll
+  for (int q = 0; q < 10; q++) a[q] = 0.f, v[q] = 0.0;
+  int cnt = 0;
+  for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
+    const int k = p / Nq, l = p - k * Nq;
+    const float zx = sIx[k] - sJx[l], zy = sIy[k] - sJy[l], zz = sIz[k] - sJz[l];
+    const float ssq = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+    const float rinv = rsqrtf(ssq);
+    const float dd = ssq * rinv;
+    const float ex = expf(-kap * dd);
+    float e = qI[k] * qJ[l] * ex * rinv;          // k_e q_k q_l e^{-kappa d} / d
+    float g = e * fmaf(kap, dd, 1.f) * rinv;      // ... (kappa d + 1) / d^2
+    if (dd <= 8.f) {
+      const float sr = sg * rinv, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+      g = fmaf(kex * (12.f * sr12 - 6.f * sr6), rinv, g);
+      e = fmaf(kex, sr12 - sr6, e);
+    }
+    const float gz = g * rinv;
+    const float fx = gz * zx, fy = gz * zy, fz = gz * zz;
+    a[0] += fx; a[1] += fy; a[2] += fz;
+    a[3] = fmaf(lIy[k], fz, fmaf(-lIz[k], fy, a[3]));
+    a[4] = fmaf(lIz[k], fx, fmaf(-lIx[k], fz, a[4]));
+    a[5] = fmaf(lIx[k], fy, fmaf(-lIy[k], fx, a[5]));
+    a[6] = fmaf(-lJy[l], fz, fmaf(lJz[l], fy, a[6]));
+    a[7] = fmaf(-lJz[l], fx, fmaf(lJx[l], fz, a[7]));
+    a[8] = fmaf(-lJx[l], fy, fmaf(lJy[l], fx, a[8]));
+    a[9] += e;
+    if (++cnt == kCCFlush) {
+#pragma unroll
+      for (int q = 0; q < 10; q++) v[q] += (double)a[q], a[q] = 0.f;
+      cnt = 0;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 10; q++) v[q] += (double)a[q];
+  bsum<10>(v, red);
+  if (threadIdx.x == 0) {
+    out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
+    out[3] = ai.x * v[3] + ai.y * v[4] + ai.z * v[5];
+    out[4] = bi.x * v[3] + bi.y * v[4] + bi.z * v[5];
+    out[5] = ci.x * v[3] + ci.y * v[4] + ci.z * v[5];
+    out[6] = aj.x * v[6] + aj.y * v[7] + aj.z * v[8];
+    out[7] = bj.x * v[6] + bj.y * v[7] + bj.z * v[8];
+    out[8] = cj.x * v[6] + cj.y * v[7] + cj.z * v[8];
+    out[9] = v[9];
+  }
+}
+
 // DNA/core (func.cpp:1355-1488): one warp per (linker bead d, core J).
 // Slot: force on the DNA bead (3), torque on the core (3), energy.
 template <bool MX>
@@ -889,8 +987,13 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   k_chain_bonded<<<cdiv(M.n, 128), 128, 0, st>>>(M, X, Fm, Tm, Ebond);
   L++;
   if (M.n_c > 1) {
-    size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
-    k_core_coreX<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+    if (mixed) {
+      size_t sm = (size_t)((14 * M.Nq + 1) / 2 + 32 * 10) * sizeof(double);
+      k_core_core_mx<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+    } else {
+      size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
+      k_core_coreX<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+    }
     L++;
   }
   if (M.n_dna > 0 && M.n_c > 0) { k_dna_coreX<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc); L++; }
