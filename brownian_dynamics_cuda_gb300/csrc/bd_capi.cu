@@ -293,6 +293,8 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   for (int q = 0; q < 3; q++) { addD(3 * n); addD(3 * n); addD(3 * nt); addD(3 * nL); addD(1); }
   addD((size_t)nc * nc * 10); addD(ndna * nc * 7); addD(nlhc * nc * 10); addD(ebuf);
   addD(3 * (size_t)M.n_D); addD(c->m); addD(c->m); addD(3 * n); addD(bdk::trmv_scratch_doubles(c->m)); addD(1); addI(1);
+  const int npos = n + nt + nL + nlhc * M.n_lh_g;
+  addD((nt + 1) / 2); addD(2 * (size_t)npos); addD(2 * (size_t)npos);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
   if (c->precision != BD_PREC_MIXED && c->precision != BD_PREC_FP64)
@@ -345,6 +347,10 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   c->rr = ar.take<double>(3 * n);
   c->rd_part = ar.take<double>(bdk::trmv_scratch_doubles(c->m));
   c->energy = ar.take<double>(1);
+  float* d_tqf = ar.take<float>(nt);
+  c->S.ph = ar.take<float4>(npos);
+  c->S.pl = ar.take<float4>(npos);
+  c->S.ot = n; c->S.ol = n + nt; c->S.og = n + nt + nL; c->S.npos = npos;
   c->negpiv = ar.take<int>(1);
   cudaStream_t st = c->stream;
   std::vector<int> tgrp_pad(nt + 2, -1);
@@ -372,6 +378,18 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   M.t_core_bead = d_tcb; M.LH_g_pos = d_gpos0; M.LH_conn = d_conn; M.nc_lh_flag = d_nclh;
   M.LH_q = d_lhp[0]; M.LH_vdw_hh = d_lhp[1]; M.LH_vdw_hc = d_lhp[2]; M.LH_vdw_hl = d_lhp[3]; M.LH_vdw_ht = d_lhp[4];
   M.LH_kstr = d_lhp[5]; M.LH_kben = d_lhp[6]; M.LH_streq = d_lhp[7]; M.LH_betaeq = d_lhp[8];
+  {
+    std::vector<float> tqf(nt);
+    for (int t = 0; t < nt; t++) tqf[t] = (float)m->t_q[t];
+    if (nt && cudaMemcpyAsync(d_tqf, tqf.data(), nt * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
+    if (nt && cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
+    M.t_qf = d_tqf;
+    M.tails_by_core = M.n_t > 0;
+    for (int t = 0; t < nt && M.tails_by_core; t++)
+      if (t_core_bead[t] != -1 && (t / M.n_t >= nc || t_core_bead[t] != core_bead[t / M.n_t])) M.tails_by_core = 0;
+  }
+  if ((nL > 0 || nlhc > 0) && np > 64) return fail(set_error(BD_ERR_ARG, "bd_create: more than 64 LH bead types"));
   // state
   if ((rc = up(c->X.r, s->r, 3 * n, st)) || (rc = up(c->X.a, s->a, 3 * n, st)) || (rc = up(c->X.b, s->b, 3 * n, st)) ||
       (rc = up(c->X.c, s->c, 3 * n, st)) || (rc = up(c->X.r_t, s->r_t, 3 * nt, st)) ||

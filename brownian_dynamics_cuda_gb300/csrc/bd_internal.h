@@ -75,6 +75,8 @@ struct DevModel {
   const double *LH_q, *LH_vdw_hh, *LH_vdw_hc, *LH_vdw_hl, *LH_vdw_ht, *LH_kstr, *LH_kben, *LH_streq, *LH_betaeq;
   double qmax_core;        // max |core_pos| (nm), for exact far-pair skipping
   double gmax;             // max |LH_g_pos|
+  const float* t_qf;       // [n_tail] tail charges in FP32 (mixed path)
+  int tails_by_core;       // tail t belongs to core t / n_t (or to none): anchored-tail scans per core
 };
 
 // Configuration-dependent arrays of one state (current or predicted).
@@ -101,6 +103,10 @@ struct DevScratch {
   double* gc;    // [n_lhcore * n_c * 10] G-head(core I) - charges(core L): F_I(3) T_I(3) T_L(3) E
   double* ebuf;  // [nE] per-kernel energy partials
   int nE;
+  // mixed path: every position of the force pass as a double-float pair
+  // (hi, lo) of FP32 xyz, chain | tails | LH | G-heads
+  float4 *ph, *pl;
+  int ot, ol, og, npos;
 };
 
 namespace bdk {

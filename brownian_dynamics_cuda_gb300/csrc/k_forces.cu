@@ -586,6 +586,66 @@ __global__ void k_ghead_core(DevModel M, DevState X, double* slots) {
 // One CTA per chain bead: every remaining contribution to its force and
 // torque, plus the slot reductions; writes the bead's final F, T and its
 // energy share.
+// Block sum of a chain bead's pair terms, then the slot reductions in a
+// fixed order and the bonded terms; thread 0 stores.
+__device__ void chain_finish(const DevModel& M, const DevScratch& S, const double* Fm, const double* Tm,
+                             const double* Ech, DevForces& out, double* Eout, int j, V3 F, V3 T, double E,
+                             double* red) {
+  const bool dna = M.type[j] == 0;
+  double v[7] = {F.x, F.y, F.z, T.x, T.y, T.z, E};
+  bsum<7>(v, red);
+  if (threadIdx.x != 0) return;
+  F = V3{v[0], v[1], v[2]};
+  T = V3{v[3], v[4], v[5]};
+  E = v[6];
+  // slot reductions, fixed order
+  if (dna) {
+    const int D = j - M.core_rank[j] - 1;  // linker beads before j
+    for (int J = 0; J < M.n_c; J++) {
+      const double* s = S.dc + ((size_t)D * M.n_c + J) * 7;
+      F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
+    }
+  } else {
+    const int J = M.core_rank[j];
+    for (int K = 0; K < M.n_c; K++) {
+      if (K < J) {
+        const double* s = S.cc + ((size_t)K * M.n_c + J) * 10;
+        F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
+        T.x = T.x + s[6]; T.y = T.y + s[7]; T.z = T.z + s[8];
+      } else if (K > J) {
+        const double* s = S.cc + ((size_t)J * M.n_c + K) * 10;
+        F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
+        T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
+        E = E + s[9];
+      }
+    }
+    for (int D = 0; D < M.n_dna; D++) {
+      const double* s = S.dc + ((size_t)D * M.n_c + J) * 7;
+      F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
+      T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
+      E = E + s[6];
+    }
+    const int lc = M.core_lh[J];
+    for (int I = 0; I < M.n_lhcore; I++) {
+      const double* s = S.gc + ((size_t)I * M.n_c + J) * 10;
+      F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
+      T.x = T.x + s[6]; T.y = T.y + s[7]; T.z = T.z + s[8];
+    }
+    if (lc >= 0) {
+      for (int L = 0; L < M.n_c; L++) {
+        const double* s = S.gc + ((size_t)lc * M.n_c + L) * 10;
+        F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
+        T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
+        E = E + s[9];
+      }
+    }
+  }
+  V3 Fb = ld3(Fm + 3 * j), Tb = ld3(Tm + 3 * j);
+  st3(out.F + 3 * j, V3{Fb.x + F.x, Fb.y + F.y, Fb.z + F.z});
+  st3(out.T + 3 * j, V3{Tb.x + T.x, Tb.y + T.y, Tb.z + T.z});
+  Eout[j] = Ech[j] + E;
+}
+
 constexpr int kGatherThreads = 256;
 
 template <bool MX>
@@ -747,58 +807,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, Dev
       }
     }
   }
-  double v[7] = {F.x, F.y, F.z, T.x, T.y, T.z, E};
-  bsum<7>(v, red);
-  if (tid != 0) return;
-  F = V3{v[0], v[1], v[2]};
-  T = V3{v[3], v[4], v[5]};
-  E = v[6];
-  // slot reductions, fixed order
-  if (dna) {
-    const int D = j - M.core_rank[j] - 1;  // linker beads before j
-    for (int J = 0; J < M.n_c; J++) {
-      const double* s = S.dc + ((size_t)D * M.n_c + J) * 7;
-      F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
-    }
-  } else {
-    const int J = M.core_rank[j];
-    for (int K = 0; K < M.n_c; K++) {
-      if (K < J) {
-        const double* s = S.cc + ((size_t)K * M.n_c + J) * 10;
-        F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
-        T.x = T.x + s[6]; T.y = T.y + s[7]; T.z = T.z + s[8];
-      } else if (K > J) {
-        const double* s = S.cc + ((size_t)J * M.n_c + K) * 10;
-        F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
-        T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
-        E = E + s[9];
-      }
-    }
-    for (int D = 0; D < M.n_dna; D++) {
-      const double* s = S.dc + ((size_t)D * M.n_c + J) * 7;
-      F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
-      T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
-      E = E + s[6];
-    }
-    const int lc = M.core_lh[J];
-    for (int I = 0; I < M.n_lhcore; I++) {
-      const double* s = S.gc + ((size_t)I * M.n_c + J) * 10;
-      F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
-      T.x = T.x + s[6]; T.y = T.y + s[7]; T.z = T.z + s[8];
-    }
-    if (lc >= 0) {
-      for (int L = 0; L < M.n_c; L++) {
-        const double* s = S.gc + ((size_t)lc * M.n_c + L) * 10;
-        F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
-        T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
-        E = E + s[9];
-      }
-    }
-  }
-  V3 Fb = ld3(Fm + 3 * j), Tb = ld3(Tm + 3 * j);
-  st3(out.F + 3 * j, V3{Fb.x + F.x, Fb.y + F.y, Fb.z + F.z});
-  st3(out.T + 3 * j, V3{Tb.x + T.x, Tb.y + T.y, Tb.z + T.z});
-  Eout[j] = Ech[j] + E;
+  chain_finish(M, S, Fm, Tm, Ech, out, Eout, j, F, T, E, red);
 }
 
 // ------------------------------------------------------------ tails
@@ -953,6 +962,429 @@ __global__ void k_lh_gather(DevModel M, DevState X, DevForces out, double* Eout)
   }
 }
 
+// ------------------------------------------------------------ mixed path: FP32 pair loops
+// The gather kernels of the mixed path evaluate every pair in FP32 from a
+// per-pass mirror of the positions as double-float pairs (hi, lo): the
+// separation (hi_a - hi_b) + (lo_a - lo_b) keeps the FP64 positions'
+// accuracy without FP64 arithmetic.  Pair sums run in FP32 for 32 pairs,
+// then in FP64; torques from pair forces are summed in the world frame
+// (lever x f) and turned into the body frame once.  The pair formulas and
+// cut-offs are those of pair_f1_mx (func.cpp:278-345).
+
+__global__ void k_mirror(DevModel M, DevState X, float4* ph, float4* pl, int npos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npos) return;
+  const int n = M.n, nt = M.n_tail, nL = M.n_LH;
+  const double* p = i < n ? X.r + 3 * i
+                  : i < n + nt ? X.r_t + 3 * (i - n)
+                  : i < n + nt + nL ? X.r_lh + 3 * (i - n - nt)
+                  : X.gpos + 3 * (i - n - nt - nL);
+  const double x = p[0], y = p[1], z = p[2];
+  const float hx = (float)x, hy = (float)y, hz = (float)z;
+  ph[i] = make_float4(hx, hy, hz, 0.f);
+  pl[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.f);
+}
+
+struct PF {
+  float4 h, l;
+};
+__device__ __forceinline__ PF ldpf(const DevScratch& S, int i) { return PF{S.ph[i], S.pl[i]}; }
+// a - b
+__device__ __forceinline__ float3 sepf(const PF& a, const PF& b) {
+  return make_float3((a.h.x - b.h.x) + (a.l.x - b.l.x), (a.h.y - b.h.y) + (a.l.y - b.l.y),
+                     (a.h.z - b.h.z) + (a.l.z - b.l.z));
+}
+__device__ __forceinline__ float3 crossf(const float3& u, const float3& v) {
+  return make_float3(fmaf(u.y, v.z, -u.z * v.y), fmaf(u.z, v.x, -u.x * v.z), fmaf(u.x, v.y, -u.y * v.x));
+}
+
+// force on particle 1 from particle 2, d = c1 - c2; qq = k_e q1 q2
+template <bool DH, bool LJ>
+__device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float sig, float3 d, float& E) {
+  const float d2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+  const float dd = sqrtf(d2);
+  float t = 0.f;
+  if (DH && dd < 7.f) {
+    const float ex = expf(-kap * dd);
+    t = qq * fmaf(kap, dd, 1.f) * ex / d2;
+    E += qq * ex / dd;
+  }
+  if (LJ && dd < 4.f) {
+    const float sr = sig / dd, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+    t = t - kev * (6.f * sr6 - 12.f * sr12) / dd;
+    E += kev * (sr12 - sr6);
+  }
+  const float w = t / dd;
+  return make_float3(clamp09f(w * d.x), clamp09f(w * d.y), clamp09f(w * d.z));
+}
+
+// FP32 partial sums of force, world torque and energy, flushed to FP64
+struct FAcc {
+  float f[7];
+  double s[7];
+  int n;
+  __device__ void init() {
+#pragma unroll
+    for (int q = 0; q < 7; q++) f[q] = 0.f, s[q] = 0.0;
+    n = 0;
+  }
+  __device__ void flush() {
+#pragma unroll
+    for (int q = 0; q < 7; q++) s[q] += (double)f[q], f[q] = 0.f;
+    n = 0;
+  }
+  __device__ void tick() {
+    if (++n == 32) flush();
+  }
+  __device__ void force(const float3& v) { f[0] += v.x; f[1] += v.y; f[2] += v.z; }
+  __device__ void torque(const float3& v) { f[3] += v.x; f[4] += v.y; f[5] += v.z; }
+};
+
+// LH bead-type parameters in FP32, per CTA: q, vdw_hh, vdw_hl, vdw_ht
+struct LHf {
+  float q[64], hh[64], hl[64], ht[64];
+};
+__device__ void load_lhf(const DevModel& M, LHf& P) {
+  const int np = M.n_lh_n + M.n_lh_g + M.n_lh_c;
+  for (int i = threadIdx.x; i < np && i < 64; i += blockDim.x) {
+    P.q[i] = (float)M.LH_q[i];
+    P.hh[i] = (float)M.LH_vdw_hh[i];
+    P.hl[i] = (float)M.LH_vdw_hl[i];
+    P.ht[i] = (float)M.LH_vdw_ht[i];
+  }
+  __syncthreads();
+}
+
+// Tail beads, one warp each (func.cpp:1809-1917, 2343-2476 for the LH side).
+__global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
+  __shared__ LHf P;
+  load_lhf(M, P);
+  const int lane = threadIdx.x & 31;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (t >= M.n_tail) return;
+  V3 rt = ld3(X.r_t + 3 * t);
+  V3 F{0.0, 0.0, 0.0};
+  double E = 0.0;
+  const int* grp = M.t_grp;
+  const int nt = M.n_tail;
+  if (lane == 0) {  // bonded terms and the anchor, as the FP64 path
+    if (t >= 1 && grp[t - 1] == grp[t]) acc(F, stretch_f2(M.h_t[t - 1], ld3(X.r_t + 3 * t - 3), rt, M.lo_t[t - 1]));
+    if (t + 1 < nt && grp[t] == grp[t + 1]) acc(F, stretch_f1(M.h_t[t], rt, ld3(X.r_t + 3 * t + 3), M.lo_t[t], E));
+    for (int s = t - 2; s <= t; s++) {
+      if (s < 0 || s + 2 >= nt) continue;
+      if (!(grp[s] == grp[s + 1] && grp[s] == grp[s + 2])) continue;
+      V3 f1, f2, f3;
+      double e = 0.0;
+      bend3(M.g_t[s], X.beta_t[s], M.beta_o_t[s], ld3(X.r_t + 3 * s), ld3(X.r_t + 3 * s + 3), ld3(X.r_t + 3 * s + 6), f1,
+            f2, f3, e);
+      if (s == t) E = E + e;
+      dec(F, s == t ? f1 : (s == t - 1 ? f2 : f3));
+    }
+    int J = t / M.n_t, jt = t - J * M.n_t;
+    if (M.nc_t_flag[J] == 1 && M.tail_fix[jt] == 1) {
+      int cb = M.core_bead[J];
+      V3 ro = site(X, cb, M.tail_pos + 3 * jt);
+      V3 st{rt.x - ro.x, rt.y - ro.y, rt.z - ro.z};
+      F.x = F.x - M.h * st.x; F.y = F.y - M.h * st.y; F.z = F.z - M.h * st.z;
+    }
+  }
+  const float ke = (float)M.k_e, kap = (float)M.debye, kex = (float)M.k_ex;
+  const float qt = ke * M.t_qf[t];
+  const PF pt = ldpf(S, S.ot + t);
+  FAcc A;
+  A.init();
+  float dummy = 0.f;
+  for (int u = lane; u < nt; u += 32) {  // tail/tail (func.cpp:1863-1891); energy on the lower index
+    if (u == t) continue;
+    int lo = t < u ? t : u, hi = t < u ? u : t;
+    if (!(grp[lo] != grp[hi] || hi > lo + 2)) continue;
+    float e = 0.f;
+    A.force(pairf<true, false>(qt * M.t_qf[u], kap, 0.f, 0.f, sepf(pt, ldpf(S, S.ot + u)), e));
+    if (t < u) A.f[6] += e;
+    A.tick();
+  }
+  const float ql = (float)M.q_l, sTL = (float)M.sTL;
+  for (int q = lane; q < M.n_dna; q += 32) {  // linker DNA (func.cpp:1898-1917); energy here
+    A.force(pairf<true, true>(qt * ql, kap, kex, sTL, sepf(pt, ldpf(S, M.dna_bead[q])), A.f[6]));
+    A.tick();
+  }
+  if (M.t_fix[t] == 0) {  // LH beads and globular heads on free tail beads (energies on their side)
+    for (int b = lane; b < M.n_LH; b += 32) {
+      int p = lh_param(M, b);
+      A.force(pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], sepf(pt, ldpf(S, S.ol + b)), dummy));
+      A.tick();
+    }
+    for (int s = lane; s < M.n_lhcore * M.n_lh_g; s += 32) {
+      int m = s % M.n_lh_g;
+      A.force(pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + s)), dummy));
+      A.tick();
+    }
+  }
+  A.flush();
+  F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
+  F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
+  if (lane == 0) {
+    st3(out.tF + 3 * t, F);
+    Eout[t] = E;
+  }
+}
+
+// Mobile LH beads, one warp each (func.cpp:2109-2398, 2588-2644, 2725-2777).
+__global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
+  __shared__ LHf P;
+  load_lhf(M, P);
+  const int lane = threadIdx.x & 31;
+  const int bI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (bI >= M.n_LH) return;
+  const int nL = M.n_LH, nlh = M.nlh;
+  V3 rb = ld3(X.r_lh + 3 * bI);
+  const int pb = lh_param(M, bI);
+  V3 F{0.0, 0.0, 0.0};
+  double E = 0.0;
+  if (lane == 0) {  // bonded terms and the globular-head anchor, as the FP64 path
+    if (bI >= 1) {
+      int p = lh_param(M, bI - 1);
+      if (M.LH_conn[p] == 1) acc(F, stretch_f2(M.LH_kstr[p], ld3(X.r_lh + 3 * bI - 3), rb, M.LH_streq[p]));
+    }
+    if (M.LH_conn[pb] == 1 && bI + 1 < nL) acc(F, stretch_f1(M.LH_kstr[pb], rb, ld3(X.r_lh + 3 * bI + 3), M.LH_streq[pb], E));
+    for (int s = bI - 1; s <= bI + 1; s++) {
+      if (s < 0 || s >= nL) continue;
+      if (!((s % M.n_lh_c != 0) && (s % M.n_lh_c != M.n_lh_c - 1))) continue;
+      int ps = lh_param(M, s);
+      V3 f1, f2, f3;
+      double e = 0.0;
+      bend3(M.LH_kben[ps], X.beta_lh[s], M.LH_betaeq[ps], ld3(X.r_lh + 3 * s - 3), ld3(X.r_lh + 3 * s),
+            ld3(X.r_lh + 3 * s + 3), f1, f2, f3, e);
+      if (s == bI) E = E + e;
+      dec(F, s == bI - 1 ? f3 : (s == bI ? f2 : f1));
+    }
+    if (bI % nlh == 0) {
+      int lc = bI / nlh;
+      for (int jj = 0; jj < M.n_lh_g; jj++) {
+        int pj = jj + M.n_lh_n;
+        if (M.LH_conn[pj] != 1) continue;
+        V3 g = ld3(X.gpos + 3 * (lc * M.n_lh_g + jj));
+        double d = sqrt((rb.x - g.x) * (rb.x - g.x) + (rb.y - g.y) * (rb.y - g.y) + (rb.z - g.z) * (rb.z - g.z));
+        double kst = M.LH_kstr[pj], eq = M.LH_streq[pj];
+        V3 st{(d - eq) * (rb.x - g.x) / d, (d - eq) * (rb.y - g.y) / d, (d - eq) * (rb.z - g.z) / d};
+        F.x = F.x - kst * st.x * 10; F.y = F.y - kst * st.y * 10; F.z = F.z - kst * st.z * 10;
+      }
+    }
+  }
+  const float ke = (float)M.k_e, kap = (float)M.debye, kex = (float)M.k_ex;
+  const float qb = ke * P.q[pb];
+  const PF pp = ldpf(S, S.ol + bI);
+  FAcc A;
+  A.init();
+  float dummy = 0.f;
+  for (int u = lane; u < nL; u += 32) {  // LH/LH (func.cpp:2190-2244); energy on the lower index
+    if (u == bI) continue;
+    const int pu = lh_param(M, u);
+    const float sig = (P.hh[pb] + P.hh[pu]) * 0.5f;
+    float e = 0.f;
+    const float3 d = sepf(pp, ldpf(S, S.ol + u));
+    if (bI / nlh == u / nlh) {
+      int lo = bI < u ? bI : u, hi = bI < u ? u : bI;
+      if (!(hi > lo + 1)) continue;
+      A.force(pairf<false, true>(0.f, kap, kex, sig, d, e));
+    } else {
+      A.force(pairf<true, true>(qb * P.q[pu], kap, kex, sig, d, e));
+    }
+    if (bI < u) A.f[6] += e;
+    A.tick();
+  }
+  const float ql = (float)M.q_l;
+  for (int q = lane; q < M.n_dna; q += 32) {  // linker DNA; energy here
+    A.force(pairf<true, true>(qb * ql, kap, kex, P.hl[pb], sepf(pp, ldpf(S, M.dna_bead[q])), A.f[6]));
+    A.tick();
+  }
+  for (int t = lane; t < M.n_tail; t += 32) {  // tails; energy here
+    A.force(pairf<true, true>(qb * M.t_qf[t], kap, kex, P.ht[pb], sepf(pp, ldpf(S, S.ot + t)), A.f[6]));
+    A.tick();
+  }
+  const int own = bI / nlh;
+  for (int s = lane; s < M.n_lhcore * M.n_lh_g; s += 32) {  // other LHs' globular heads; energy on the core
+    int K = s / M.n_lh_g, m = s - K * M.n_lh_g;
+    if (K == own) continue;
+    A.force(pairf<true, true>(qb * P.q[m], kap, kex, (P.hh[m] + P.hh[pb]) * 0.5f, sepf(pp, ldpf(S, S.og + s)), dummy));
+    A.tick();
+  }
+  A.flush();
+  F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
+  F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
+  if (lane == 0) {
+    st3(out.lF + 3 * bI, F);
+    Eout[bI] = E;
+  }
+}
+
+// Chain beads, one CTA each.
+__global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, DevState X, const double* Fm,
+                                                                   const double* Tm, const double* Ech, DevScratch S,
+                                                                   DevForces out, double* Eout) {
+  __shared__ double red[32 * 7];
+  __shared__ LHf P;
+  load_lhf(M, P);
+  const int j = blockIdx.x;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  V3 rj = ld3(X.r + 3 * j), aj = ld3(X.a + 3 * j), bj = ld3(X.b + 3 * j), cj = ld3(X.c + 3 * j);
+  V3 F{0.0, 0.0, 0.0}, T{0.0, 0.0, 0.0};
+  double E = 0.0;
+  const float ke = (float)M.k_e, kap = (float)M.debye, kex = (float)M.k_ex, ql = (float)M.q_l;
+  const PF pj = ldpf(S, j);
+  FAcc A;
+  A.init();
+  float dummy = 0.f;
+  if (M.type[j] == 0) {
+    if (chain_ok(M, j)) {  // DNA/DNA (func.cpp:1326-1354); energy on the lower index
+      const float kll = (float)M.debyell, qq = ke * ql * ql, sDD = (float)M.sDD;
+      for (int i = tid; i < M.n; i += nt) {
+        if (i == j || M.type[i] != 0 || abs(i - j) <= 1 || !chain_ok(M, i)) continue;
+        const float3 z = sepf(pj, ldpf(S, i));
+        const float df = sqrtf(fmaf(z.x, z.x, fmaf(z.y, z.y, z.z * z.z)));
+        if (df > 25.f) continue;
+        const float mi = 1.f / df, ex = expf(-kll * df);
+        float g = qq * ex * fmaf(kll, df, 1.f) / (df * df), e = qq * ex / df;
+        if (df <= 8.f) {
+          const float sr = sDD / df, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+          g += kex * (12.f * sr12 - 6.f * sr6) / df;
+          e += kex * (sr12 - sr6);
+        }
+        if (j < i) A.f[6] += e;
+        A.force(make_float3(g * z.x * mi, g * z.y * mi, g * z.z * mi));
+        A.tick();
+      }
+    }
+    const float qlk = ke * ql, sTL = (float)M.sTL;
+    for (int t = tid; t < M.n_tail; t += nt) {  // tails on this DNA bead; energy on the tail side
+      A.force(pairf<true, true>(qlk * M.t_qf[t], kap, kex, sTL, sepf(pj, ldpf(S, S.ot + t)), dummy));
+      A.tick();
+    }
+    for (int b = tid; b < M.n_LH; b += nt) {  // LH beads; energy on the LH side
+      int p = lh_param(M, b);
+      A.force(pairf<true, true>(qlk * P.q[p], kap, kex, P.hl[p], sepf(pj, ldpf(S, S.ol + b)), dummy));
+      A.tick();
+    }
+    for (int s = tid; s < M.n_lhcore * M.n_lh_g; s += nt) {  // globular heads; energy on the core side
+      int m = s % M.n_lh_g;
+      A.force(pairf<true, true>(qlk * P.q[m], kap, kex, P.hl[m], sepf(pj, ldpf(S, S.og + s)), dummy));
+      A.tick();
+    }
+  } else {
+    const int J = M.core_rank[j];
+    const int lc = M.core_lh[J];
+    if (lc >= 0) {
+      const int ng = M.n_lh_g;
+      for (int s = tid; s < ng * M.n; s += nt) {  // G-head vs linker DNA (func.cpp:2481-2522); energy here
+        int m = s / M.n, l = s - m * M.n;
+        if (M.type[l] != 0) continue;
+        const PF g = ldpf(S, S.og + lc * ng + m);
+        const float3 f1 = pairf<true, true>(ke * P.q[m] * ql, kap, kex, P.hl[m], sepf(g, ldpf(S, l)), A.f[6]);
+        A.force(f1);
+        A.torque(crossf(sepf(g, pj), f1));
+        A.tick();
+      }
+      for (int s = tid; s < ng * M.n_tail; s += nt) {  // G-head vs tails (func.cpp:2403-2476)
+        int m = s / M.n_tail, t = s - m * M.n_tail;
+        const PF g = ldpf(S, S.og + lc * ng + m);
+        const float3 f1 = pairf<true, true>(ke * P.q[m] * M.t_qf[t], kap, kex, P.ht[m], sepf(g, ldpf(S, S.ot + t)),
+                                            A.f[6]);
+        A.force(f1);
+        A.torque(crossf(sepf(g, pj), f1));
+        A.tick();
+      }
+      for (int s = tid; s < ng * M.n_LH; s += nt) {  // G-head vs other LHs' beads (func.cpp:2590-2644)
+        int m = s / M.n_LH, b = s - m * M.n_LH;
+        if (b / M.nlh == lc) continue;
+        int p2 = lh_param(M, b);
+        const PF g = ldpf(S, S.og + lc * ng + m);
+        const float3 f1 = pairf<true, true>(ke * P.q[m] * P.q[p2], kap, kex, (P.hh[m] + P.hh[p2]) * 0.5f,
+                                            sepf(g, ldpf(S, S.ol + b)), A.f[6]);
+        A.force(f1);
+        A.torque(crossf(sepf(g, pj), f1));
+        A.tick();
+      }
+      for (int s = tid; s < ng * M.n_lhcore * ng; s += nt) {  // G-head/G-head (func.cpp:2649-2719); lower core
+        int m = s / (M.n_lhcore * ng), rest = s - m * (M.n_lhcore * ng);
+        int K = rest / ng, m1 = rest - K * ng;
+        if (K == lc) continue;
+        const PF g = ldpf(S, S.og + lc * ng + m);
+        float e = 0.f;
+        const float3 f1 = pairf<true, true>(ke * P.q[m] * P.q[m1], kap, kex, (P.hh[m] + P.hh[m1]) * 0.5f,
+                                            sepf(g, ldpf(S, S.og + K * ng + m1)), e);
+        if (lc < K) A.f[6] += e;
+        A.force(f1);
+        A.torque(crossf(sepf(g, pj), f1));
+        A.tick();
+      }
+      if (tid == 0) {  // G-head <-> first C-term bead anchor (func.cpp:2725-2777), FP64
+        for (int jj = 0; jj < ng; jj++) {
+          int pjj = jj + M.n_lh_n;
+          if (M.LH_conn[pjj] != 1) continue;
+          V3 g = ld3(X.gpos + 3 * (lc * ng + jj));
+          V3 q = ld3(X.r_lh + 3 * (lc * M.nlh));
+          double d = sqrt((q.x - g.x) * (q.x - g.x) + (q.y - g.y) * (q.y - g.y) + (q.z - g.z) * (q.z - g.z));
+          double kst = M.LH_kstr[pjj], eq = M.LH_streq[pjj];
+          E = E + kst * (d - eq) * (d - eq) / 2;
+          V3 st{(d - eq) * (q.x - g.x) / d, (d - eq) * (q.y - g.y) / d, (d - eq) * (q.z - g.z) / d};
+          F.x = F.x + kst * st.x * 10; F.y = F.y + kst * st.y * 10; F.z = F.z + kst * st.z * 10;
+          double fa = kst * (aj.x * st.x + aj.y * st.y + aj.z * st.z);
+          double fb = kst * (bj.x * st.x + bj.y * st.y + bj.z * st.z);
+          double fc = kst * (cj.x * st.x + cj.y * st.y + cj.z * st.z);
+          const double* gp = M.LH_g_pos + 3 * jj;
+          T.x = T.x + fc * gp[1] - fb * gp[2];
+          T.y = T.y + fa * gp[2] - fc * gp[0];
+          T.z = T.z + fb * gp[0] - fa * gp[1];
+        }
+      }
+    }
+    if (M.nc_t_flag[J] == 1) {  // tail anchors of this core (func.cpp:1971-2022), FP64
+      for (int jt = tid; jt < M.n_t; jt += nt) {
+        if (M.tail_fix[jt] != 1) continue;
+        V3 ro = body(rj, aj, bj, cj, M.tail_pos + 3 * jt);
+        int tb = J * M.n_t + jt;
+        V3 rt = ld3(X.r_t + 3 * tb);
+        V3 st{rt.x - ro.x, rt.y - ro.y, rt.z - ro.z};
+        E = E + M.h * (st.x * st.x + st.y * st.y + st.z * st.z) / 2;
+        V3 hs{M.h * st.x, M.h * st.y, M.h * st.z};
+        acc(F, hs);
+        acc(T, torque_rel(hs, M.tail_pos + 3 * jt, aj, bj, cj));
+      }
+    }
+    // LH and G-head forces on this core's anchored tail beads go to the core
+    // (func.cpp:2361-2391, 2436-2465)
+    const int t_lo = M.tails_by_core ? J * M.n_t : 0;
+    const int t_hi = M.tails_by_core ? min((J + 1) * M.n_t, M.n_tail) : M.n_tail;
+    for (int t0 = t_lo; t0 < t_hi; t0++) {
+      if (M.t_fix[t0] == 0 || M.t_core_bead[t0] != j) continue;
+      const PF pt = ldpf(S, S.ot + t0);
+      const float3 lever = sepf(pt, pj);
+      const float qt = ke * M.t_qf[t0];
+      for (int b = tid; b < M.n_LH; b += nt) {
+        int p = lh_param(M, b);
+        const float3 f2 = pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], sepf(pt, ldpf(S, S.ol + b)), dummy);
+        A.force(f2);
+        A.torque(crossf(lever, f2));
+        A.tick();
+      }
+      for (int s = tid; s < M.n_lhcore * M.n_lh_g; s += nt) {
+        int m = s % M.n_lh_g;
+        const float3 f2 = pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + s)), dummy);
+        A.force(f2);
+        A.torque(crossf(lever, f2));
+        A.tick();
+      }
+    }
+  }
+  A.flush();
+  F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
+  // world-frame torques of the pair terms into the body frame
+  T.x += aj.x * A.s[3] + aj.y * A.s[4] + aj.z * A.s[5];
+  T.y += bj.x * A.s[3] + bj.y * A.s[4] + bj.z * A.s[5];
+  T.z += cj.x * A.s[3] + cj.y * A.s[4] + cj.z * A.s[5];
+  chain_finish(M, S, Fm, Tm, Ech, out, Eout, j, F, T, E, red);
+}
+
 // Total energy: chain, tail and LH shares in a fixed order.
 __global__ void k_energy(int n0, const double* e0, double* E) {
   __shared__ double red[32];
@@ -984,6 +1416,7 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   auto k_chain_gatherX = KSEL(k_chain_gather);
 #undef KSEL
   if (M.n_lhcore > 0) { k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X); L++; }
+  if (mixed) { k_mirror<<<cdiv(S.npos, 128), 128, 0, st>>>(M, X, S.ph, S.pl, S.npos); L++; }
   k_chain_bonded<<<cdiv(M.n, 128), 128, 0, st>>>(M, X, Fm, Tm, Ebond);
   L++;
   if (M.n_c > 1) {
@@ -998,9 +1431,15 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   }
   if (M.n_dna > 0 && M.n_c > 0) { k_dna_coreX<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc); L++; }
   if (M.n_lhcore > 0) { k_ghead_coreX<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc); L++; }
-  if (M.n_tail > 0) { k_tail_gatherX<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et); L++; }
-  if (M.n_LH > 0) { k_lh_gatherX<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El); L++; }
-  k_chain_gatherX<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
+  if (mixed) {
+    if (M.n_tail > 0) { k_tail_gather_mx<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, S, out, Et); L++; }
+    if (M.n_LH > 0) { k_lh_gather_mx<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, S, out, El); L++; }
+    k_chain_gather_mx<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
+  } else {
+    if (M.n_tail > 0) { k_tail_gatherX<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et); L++; }
+    if (M.n_LH > 0) { k_lh_gatherX<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El); L++; }
+    k_chain_gatherX<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
+  }
   k_energy<<<1, 256, 0, st>>>(M.n + M.n_tail + M.n_LH, S.ebuf, out.E);
   return L + 2;
 }
