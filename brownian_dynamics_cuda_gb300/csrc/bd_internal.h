@@ -120,7 +120,7 @@ void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream
 // returns the number of kernels launched
 int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);
 // rpy_chol.cu
-// df: store each element as the double-float pair (hi, lo) of FP32 (mixed path)
+// df: mixed path, FP32 RPY blocks stored as double-float pairs (value, 0)
 void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
                   cudaStream_t st, bool df = false);
 int potrf_fp64(int m, double* A, int lda, double* rd_acc, const double* p, double s2dt, int* d_negpiv,

@@ -25,19 +25,6 @@ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 // ------------------------------------------------------------ RPY
 constexpr int kRpyTile = 32;
 
-// element store: FP64, or the double-float pair (hi, lo) of the mixed path
-template <bool DF>
-__device__ __forceinline__ void st_elem(double* A, size_t idx, double x) {
-  if (DF) {
-    const float hi = __double2float_rn(x);
-    const float lo = __double2float_rn(x - (double)hi);
-    reinterpret_cast<float2*>(A)[idx] = make_float2(hi, lo);
-  } else {
-    A[idx] = x;
-  }
-}
-
-template <bool DF>
 __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ r, const double* __restrict__ rad,
                                              double a1, double a2, double* __restrict__ A, int lda) {
   int bi = blockIdx.y, bj = blockIdx.x;
@@ -51,7 +38,7 @@ __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ 
     if (j >= nD || j > i) continue;
     if (j == i) {
       for (int l = 0; l < 3; l++)
-        for (int k = l; k < 3; k++) st_elem<DF>(A, (size_t)(3 * j + l) * lda + 3 * i + k, (k == l) ? a1 / radi : 0.0);
+        for (int k = l; k < 3; k++) A[(size_t)(3 * j + l) * lda + 3 * i + k] = (k == l) ? a1 / radi : 0.0;
       continue;
     }
     V3 rj = ld3(r + 3 * j);
@@ -62,8 +49,38 @@ __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ 
     double Db[3][3];
     rpy_block(sij, ssq, s, radi, radj, a1, a2, Db);
     for (int l = 0; l < 3; l++) {
-      const size_t col = (size_t)(3 * j + l) * lda + 3 * i;
-      for (int k = 0; k < 3; k++) st_elem<DF>(A, col + k, Db[k][l]);
+      double* col = A + (size_t)(3 * j + l) * lda + 3 * i;
+      for (int k = 0; k < 3; k++) col[k] = Db[k][l];
+    }
+  }
+}
+
+// Mixed path: the same lower triangle from the FP32 form of the RPY block
+// (separations formed in FP64, then FP32), stored as the double-float pair
+// (value, 0).  No FP64 arithmetic beyond the separation.
+__global__ void __launch_bounds__(256) k_rpy_mx(int nD, const double* __restrict__ r, const double* __restrict__ rad,
+                                                double a1, double a2, float2* __restrict__ A, int lda) {
+  int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj > bi) return;
+  int i = bi * kRpyTile + threadIdx.x;
+  if (i >= nD) return;
+  const V3 ri = ld3(r + 3 * i);
+  const float radi = (float)rad[i], a1f = (float)a1, a2f = (float)a2;
+  for (int jj = threadIdx.y; jj < kRpyTile; jj += blockDim.y) {
+    int j = bj * kRpyTile + jj;
+    if (j >= nD || j > i) continue;
+    if (j == i) {
+      for (int l = 0; l < 3; l++)
+        for (int k = l; k < 3; k++)
+          A[(size_t)(3 * j + l) * lda + 3 * i + k] = make_float2((k == l) ? a1f / radi : 0.f, 0.f);
+      continue;
+    }
+    const V3 rj = ld3(r + 3 * j);
+    float Db[3][3];
+    rpy_block_f((float)(ri.x - rj.x), (float)(ri.y - rj.y), (float)(ri.z - rj.z), radi, (float)rad[j], a1f, a2f, Db);
+    for (int l = 0; l < 3; l++) {
+      float2* col = A + (size_t)(3 * j + l) * lda + 3 * i;
+      for (int k = 0; k < 3; k++) col[k] = make_float2(Db[k][l], 0.f);
     }
   }
 }
@@ -212,22 +229,37 @@ __global__ void __launch_bounds__(kRdRows) k_trmv_part(int m, const double* __re
   if (i < m) part[(size_t)kc * m + i] = s;
 }
 
-// the same over the double-float factor of the mixed path
+// The same over the double-float factor of the mixed path, in FP32
+// arithmetic: each product L_ik p_k is formed exactly as x + ex (p split into
+// FP32 hi + lo once per CTA, FMA for the rounding error of L_ik p_hi) and
+// summed with a two-sum into (s, c); ~40 significant bits per partial sum.
 __global__ void __launch_bounds__(kRdRows) k_trmv_part_df(int m, const float2* __restrict__ A, int lda,
                                                           const double* __restrict__ p, double s2dt,
                                                           double* __restrict__ part) {
+  __shared__ float2 ps[kRdChunk];
   int i = blockIdx.x * kRdRows + threadIdx.x;
   int kc = blockIdx.y;
   int k0 = kc * kRdChunk, k1 = min(k0 + kRdChunk, m);
-  double s = 0.0;
-  if (i < m) {
-    int kend = min(k1, i + 1);
-    for (int k = k0; k < kend; k++) {
-      const float2 a = A[(size_t)k * lda + i];
-      s = s + (s2dt * ((double)a.x + (double)a.y)) * p[k];
-    }
+  for (int k = k0 + threadIdx.x; k < k1; k += kRdRows) {
+    const double pk = p[k];
+    const float h = (float)pk;
+    ps[k - k0] = make_float2(h, (float)(pk - (double)h));
   }
-  if (i < m) part[(size_t)kc * m + i] = s;
+  __syncthreads();
+  if (i >= m) return;
+  float sh = 0.f, sc = 0.f;
+  int kend = min(k1, i + 1);
+  for (int k = k0; k < kend; k++) {
+    const float2 a = A[(size_t)k * lda + i];
+    const float2 q = ps[k - k0];
+    const float x = a.x * q.x;
+    const float ex = fmaf(a.x, q.x, -x) + fmaf(a.x, q.y, a.y * q.x);
+    const float t = sh + x;
+    const float bp = t - sh;
+    sc += ((sh - (t - bp)) + (x - bp)) + ex;
+    sh = t;
+  }
+  part[(size_t)kc * m + i] = s2dt * ((double)sh + (double)sc);
 }
 
 __global__ void k_trmv_sum(int m, int nchunk, const double* __restrict__ part, double* __restrict__ rd) {
@@ -246,9 +278,9 @@ void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, dou
                   cudaStream_t st, bool df) {
   int nt = cdiv(nD, kRpyTile);
   if (df)
-    k_rpy<true><<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
+    k_rpy_mx<<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, reinterpret_cast<float2*>(A), lda);
   else
-    k_rpy<false><<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
+    k_rpy<<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
 }
 
 int potrf_fp64(int m, double* A, int lda, double* /*rd_acc*/, const double* /*p*/, double /*s2dt*/, int* d_negpiv,

@@ -20,13 +20,16 @@ def case(request):
     return request.param, fib, z
 
 
-def test_mixed_tensor_storage(case):
-    """The double-float tensor holds the FP64 RPY tensor to ~2^-48."""
+def test_mixed_tensor_fp32(case):
+    """The mixed path assembles the RPY tensor in FP32 (separations formed in
+    FP64): every entry within a few FP32 ulps of the FP64 tensor."""
     from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
     name, fib, z = case
     D64 = Context(fib, precision=PREC_FP64).diffusion_tensor()
     Dm = Context(fib, precision=PREC_MIXED).diffusion_tensor()
-    assert np.abs(Dm - D64).max() <= 1e-13 * np.abs(D64).max()
+    assert np.abs(Dm - D64).max() <= 5e-7 * np.abs(D64).max()
+    big = np.abs(D64) > 1e-3 * np.abs(D64).max()
+    assert (np.abs(Dm - D64)[big] / np.abs(D64)[big]).max() <= 2e-6
 
 
 def test_mixed_factor_matches_fp64(case):
