@@ -142,6 +142,31 @@ __device__ __forceinline__ void dp_row_solve(float* row, const float (*Lf)[kLd],
 
 // Runs in a CTA of kRestThreads threads; threads >= kDpThreads only take
 // part in the barriers.  `b` is the CTA's index among the panel CTAs.
+// Cholesky of a 32 x 32 block held by one warp, lane i holding row i (a[j],
+// j <= i), right-looking in registers: pivot from lane c, 1/sqrt once
+// (rsqrt), column c scaled, rank-1 update of the columns to its right with
+// L[j][c] shuffled from lane j.  FULL (w == 32) is branch-free, so the
+// compiler can start column c+1's pivot while column c's update is in
+// flight.  Lane c keeps 1/L[c][c] in invv and flags a negative pivot
+// (replaced by its absolute value, func.cpp:827-833).
+template <bool FULL>
+__device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, float& invv, int& neg) {
+#pragma unroll
+  for (int c = 0; c < 32; c++) {
+    if (!FULL && c >= w) break;
+    const float d = __shfl_sync(0xffffffffu, a[c], c);
+    const float ad = fabsf(d);
+    const float inv = rsqrtf(ad);
+    if (lane == c) {
+      invv = inv;
+      neg = d < 0.f;
+    }
+    a[c] = (lane == c) ? ad * inv : ((lane > c) ? a[c] * inv : a[c]);
+#pragma unroll
+    for (int j = c + 1; j < 32; j++) a[j] = fmaf(-a[c], __shfl_sync(0xffffffffu, a[c], j), a[j]);
+  }
+}
+
 __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, int lda, int m, int k0, int kb, int tile0,
                                             int b, unsigned char* PS, int* negpiv) {
   float (*Ls)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);
@@ -189,25 +214,12 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, int lda, int
       float a[32];
 #pragma unroll
       for (int j = 0; j < 32; j++) a[j] = (lane < w && j <= lane) ? Ls[c0 + lane][c0 + j] : 0.f;
-#pragma unroll
-      for (int c = 0; c < 32; c++) {
-        if (c < w) {
-          const float d = __shfl_sync(0xffffffffu, a[c], c);
-          const float piv = sqrtf(fabsf(d));
-          const float inv = 1.f / piv;
-          if (lane == 0) {
-            invd[c0 + c] = inv;
-            if (is_diag && d < 0.f) atomicAdd(negpiv, 1);
-          }
-          if (lane == c) a[c] = piv;
-          else if (lane > c) a[c] *= inv;
-#pragma unroll
-          for (int j = c + 1; j < 32; j++) {
-            const float ljc = __shfl_sync(0xffffffffu, a[c], j);
-            a[j] = fmaf(-a[c], ljc, a[j]);
-          }
-        }
-      }
+      float invv = 0.f;
+      int neg = 0;
+      if (w == 32) warp_chol32<true>(a, 32, lane, invv, neg);
+      else warp_chol32<false>(a, w, lane, invv, neg);
+      if (lane < w) invd[c0 + lane] = invv;
+      if (is_diag && neg) atomicAdd(negpiv, 1);
 #pragma unroll
       for (int j = 0; j < 32; j++)
         if (lane < w && j <= lane) Ls[c0 + lane][c0 + j] = a[j];
@@ -599,4 +611,5 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
 }
 
 }  // namespace bdk
+
 
