@@ -241,7 +241,8 @@ def run_ours(args):
     prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
     fib, spec = make_fiber(args.config, 1 + rank)
     stream = torch.cuda.Stream()
-    ctx = Context(fib, precision=prec, use_graph=True, device=local, stream=stream.cuda_stream)
+    freq = args.frequency_rp
+    ctx = Context(fib, precision=prec, use_graph=True, frequency_RP=freq, device=local, stream=stream.cuda_stream)
     n3, m = 3 * fib.sizes["n"], fib.m
     nsteps = args.warmup + args.steps
     noise = Noise(1000 + rank)
@@ -284,7 +285,7 @@ def run_ours(args):
     launches = ctx.launch_count() * args.steps
     # e2e: reference-facing call with host buffers (noise H2D, r_lh D2H every
     # step, full state D2H on sampling steps every 100 steps)
-    e2e_ctx = Context(fib, precision=prec, use_graph=True, device=local, stream=stream.cuda_stream)
+    e2e_ctx = Context(fib, precision=prec, use_graph=True, frequency_RP=freq, device=local, stream=stream.cuda_stream)
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
     rr_h = [pin(h[0]) for h in host]
     p_h = [pin(h[1]) for h in host]
@@ -332,7 +333,7 @@ def run_ours(args):
     # the plain FP64 step on the same fiber and noise: the metric's reference
     # point, and the mixed step's displacement error against it
     vs64 = None
-    if prec == PREC_MIXED:
+    if prec == PREC_MIXED and not args.no_fp64:
         vs64 = fp64_comparison(fib, rr_d, p_d, host, args, local, stream)
         if world > 1:
             vs64["fp64_steps_per_s"] = replica_rate(max_over_ranks(1000.0 / vs64["fp64_steps_per_s"]), world)
@@ -348,6 +349,7 @@ def run_ours(args):
                 "vs_baseline": None, "dtype": "f64" if prec == PREC_FP64 else "bf16x3+f64",
                 "data": "synthetic (seeded fiber generator, reference file formats)",
                 "config": {"workload": spec.name, "n_D": fib.n_D, "3N": m, "precision": args.precision,
+                           "frequency_RP": args.frequency_rp,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (D is %.2f GB)" %
                                                                          (m * m * 8 / 1e9)},
                 "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
@@ -361,18 +363,84 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batch(args):
+    """Config 2: replicas of uneven size and salt (nucleosomes 12-48, linkers
+    20-60 bp, 50/100/150 mM) advanced together through bd_batch_* (one CUDA
+    graph per batch step); metric replica-steps/s."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Batch, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber as mk
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
+    fibers = [mk(config(2, seed=1 + rank, replica=i), tempfile.mkdtemp(prefix="bdrep_")) for i in range(args.replicas)]
+    stream = torch.cuda.Stream()
+    b = Batch(fibers, precision=prec, use_graph=True, device=local, stream=stream.cuda_stream)
+    nsteps = args.warmup + args.steps
+    gens = [Noise(1000 + i) for i in range(len(fibers))]
+    host = [[g.step(s, f.arrays["r_var"], f.m) for s in range(nsteps)] for g, f in zip(gens, fibers)]
+    d_rr = [[torch.tensor(h[s][0], device="cuda") for s in range(nsteps)] for h in host]
+    d_p = [[torch.tensor(h[s][1], device="cuda") for s in range(nsteps)] for h in host]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for s in range(args.warmup):
+            b.step_device([x[s].data_ptr() for x in d_rr], [x[s].data_ptr() for x in d_p])
+        stream.synchronize()
+        clk = ClockSampler(local)
+        clk.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(args.warmup, nsteps):
+            b.step_device([x[s].data_ptr() for x in d_rr], [x[s].data_ptr() for x in d_p])
+        e1.record(stream)
+        stream.synchronize()
+        clocks = clk.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = world * len(fibers) * 1000.0 / ms
+    # e2e: host noise per replica per step through bd_batch_step
+    t0 = time.perf_counter()
+    for s in range(args.warmup, nsteps):
+        b.step([h[s][0] for h in host], [h[s][1] for h in host])
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    h2d = sum((3 * f.sizes["n"] + f.m) * 8 for f in fibers)
+    sizes = [f.m for f in fibers]
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "replica-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if prec == PREC_FP64 else "bf16x3+f64",
+                "data": "synthetic (seeded fiber generator, reference file formats)",
+                "config": {"workload": "cfg2_replicas", "replicas": len(fibers), "3N_min": min(sizes),
+                           "3N_max": max(sizes), "3N_sum": sum(sizes), "precision": args.precision,
+                           "parallelism": f"replicas x{world}", "l2": "inputs larger than L2"},
+                "e2e": {"value": world * len(fibers) / e2e_s, "unit": "replica-steps/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": 8 * len(fibers)},
+                "gpu_launches": None, "clocks": clocks, "roofline": None, "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+    b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 5; 10 for config 4)")
+    ap.add_argument("--warmup", type=int, default=None, help="warm-up steps (default 3; 10 for config 4)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--replicas", type=int, default=256, help="config 2: number of replicas")
+    ap.add_argument("--frequency-rp", type=int, default=None,
+                    help="rebuild and refactor D every k steps (default 1; 10 for config 4)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg of the mixed run")
     args = ap.parse_args()
+    big = args.config == 4
+    args.frequency_rp = args.frequency_rp or (10 if big else 1)
+    args.steps = args.steps if args.steps is not None else (10 if big else 5)
+    args.warmup = args.warmup if args.warmup is not None else (10 if big else 3)
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == 2:
+        run_batch(args)
     else:
         run_ours(args)
 

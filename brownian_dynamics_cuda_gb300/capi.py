@@ -89,6 +89,14 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_sizes.argtypes = [C.c_void_p, _ip]
     L.bd_step.argtypes = [C.c_void_p, _dp, _dp, _dp]
     L.bd_step_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bd_batch_create.argtypes = [C.c_int, C.POINTER(bd_model), C.POINTER(bd_state), C.POINTER(bd_options),
+                                  C.POINTER(C.c_void_p)]
+    L.bd_batch_destroy.argtypes = [C.c_void_p]
+    L.bd_batch_size.argtypes = [C.c_void_p, _ip]
+    L.bd_batch_context.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+    L.bd_batch_step.argtypes = [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp), _dp]
+    L.bd_batch_step_device.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+    L.bd_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_ulong, _dp]
     L.bd_step_reference.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp] + [_dp] * 6
     L.bd_forces.argtypes = [C.c_void_p] + [_dp] * 5
     L.bd_diffusion_tensor.argtypes = [C.c_void_p, _dp]
@@ -293,9 +301,23 @@ class Context:
         _check(self._L.bd_sizes(self._h, sz))
         self.n, self.n_c, self.n_tail, self.n_LH, self.n_D, self.m, self.lda, self.precision = list(sz)
 
+    @classmethod
+    def _view(cls, handle: C.c_void_p, fiber: Fiber) -> "Context":
+        """A non-owning Context over a handle another object owns (a batch replica)."""
+        self = cls.__new__(cls)
+        self._L = load_library()
+        self.fiber = fiber
+        self._h = handle
+        self._owned = False
+        sz = (C.c_int * 8)()
+        _check(self._L.bd_sizes(self._h, sz))
+        self.n, self.n_c, self.n_tail, self.n_LH, self.n_D, self.m, self.lda, self.precision = list(sz)
+        return self
+
     def close(self) -> None:
         if getattr(self, "_h", None):
-            self._L.bd_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._L.bd_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -375,3 +397,59 @@ class Context:
         v = C.c_int()
         _check(self._L.bd_negative_pivots(self._h, C.byref(v)))
         return v.value
+
+
+class Batch:
+    """Independent fibers (replicas) advanced together (bd_batch_*): one
+    stream, one CUDA graph per batch step running every replica's step."""
+
+    def __init__(self, fibers: list, precision: int = PREC_MIXED, use_graph: bool = True, device: int = 0,
+                 stream: int = 0):
+        self._L = load_library()
+        self.fibers = list(fibers)
+        R = len(self.fibers)
+        models = (bd_model * R)(*[f.model_struct() for f in self.fibers])
+        states = (bd_state * R)(*[f.state_struct() for f in self.fibers])
+        o = bd_options(precision=precision, frequency_RP=1, use_graph=int(use_graph), device=device,
+                       stream=C.c_void_p(stream) if stream else None)
+        self._h = C.c_void_p()
+        _check(self._L.bd_batch_create(R, models, states, C.byref(o), C.byref(self._h)))
+        self.contexts = []
+        for i in range(R):
+            h = C.c_void_p()
+            _check(self._L.bd_batch_context(self._h, i, C.byref(h)))
+            self.contexts.append(Context._view(h, self.fibers[i]))
+
+    def __len__(self) -> int:
+        return len(self.fibers)
+
+    def step(self, rrs: list, ps: list) -> np.ndarray:
+        R = len(self)
+        rrs = [np.ascontiguousarray(x, dtype=np.float64) for x in rrs]  # kept alive for the call
+        ps = [np.ascontiguousarray(x, dtype=np.float64) for x in ps]
+        rr = (_dp * R)(*[_pd(x) for x in rrs])
+        pp = (_dp * R)(*[_pd(x) for x in ps])
+        e = np.zeros(R)
+        _check(self._L.bd_batch_step(self._h, rr, pp, _pd(e)))
+        return e
+
+    def step_device(self, d_rr: list, d_p: list) -> None:
+        R = len(self)
+        a = (C.c_void_p * R)(*[C.c_void_p(x) for x in d_rr])
+        b = (C.c_void_p * R)(*[C.c_void_p(x) for x in d_p])
+        _check(self._L.bd_batch_step_device(self._h, a, b))
+
+    def run(self, nsteps: int, seed_base: int) -> np.ndarray:
+        e = np.zeros(len(self))
+        _check(self._L.bd_batch_run(self._h, nsteps, seed_base, _pd(e)))
+        return e
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            for c in self.contexts:
+                c._h = None
+            self._L.bd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

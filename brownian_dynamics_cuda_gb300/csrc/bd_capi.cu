@@ -97,6 +97,7 @@ struct bd_ctx {
   double kflop = 0.0;
   // host copies for the drop-in paths
   std::vector<int> h_type;
+  std::vector<double> h_rvar;  // rotational noise scale (bd_batch_run draws noise on the host)
 };
 
 namespace {
@@ -254,6 +255,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   M.n_dna = (int)dna_bead.size();
   M.n_lhcore = (int)lh_core_bead.size();
   c->h_type.assign(m->type, m->type + n);
+  if (m->r_var) c->h_rvar.assign(m->r_var, m->r_var + 3 * (size_t)n);
   double qmax = 0, gmax = 0;
   for (int k = 0; k < M.Nq; k++) {
     const double* p = m->core_pos + 3 * k;
@@ -728,5 +730,177 @@ extern "C" int bd_negative_pivots(bd_ctx* c, int* out) {
   CK(cudaMemcpyAsync(&c->host_negpiv, c->negpiv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   *out = c->host_negpiv;
+  return BD_OK;
+}
+
+// ------------------------------------------------------------ batches
+struct bd_batch {
+  std::vector<bd_ctx*> ctx;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int use_graph = 0;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<bd_noise*> noise;
+  std::vector<std::vector<double>> h_rr, h_p;
+};
+
+static int batch_device_step(bd_batch* b) {
+  bool graph_ok = b->use_graph;
+  for (bd_ctx* c : b->ctx) graph_ok = graph_ok && c->freq_rp == 1;
+  if (graph_ok) {
+    if (!b->graph) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = BD_OK;
+      for (bd_ctx* c : b->ctx)
+        if (!rc) rc = step_device(c, c->rr, c->p);
+      cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+      if (rc) return rc;
+      if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_batch: graph capture failed");
+      e = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_batch: graph instantiation failed");
+    }
+    CK(cudaGraphLaunch(b->graph, b->stream));
+  } else {
+    for (bd_ctx* c : b->ctx) {
+      int rc = step_device(c, c->rr, c->p);
+      if (rc) return rc;
+    }
+  }
+  for (bd_ctx* c : b->ctx) c->step_count++;
+  return BD_OK;
+}
+
+extern "C" int bd_batch_create(int nrep, const bd_model* models, const bd_state* states, const bd_options* opt,
+                               bd_batch** out) {
+  if (nrep <= 0 || !models || !states || !out) return set_error(BD_ERR_ARG, "bd_batch_create: bad argument");
+  bd_batch* b = new bd_batch();
+  bd_options o{};
+  if (opt) o = *opt;
+  else o.precision = BD_PREC_FP64, o.frequency_RP = 1;
+  if (cudaSetDevice(o.device) != cudaSuccess) {
+    delete b;
+    return set_error(BD_ERR_CUDA, "bd_batch_create: cudaSetDevice failed");
+  }
+  b->stream = static_cast<cudaStream_t>(o.stream);
+  if (!b->stream) {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete b;
+      return set_error(BD_ERR_CUDA, "bd_batch_create: stream creation failed");
+    }
+    b->own_stream = true;
+  }
+  b->use_graph = o.use_graph;
+  o.stream = b->stream;
+  o.use_graph = 0;  // the batch captures one graph for all replicas
+  for (int i = 0; i < nrep; i++) {
+    bd_ctx* c = nullptr;
+    int rc = bd_create(&models[i], &states[i], &o, &c);
+    if (rc) {
+      bd_batch_destroy(b);
+      return rc;
+    }
+    b->ctx.push_back(c);
+  }
+  *out = b;
+  return BD_OK;
+}
+
+extern "C" int bd_batch_destroy(bd_batch* b) {
+  if (!b) return BD_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (bd_ctx* c : b->ctx) bd_destroy(c);
+  for (bd_noise* g : b->noise) bd_noise_free(g);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return BD_OK;
+}
+
+extern "C" int bd_batch_size(const bd_batch* b, int* nrep) {
+  if (!b || !nrep) return set_error(BD_ERR_ARG, "bd_batch_size: null argument");
+  *nrep = (int)b->ctx.size();
+  return BD_OK;
+}
+
+extern "C" int bd_batch_context(bd_batch* b, int i, bd_ctx** out) {
+  if (!b || !out || i < 0 || i >= (int)b->ctx.size()) return set_error(BD_ERR_ARG, "bd_batch_context: bad argument");
+  *out = b->ctx[i];
+  return BD_OK;
+}
+
+static int batch_finish(bd_batch* b, double* energies) {
+  const int nr = (int)b->ctx.size();
+  std::vector<double> e(nr, 0.0);
+  std::vector<int> derr(nr, 0);
+  for (int i = 0; i < nr; i++) {
+    bd_ctx* c = b->ctx[i];
+    CK(cudaMemcpyAsync(&e[i], c->F0.E, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    if (c->d_err) CK(cudaMemcpyAsync(&derr[i], c->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < nr; i++) {
+    if (derr[i]) return set_error(BD_ERR_CUDA, "bd_batch: a tensor-core kernel timed out");
+    if (!std::isfinite(e[i])) return set_error(BD_ERR_NONFINITE, "bd_batch: non-finite energy");
+    if (energies) energies[i] = e[i];
+  }
+  return BD_OK;
+}
+
+extern "C" int bd_batch_step(bd_batch* b, const double* const* rr, const double* const* p, double* energies) {
+  if (!b || !rr || !p) return set_error(BD_ERR_ARG, "bd_batch_step: null argument");
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    bd_ctx* c = b->ctx[i];
+    if (!rr[i] || !p[i]) return set_error(BD_ERR_ARG, "bd_batch_step: null noise pointer");
+    CK(cudaMemcpyAsync(c->rr, rr[i], 3 * (size_t)c->M.n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(c->p, p[i], (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  }
+  int rc = batch_device_step(b);
+  if (rc) return rc;
+  return batch_finish(b, energies);
+}
+
+extern "C" int bd_batch_step_device(bd_batch* b, const double* const* d_rr, const double* const* d_p) {
+  if (!b || !d_rr || !d_p) return set_error(BD_ERR_ARG, "bd_batch_step_device: null argument");
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    bd_ctx* c = b->ctx[i];
+    if (!d_rr[i] || !d_p[i]) return set_error(BD_ERR_ARG, "bd_batch_step_device: null noise pointer");
+    if (d_rr[i] != c->rr)
+      CK(cudaMemcpyAsync(c->rr, d_rr[i], 3 * (size_t)c->M.n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+    if (d_p[i] != c->p)
+      CK(cudaMemcpyAsync(c->p, d_p[i], (size_t)c->m * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  }
+  return batch_device_step(b);
+}
+
+extern "C" int bd_batch_run(bd_batch* b, int nsteps, unsigned long seed_base, double* energies) {
+  if (!b || nsteps < 0) return set_error(BD_ERR_ARG, "bd_batch_run: bad argument");
+  const size_t nr = b->ctx.size();
+  if (b->noise.empty()) {
+    b->noise.resize(nr, nullptr);
+    b->h_rr.resize(nr);
+    b->h_p.resize(nr);
+    for (size_t i = 0; i < nr; i++) {
+      if (b->ctx[i]->h_rvar.empty()) return set_error(BD_ERR_ARG, "bd_batch_run: a replica's model has no r_var");
+      int rc = bd_noise_create(seed_base + i, &b->noise[i]);
+      if (rc) return rc;
+      b->h_rr[i].resize(3 * (size_t)b->ctx[i]->M.n);
+      b->h_p[i].resize(b->ctx[i]->m);
+    }
+  }
+  std::vector<const double*> prr(nr), pp(nr);
+  for (int s = 0; s < nsteps; s++) {
+    for (size_t i = 0; i < nr; i++) {
+      bd_ctx* c = b->ctx[i];
+      int rc = bd_noise_step(b->noise[i], (int)c->step_count, 3 * c->M.n, c->h_rvar.data(), c->m, b->h_rr[i].data(),
+                             b->h_p[i].data());
+      if (rc) return rc;
+      prr[i] = b->h_rr[i].data();
+      pp[i] = b->h_p[i].data();
+    }
+    int rc = bd_batch_step(b, prr.data(), pp.data(), s + 1 == nsteps ? energies : nullptr);
+    if (rc) return rc;
+  }
   return BD_OK;
 }

@@ -205,6 +205,30 @@ int bd_dev_potrf(bd_ctx* ctx, int m, double* d_A, int lda, int precision, int* d
 int bd_noise_displacement_noalloc(int m, const double* d_L, int lda, const double* d_p, double s2dt, double* d_rd,
                                   void* stream);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent fibers (replicas, e.g. of uneven size and salt) advanced
+ * together.  All replicas share one stream; with use_graph one CUDA graph
+ * holds every replica's step, run in turn (no two replicas' tensor-core
+ * kernels overlap).  No counterpart in the reference, which runs one fiber
+ * per process (main.cpp); each replica's step is the bd_step of its own
+ * context.  Options apply to every replica (frequency_RP must be 1 for the
+ * graph). */
+typedef struct bd_batch bd_batch;
+int bd_batch_create(int nrep, const bd_model* models, const bd_state* states, const bd_options* opt, bd_batch** out);
+int bd_batch_destroy(bd_batch* b);
+int bd_batch_size(const bd_batch* b, int* nrep);
+/* The context of replica i (for bd_get_state, bd_set_state, bd_forces ...). */
+int bd_batch_context(bd_batch* b, int i, bd_ctx** out);
+/* One step of every replica: rr[i], p[i] are replica i's host noise (as for
+ * bd_step); energies[i] (optional) receives its energy. */
+int bd_batch_step(bd_batch* b, const double* const* rr, const double* const* p, double* energies);
+/* The same with device noise; stream-ordered, no host synchronisation. */
+int bd_batch_step_device(bd_batch* b, const double* const* d_rr, const double* const* d_p);
+/* nsteps steps with each replica's own host noise stream (MT19937 seeded
+ * seed_base + i, draws as main.cpp:479-486); energies as bd_batch_step after
+ * the last step. */
+int bd_batch_run(bd_batch* b, int nsteps, unsigned long seed_base, double* energies);
+
 /* Timing of the last step's phases on the device (ms): rpy chol rd forces1
  * update1 frames forces2 update2 total.  Valid after a step with use_graph=0. */
 int bd_phase_times(bd_ctx* ctx, float* out9);
