@@ -7,7 +7,8 @@
 // is ~2 operations per clock per SM); the arithmetic is FP32-class:
 //   k_dpanel    one launch per panel: every CTA factors the 128 x 128
 //               diagonal block in shared memory (FP32, 32-column blocks,
-//               left-looking across blocks), CTA 0 writes it back and the
+//               left-looking across blocks), CTA 0 keeps it in a side buffer
+//               (copied into A after the last panel) and the
 //               others solve one 128-row tile each, L_ik = A_ik L_kk^-T, by
 //               forward substitution, write it back and split it into three
 //               BF16 slices (hi + mid + lo = the FP32 value exactly), stored
@@ -167,7 +168,7 @@ __device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, flo
   }
 }
 
-__device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, int lda, int m, int k0, int kb, int tile0,
+__device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, int lda, int m, int k0, int kb, int tile0,
                                             int b, unsigned char* PS, int* negpiv) {
   float (*Ls)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);
   float (*X)[kLd] = reinterpret_cast<float (*)[kLd]>(reinterpret_cast<float*>(sm4) + kT * kLd);
@@ -230,10 +231,12 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, int lda, int
     __syncthreads();
   }
   if (is_diag) {
+    // L_kk goes to a side buffer, not into A: panel CTAs of this launch that
+    // start after this one has finished (more CTAs than SMs) still read A_kk
     if (work)
-      for (int e = tid; e < kb * kb; e += kDpThreads) {
-        const int c = e / kb, r = e - c * kb;
-        if (r >= c) A[(size_t)(k0 + c) * lda + k0 + r] = make_float2(Ls[r][c], 0.f);
+      for (int e = tid; e < kT * kT; e += kDpThreads) {
+        const int c = e >> 7, r = e & (kT - 1);
+        Ldg[e] = (r >= c && r < kb && c < kb) ? Ls[r][c] : 0.f;  // column-major
       }
     return;
   }
@@ -521,17 +524,28 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
 // and the tiles below it, writing its slices to PSp); the remaining CTAs
 // apply an earlier panel's trailing update (tiles from jlo, slices PSu).
 // The two parts touch disjoint columns and slice buffers.
-__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(float2* A, int lda, int m, int ndp, int pk0, int pkb,
+__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(float2* A, float* Ldg, int lda, int m, int ndp, int pk0, int pkb,
                                                               unsigned char* PSp, int* negpiv, int jlo, int col_only,
                                                               int ntiles, int group,
                                                               const unsigned char* __restrict__ PSu, int* err) {
   extern __shared__ float4 smem4[];
   if ((int)blockIdx.x < ndp) {
-    dpanel_body(smem4, A, lda, m, pk0, pkb, pk0 / kT + 1, (int)blockIdx.x, PSp, negpiv);
+    dpanel_body(smem4, A, Ldg, lda, m, pk0, pkb, pk0 / kT + 1, (int)blockIdx.x, PSp, negpiv);
     return;
   }
   rest_body(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group, (int)blockIdx.x - ndp,
             PSu, err);
+}
+
+// After the last panel: the diagonal factors L_kk from the side buffer into
+// the lower triangles of A's diagonal blocks, as (L, 0) pairs.
+__global__ void __launch_bounds__(256) k_diag_scatter(float2* A, int lda, int m, const float* __restrict__ Ld) {
+  const int k = blockIdx.x, k0 = k * kT, kb = min(kT, m - k0);
+  const float* src = Ld + (size_t)k * kT * kT;
+  for (int e = threadIdx.x; e < kT * kT; e += blockDim.x) {
+    const int c = e >> 7, r = e & (kT - 1);
+    if (r >= c && r < kb && c < kb) A[(size_t)(k0 + c) * lda + k0 + r] = make_float2(src[e], 0.f);
+  }
 }
 
 }  // namespace
@@ -540,7 +554,9 @@ namespace bdk {
 
 // two panel-slice buffers: panel k writes buffer k & 1 while the updates of
 // panel k - 1 still read the other
-size_t mixed_panel_bytes(int m) { return 2 * (size_t)cdiv(m, kT) * kTileBytes; }
+size_t mixed_panel_bytes(int m) {  // two slice buffers, then the diagonal factors
+  return 2 * (size_t)cdiv(m, kT) * kTileBytes + (size_t)cdiv(m, kT) * kT * kT * sizeof(float);
+}
 int mixed_tiles(int m) { return cdiv(m, kT); }
 
 static bool g_attr_done = false;
@@ -585,13 +601,14 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
   int L = 0, pairs = 0;
   auto kb_of = [&](int k) { return (m - k * kT < kT) ? m - k * kT : kT; };
   // panel 0 alone
-  k_chol_step<<<nt, kRestThreads, kRestSmem, st>>>(A, lda, m, nt, 0, kb_of(0), PS, negpiv, 0, 0, 0, 1, PS, err);
+  float* Ld = reinterpret_cast<float*>(PS + 2 * buf);  // [nt][128 x 128] diagonal factors
+  k_chol_step<<<nt, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, nt, 0, kb_of(0), PS, negpiv, 0, 0, 0, 1, PS, err);
   L++;
   for (int k = 0; k + 1 < nt; k++) {
     const int below = nt - k - 1;
     const unsigned char* psk = PS + (size_t)(k & 1) * buf;
     unsigned char* psn = PS + (size_t)((k + 1) & 1) * buf;
-    k_chol_step<<<below, kRestThreads, kRestSmem, st>>>(A, lda, m, 0, 0, 0, psn, negpiv, k + 1, 1, below, 1, psk,
+    k_chol_step<<<below, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, 0, 0, 0, psn, negpiv, k + 1, 1, below, 1, psk,
                                                          err);
     L++;
     const int rest = below - 1;
@@ -600,12 +617,15 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     const int ndp = nt - k - 1;  // panel k+1: its diagonal block and the tiles below it
     if (kev) cudaEventRecord(kev[2 * pairs], st);
     k_chol_step<<<ndp + cdiv(tiles, group), kRestThreads, kRestSmem, st>>>(
-        A, lda, m, ndp, (k + 1) * kT, kb_of(k + 1), psn, negpiv, k + 2, 0, tiles, group, psk, err);
+        A, Ld + (size_t)(k + 1) * kT * kT, lda, m, ndp, (k + 1) * kT, kb_of(k + 1), psn, negpiv, k + 2, 0, tiles,
+        group, psk, err);
     if (kev) cudaEventRecord(kev[2 * pairs + 1], st);
     pairs++;
     if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles;  // BF16 tensor work issued
     L++;
   }
+  k_diag_scatter<<<nt, 256, 0, st>>>(A, lda, m, Ld);
+  L++;
   if (kev_pairs) *kev_pairs = pairs;
   return L;
 }

@@ -68,3 +68,21 @@ def test_cfg1_mixed_factor_matches_fp64(cfg1):
         assert cm.negative_pivots() == 0
         assert np.isfinite(Lm).all()
         assert np.abs(Lm - L64).max() <= 2e-6 * scale
+
+
+def test_mixed_factor_more_panels_than_sms(tmp_path):
+    """3N = 25,410 (199 panels): panel launches have more CTAs than the GPU
+    has SMs, so some panel CTAs start after others have finished; the mixed
+    noise displacement still matches the FP64 one."""
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, make_fiber
+    spec = FiberSpec(110, [26 if k % 2 == 0 else 44 for k in range(110)], lh=True, seed=1,
+                     lh_charge_range=(0.0, 1.0), steps=10, name="n110")
+    fib = make_fiber(spec, str(tmp_path))
+    assert fib.m > 152 * 128
+    p = np.random.default_rng(0).normal(size=fib.m)
+    cm = Context(fib, precision=PREC_MIXED)
+    rm = cm.noise_displacement(p)
+    assert cm.negative_pivots() == 0
+    r64 = Context(fib, precision=PREC_FP64).noise_displacement(p)
+    assert np.abs(rm - r64).max() <= 1e-6 * np.abs(r64).max()
