@@ -32,6 +32,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "BD steps/s vs plain FP64 on 1 GB300 at <=1e-6 rel. error; replica-steps/s"
+# dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one
+# k_chol_step launch (panel 0's bulk update, 3N = 11,700) under ncu
+NCU_TRAFFIC_PER_ALG_BYTE = 1052.7 / 1047.9
 
 
 def peaks():
@@ -320,7 +323,10 @@ def run_ours(args):
         byt = rest_update_bytes(m)
         achieved = byt / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / pk["hbm_gbs"] if achieved else None, "traffic": None,
+                "frac": achieved / pk["hbm_gbs"] if achieved else None,
+                "traffic": byt * NCU_TRAFFIC_PER_ALG_BYTE,
+                "traffic_source": "DRAM read+write per algorithmic byte of one ncu capture "
+                                  "(profiles/k_chol_step_cfg1_mixed.md), times this step's algorithmic bytes",
                 "kernel": "k_chol_step (bulk tcgen05 trailing update, next panel in extra CTAs, FP64 tile "
                           "read-modify-write), %d launches/step, avg %.3f ms" % (nk, ms_k / max(nk, 1)),
                 "algorithmic_bytes_per_step": byt,
