@@ -269,6 +269,7 @@ def run_ours(args):
         ph_ctx.step_device(rr_d[0].data_ptr(), p_d[0].data_ptr())
         phases = ph_ctx.phase_times()
         kt = ph_ctx.kernel_time()
+        kbytes = ph_ctx.kernel_bytes()
         ph_ctx.close()
         barrier()
         torch.cuda.synchronize()
@@ -320,7 +321,7 @@ def run_ours(args):
         roof["frac"] = roof["achieved"] / roof["peak"]
     else:
         ms_k, nk, flop_k = kt
-        byt = rest_update_bytes(m)
+        byt = kbytes
         achieved = byt / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"] if achieved else None,

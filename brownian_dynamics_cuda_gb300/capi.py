@@ -112,6 +112,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_launch_count.argtypes = [C.c_void_p, _ip]
     L.bd_kernel_time.argtypes = [C.c_void_p, C.POINTER(C.c_float), _ip, _dp]
     L.bd_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, _ip]
+    L.bd_kernel_bytes.argtypes = [C.c_void_p, _dp]
     L.bd_negative_pivots.argtypes = [C.c_void_p, _ip]
     _lib = L
     return L
@@ -380,6 +381,12 @@ class Context:
         ms, n, fl = C.c_float(), C.c_int(), C.c_double()
         _check(self._L.bd_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(fl)))
         return ms.value, n.value, fl.value
+
+    def kernel_bytes(self) -> float:
+        """Algorithmic HBM bytes of the tensor-core update launches of the last timed step."""
+        b = C.c_double()
+        _check(self._L.bd_kernel_bytes(self._h, C.byref(b)))
+        return b.value
 
     def kernel_times(self) -> np.ndarray:
         """Per-launch ms of the tensor-core update launches of the last timed step."""

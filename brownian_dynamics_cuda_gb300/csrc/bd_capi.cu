@@ -95,6 +95,7 @@ struct bd_ctx {
   std::vector<cudaEvent_t> kev;   // per-launch events around the tensor-core update (timing steps only)
   int kev_pairs = 0;
   double kflop = 0.0;
+  double kbytes = 0.0;
   // host copies for the drop-in paths
   std::vector<int> h_type;
   std::vector<double> h_rvar;  // rotational noise scale (bd_batch_run draws noise on the host)
@@ -152,9 +153,11 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
     if (mixed) {
       const bool kt = c->timing && !c->kev.empty();
       c->kflop = 0.0;
+      c->kbytes = 0.0;
       c->kev_pairs = 0;
       L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, kt ? c->kev.data() : nullptr,
-                            kt ? &c->kev_pairs : nullptr, kt ? &c->kflop : nullptr);
+                            kt ? &c->kev_pairs : nullptr, kt ? &c->kflop : nullptr,
+                            kt ? &c->kbytes : nullptr);
     }
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
   }
@@ -685,6 +688,12 @@ extern "C" int bd_phase_times(bd_ctx* c, float* out9) {
   CK(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < 8; k++) cudaEventElapsedTime(&out9[k], c->ev[k], c->ev[k + 1]);
   cudaEventElapsedTime(&out9[8], c->ev[0], c->ev[8]);
+  return BD_OK;
+}
+
+extern "C" int bd_kernel_bytes(bd_ctx* c, double* bytes) {
+  if (!c || !bytes) return set_error(BD_ERR_ARG, "bd_kernel_bytes: null argument");
+  *bytes = c->kbytes;
   return BD_OK;
 }
 

@@ -129,11 +129,13 @@ size_t trmv_scratch_doubles(int m);
 // k_tc_chol.cu (mixed precision: FP64 storage, FP32-class arithmetic, tcgen05 trailing updates)
 size_t mixed_panel_bytes(int m);
 int set_mixed_attributes();
-// kev (optional): 2 events per panel, recorded around each launch that
-// carries the bulk trailing update (the dominant kernel); *kev_pairs = how
-// many were recorded, *kflop accumulates the tensor work those launches issue.
+// kev (optional): 2 events per launch that carries a bulk trailing update
+// (the dominant kernel); *kev_pairs = how many were recorded, *kflop and
+// *kbytes accumulate the tensor work those launches issue and their
+// algorithmic HBM bytes.
 int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
-                cudaEvent_t* kev = nullptr, int* kev_pairs = nullptr, double* kflop = nullptr);
+                cudaEvent_t* kev = nullptr, int* kev_pairs = nullptr, double* kflop = nullptr,
+                double* kbytes = nullptr);
 int mixed_tiles(int m);
 
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,

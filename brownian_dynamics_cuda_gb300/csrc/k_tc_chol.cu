@@ -331,9 +331,14 @@ __device__ __forceinline__ void rest_tile(int t, int jlo, int col_only, int& I, 
 }
 
 // `cta` is the CTA's index among the update CTAs.
+// NPAN = 1: one panel's update, the A operand resident per row of tiles.
+// NPAN = 2: two consecutive panels' updates (PS, PS2) in one read-modify-write
+// of the tile (K = 256): both operands streamed in four 96 KB chunks per
+// tile (panel, K-half) through the two stages.
+template <int NPAN>
 __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int lda, int m, int jlo, int col_only,
                                           int ntiles, int group, int cta, const unsigned char* __restrict__ PS,
-                                          int* err) {
+                                          const unsigned char* __restrict__ PS2, int* err) {
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   unsigned char* sA = sm;                 // 3 slices x 32 KB
   unsigned char* sB = sm + kTileBytes;    // 2 stages x (3 slices x 16 KB)
@@ -364,6 +369,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
   if (warp == 0) {
     if (lane == 0) {
       // ---------------- producer
+      if constexpr (NPAN == 1) {
       int curI = -1;
       uint32_t nA = 0, nfill[2] = {0, 0};
       bool ok = true;
@@ -412,10 +418,50 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
       for (int h = 0; h < 2; h++)
         if (nfill[h] > 0) (void)sm100::mbar_wait(&bars->fullB[h], (nfill[h] - 1) & 1, kWaitLimit);
       if (nA > 0) (void)sm100::mbar_wait(&bars->fullA, (nA - 1) & 1, kWaitLimit);
+      } else {
+        // two panels: chunk q = (panel q >> 1, K-half q & 1) of both operands
+        uint32_t nfill[2] = {0, 0};
+        int ctot = 0;
+        bool ok = true;
+        for (int t = t0; t < t1 && ok; t++) {
+          int I, J;
+          rest_tile(t, jlo, col_only, I, J);
+          const bool dg = I == J;
+          for (int q = 0; q < 4; q++) {
+            const int st = ctot & 1;
+            if (nfill[st] > 0) ok = sm100::mbar_wait(&bars->emptyB[st], (nfill[st] - 1) & 1, kWaitLimit);
+            if (!ok || *abort_flag) {
+              ok = false;
+              break;
+            }
+            const unsigned char* src = (q >> 1) ? PS2 : PS;
+            const int h = q & 1;
+            unsigned char* sa = sm + st * (2 * kStageBytes);
+            sm100::mbar_arrive_expect_tx(&bars->fullB[st], dg ? kStageBytes : 2 * kStageBytes);
+            for (int s2 = 0; s2 < kTileSlices; s2++)
+              sm100::bulk_g2s(sa + s2 * kHalfBytes, src + (size_t)I * kTileBytes + s2 * kSliceBytes + h * kHalfBytes,
+                              kHalfBytes, &bars->fullB[st]);
+            if (!dg)
+              for (int s2 = 0; s2 < kTileSlices; s2++)
+                sm100::bulk_g2s(sa + kStageBytes + s2 * kHalfBytes,
+                                src + (size_t)J * kTileBytes + s2 * kSliceBytes + h * kHalfBytes, kHalfBytes,
+                                &bars->fullB[st]);
+            nfill[st]++;
+            ctot++;
+          }
+        }
+        if (!ok) {
+          atomicExch(err, 3);
+          *abort_flag = 1;
+        }
+        for (int h = 0; h < 2; h++)
+          if (nfill[h] > 0) (void)sm100::mbar_wait(&bars->fullB[h], (nfill[h] - 1) & 1, kWaitLimit);
+      }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer
+      if constexpr (NPAN == 1) {
       const uint32_t idesc = sm100::idesc_bf16_f32(128, 128);
       const int pa[6] = {2, 1, 0, 1, 0, 0};  // (A slice, B slice) products, smallest first
       const int pb[6] = {0, 1, 2, 0, 1, 0};
@@ -465,6 +511,54 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
       if (!ok) {
         atomicExch(err, 4);
         *abort_flag = 1;
+      }
+      } else {
+        const uint32_t idesc = sm100::idesc_bf16_f32(128, 128);
+        const int pa[6] = {2, 1, 0, 1, 0, 0};
+        const int pb[6] = {0, 1, 2, 0, 1, 0};
+        uint32_t nuse[2] = {0, 0};
+        int ctot = 0;
+        bool ok = true;
+        int n = 0;
+        for (int t = t0; t < t1; t++, n++) {
+          int I, J;
+          rest_tile(t, jlo, col_only, I, J);
+          if (*abort_flag) break;
+          const bool dg = I == J;
+          const int acc = n & 1;
+          if (n >= 2) {
+            ok = sm100::mbar_wait(&bars->accEmpty[acc], ((n >> 1) - 1) & 1, kWaitLimit);
+            if (!ok) break;
+          }
+          sm100::tc_fence_after();
+          const uint32_t d = tmem + (uint32_t)(acc * kAccCols);
+          for (int q = 0; q < 4 && ok; q++) {
+            const int st = ctot & 1;
+            ok = sm100::mbar_wait(&bars->fullB[st], nuse[st] & 1, kWaitLimit);
+            if (!ok) break;
+            sm100::tc_fence_after();
+            const unsigned char* sa = sm + st * (2 * kStageBytes);
+            const unsigned char* sb = dg ? sa : sa + kStageBytes;
+#pragma unroll
+            for (int p = 0; p < 6; p++) {
+              const uint32_t aaddr = sm100::smem_u32(sa + pa[p] * kHalfBytes);
+              const uint32_t baddr = sm100::smem_u32(sb + pb[p] * kHalfBytes);
+#pragma unroll
+              for (int kk = 0; kk < 4; kk++)
+                sm100::mma_bf16(d, sm100::desc_kmajor_sw128(aaddr + kk * 32),
+                                sm100::desc_kmajor_sw128(baddr + kk * 32), idesc, (q | p | kk) != 0);
+            }
+            sm100::mma_commit(&bars->emptyB[st]);
+            nuse[st]++;
+            ctot++;
+          }
+          if (!ok) break;
+          sm100::mma_commit(&bars->accFull[acc]);
+        }
+        if (!ok) {
+          atomicExch(err, 4);
+          *abort_flag = 1;
+        }
       }
       // every MMA issued has finished before TMEM is freed
       sm100::mma_commit(&bars->done);
@@ -527,14 +621,19 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
 __global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(float2* A, float* Ldg, int lda, int m, int ndp, int pk0, int pkb,
                                                               unsigned char* PSp, int* negpiv, int jlo, int col_only,
                                                               int ntiles, int group,
-                                                              const unsigned char* __restrict__ PSu, int* err) {
+                                                              const unsigned char* __restrict__ PSu,
+                                                              const unsigned char* __restrict__ PSu2, int* err) {
   extern __shared__ float4 smem4[];
   if ((int)blockIdx.x < ndp) {
     dpanel_body(smem4, A, Ldg, lda, m, pk0, pkb, pk0 / kT + 1, (int)blockIdx.x, PSp, negpiv);
     return;
   }
-  rest_body(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group, (int)blockIdx.x - ndp,
-            PSu, err);
+  if (PSu2)
+    rest_body<2>(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group,
+                 (int)blockIdx.x - ndp, PSu, PSu2, err);
+  else
+    rest_body<1>(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group,
+                 (int)blockIdx.x - ndp, PSu, nullptr, err);
 }
 
 // After the last panel: the diagonal factors L_kk from the side buffer into
@@ -554,8 +653,8 @@ namespace bdk {
 
 // two panel-slice buffers: panel k writes buffer k & 1 while the updates of
 // panel k - 1 still read the other
-size_t mixed_panel_bytes(int m) {  // two slice buffers, then the diagonal factors
-  return 2 * (size_t)cdiv(m, kT) * kTileBytes + (size_t)cdiv(m, kT) * kT * kT * sizeof(float);
+size_t mixed_panel_bytes(int m) {  // three slice buffers, then the diagonal factors
+  return 3 * (size_t)cdiv(m, kT) * kTileBytes + (size_t)cdiv(m, kT) * kT * kT * sizeof(float);
 }
 int mixed_tiles(int m) { return cdiv(m, kT); }
 
@@ -585,44 +684,77 @@ static int rest_group(int tiles) {
   return g < 1 ? 1 : (g > 8 ? 8 : g);
 }
 
-// Right-looking with a lookahead of one panel, on one stream.  Step k:
-//   launch 1: panel k's update of column k+1 (the next panel's tiles);
-//   launch 2: panel k+1 (extra CTAs) together with panel k's update of the
-//             tiles right of column k+1.
-// Panel k+1 needs only column k+1, so it is factored inside the launch that
-// carries the bulk of panel k's update; the two parts write disjoint
-// columns, and panel k+1's slices go to the other buffer.  No two kernels
-// run at the same time.  Returns the number of kernel launches.
+// Right-looking with a lookahead of one panel, on one stream, no two kernels
+// at a time.  Panel p's slices live in buffer p % 3; L_kk in a side buffer.
+// Single step k (invariant: panel k factored, columns > k hold the updates
+// of panels < k):
+//   launch 1: panel k's update of column k+1;
+//   launch 2: panel k+1 (extra CTAs) + panel k's update of the tiles right
+//             of column k+1.
+// Pair (k, k+1), used while the trailing matrix is large: the bulk tiles
+// get both panels in one read-modify-write (K = 256), half the HBM traffic:
+//   launch 1: panel k's update of column k+1;
+//   launch 2: panel k+1 + panel k's update of column k+2;
+//   launch 3: panel k+1's update of column k+2;
+//   launch 4: panel k+2 + panels k and k+1 on the tiles right of column k+2.
+// Returns the number of kernel launches.
+#ifndef BD_PAIR_MIN
+#define BD_PAIR_MIN 24  // pair while at least this many tile rows remain right of column k+2
+#endif
 int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
-                cudaEvent_t* kev, int* kev_pairs, double* kflop) {
+                cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes) {
   float2* A = reinterpret_cast<float2*>(A64);  // double-float storage, 8 bytes per element
   const int nt = cdiv(m, kT);
   const size_t buf = (size_t)nt * kTileBytes;
   int L = 0, pairs = 0;
   auto kb_of = [&](int k) { return (m - k * kT < kT) ? m - k * kT : kT; };
-  // panel 0 alone
-  float* Ld = reinterpret_cast<float*>(PS + 2 * buf);  // [nt][128 x 128] diagonal factors
-  k_chol_step<<<nt, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, nt, 0, kb_of(0), PS, negpiv, 0, 0, 0, 1, PS, err);
-  L++;
-  for (int k = 0; k + 1 < nt; k++) {
+  auto psb = [&](int k) { return PS + (size_t)(k % 3) * buf; };
+  float* Ld = reinterpret_cast<float*>(PS + 3 * buf);  // [nt][128 x 128] diagonal factors
+  auto col = [&](int k) {  // panel k's update of column k+1
     const int below = nt - k - 1;
-    const unsigned char* psk = PS + (size_t)(k & 1) * buf;
-    unsigned char* psn = PS + (size_t)((k + 1) & 1) * buf;
-    k_chol_step<<<below, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, 0, 0, 0, psn, negpiv, k + 1, 1, below, 1, psk,
-                                                         err);
+    k_chol_step<<<below, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, 0, 0, 0, nullptr, negpiv, k + 1, 1, below, 1,
+                                                         psb(k), nullptr, err);
     L++;
-    const int rest = below - 1;
-    const int tiles = rest * (rest + 1) / 2;
-    const int group = tiles > 0 ? rest_group(tiles) : 1;
-    const int ndp = nt - k - 1;  // panel k+1: its diagonal block and the tiles below it
-    if (kev) cudaEventRecord(kev[2 * pairs], st);
+  };
+  // panel pn in extra CTAs + an update of the tiles from column jlo by panel
+  // pu (and pu + 1 when two), triangle or (col_only) one column
+  auto step = [&](int pn, int jlo, int pu, bool two, bool col_only, bool timed) {
+    const int ndp = nt - pn;
+    const int rows = nt - jlo;
+    const int tiles = rows <= 0 ? 0 : (col_only ? rows : rows * (rows + 1) / 2);
+    const int group = (tiles > 0 && !col_only) ? rest_group(tiles) : 1;
+    if (timed && kev) cudaEventRecord(kev[2 * pairs], st);
     k_chol_step<<<ndp + cdiv(tiles, group), kRestThreads, kRestSmem, st>>>(
-        A, Ld + (size_t)(k + 1) * kT * kT, lda, m, ndp, (k + 1) * kT, kb_of(k + 1), psn, negpiv, k + 2, 0, tiles,
-        group, psk, err);
-    if (kev) cudaEventRecord(kev[2 * pairs + 1], st);
-    pairs++;
-    if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles;  // BF16 tensor work issued
+        A, Ld + (size_t)pn * kT * kT, lda, m, ndp, pn * kT, kb_of(pn), (unsigned char*)psb(pn), negpiv, jlo,
+        col_only ? 1 : 0, tiles, group, psb(pu), two ? psb(pu + 1) : nullptr, err);
+    if (timed && kev) {
+      cudaEventRecord(kev[2 * pairs + 1], st);
+      pairs++;
+    }
+    if (timed) {
+      const double n2 = (double)(m - jlo * kT);
+      if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles * (two ? 2 : 1);  // BF16 tensor work issued
+      if (kbytes && n2 > 0) *kbytes += 16.0 * n2 * (n2 + 1) / 2;           // double-float read + write
+    }
     L++;
+  };
+  // panel 0 alone
+  k_chol_step<<<nt, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, nt, 0, kb_of(0), PS, negpiv, 0, 0, 0, 1, PS,
+                                                   nullptr, err);
+  L++;
+  int k = 0;
+  while (k + 1 < nt) {
+    if (nt - (k + 3) >= BD_PAIR_MIN) {
+      col(k);
+      step(k + 1, k + 2, k, false, true, false);
+      col(k + 1);
+      step(k + 2, k + 3, k, true, false, true);
+      k += 2;
+    } else {
+      col(k);
+      step(k + 1, k + 2, k, false, false, true);
+      k += 1;
+    }
   }
   k_diag_scatter<<<nt, 256, 0, st>>>(A, lda, m, Ld);
   L++;

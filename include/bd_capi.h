@@ -240,6 +240,9 @@ int bd_kernel_time(bd_ctx* ctx, float* total_ms, int* launches, double* tensor_f
 /* The same launches one by one: out_ms[i] for i < min(max, launches), in
  * panel order; *launches = their number. */
 int bd_kernel_times(bd_ctx* ctx, float* out_ms, int max, int* launches);
+/* Algorithmic HBM bytes of those launches: 16 B (double-float read + write)
+ * per element of every trailing triangle they update. */
+int bd_kernel_bytes(bd_ctx* ctx, double* bytes);
 /* Count of kernel launches issued by the last bd_step (graph nodes count once each). */
 int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
