@@ -328,7 +328,7 @@ def run_ours(args):
                 "traffic": byt * NCU_TRAFFIC_PER_ALG_BYTE,
                 "traffic_source": "DRAM read+write per algorithmic byte of one ncu capture "
                                   "(profiles/k_chol_step_cfg1_mixed.md), times this step's algorithmic bytes",
-                "kernel": "k_chol_step (bulk tcgen05 trailing update, next panel in extra CTAs, FP64 tile "
+                "kernel": "k_chol_step (bulk tcgen05 trailing update of one or two panels, next panel in extra CTAs, double-float tile "
                           "read-modify-write), %d launches/step, avg %.3f ms" % (nk, ms_k / max(nk, 1)),
                 "algorithmic_bytes_per_step": byt,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
