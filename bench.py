@@ -120,21 +120,6 @@ def fp64_peak_tflops() -> float:
     return 2.0 * n ** 3 / best / 1e12
 
 
-def rest_update_bytes(m: int, nb: int = 128) -> float:
-    """Algorithmic HBM bytes of the bulk trailing updates of one mixed
-    factorisation: every FP64 element of the lower triangle right of column
-    block k+1 is read and written once per panel k (16 B)."""
-    nt = -(-m // nb)
-    rows = np.array([min(nb, m - nb * i) for i in range(nt)], dtype=np.float64)
-    tot = 0.0
-    for k in range(nt - 2):
-        r = rows[k + 2:]
-        full = (r.sum() ** 2 - (r ** 2).sum()) / 2.0      # off-diagonal tiles I > J
-        tri = (r * (r + 1) / 2).sum()                      # diagonal tiles, lower part
-        tot += 16.0 * (full + tri)
-    return tot
-
-
 def fp64_comparison(fib, rr_d, p_d, host, args, local, stream) -> dict:
     """Plain FP64 step (CUDA graph, same fiber, same noise) timed like the
     headline, and the relative displacement error of one mixed step against
