@@ -4,28 +4,30 @@
 // stored as double-float pairs (hi, lo) of FP32 (column-major, 8 bytes per
 // element, ~48 significant bits), so the trailing updates accumulate without
 // an FP32 rounding per panel and without FP64 arithmetic (GB300's FP64 rate
-// is ~2 operations per clock per SM); the arithmetic is FP32-class:
-//   k_dpanel    one launch per panel: every CTA factors the 128 x 128
-//               diagonal block in shared memory (FP32, 32-column blocks,
-//               left-looking across blocks), CTA 0 keeps it in a side buffer
-//               (copied into A after the last panel) and the
-//               others solve one 128-row tile each, L_ik = A_ik L_kk^-T, by
-//               forward substitution, write it back and split it into three
-//               BF16 slices (hi + mid + lo = the FP32 value exactly), stored
-//               pre-swizzled in the 128-byte-swizzle K-major layout the MMA
-//               reads; a negative pivot is replaced by its absolute value and
-//               counted (func.cpp:827-833).
-//   k_tc_rest   trailing update A_IJ -= L_I L_J^T, a run of tiles per CTA,
-//               warp-specialised: bulk-async operand copies, six BF16
-//               products (hi.hi, hi.mid, mid.hi, hi.lo, mid.mid, lo.hi) into
-//               one of two FP32 tensor-memory accumulators (tcgen05.mma,
-//               M = N = 128, K = 16 per instruction), tcgen05.ld epilogue
-//               subtracting into the double-float tile.  The dropped products are below 2^-24 of
-//               the kept ones: FP32-class products.
-// A one-panel lookahead runs the next panel on a second stream while the
-// bulk update of the current one runs.  Every mbarrier wait is bounded; on
-// a timeout the kernel records an error code, frees its tensor memory and
-// returns.
+// is ~2 operations per clock per SM); the arithmetic is FP32-class.  One
+// kernel, k_chol_step, runs two kinds of CTA side by side:
+//   panel CTAs   factor the next panel: every one factors the 128 x 128
+//                diagonal block in shared memory (FP32, 32-column blocks),
+//                CTA 0 keeps it in a side buffer (copied into A after the
+//                last panel) and the others solve one 128-row tile each,
+//                L_ik = A_ik L_kk^-T, by forward substitution, write it back
+//                and split it into three BF16 slices (hi + mid + lo = the
+//                FP32 value exactly), stored pre-swizzled in the
+//                128-byte-swizzle K-major layout the MMA reads; a negative
+//                pivot is replaced by its absolute value and counted
+//                (func.cpp:827-833).
+//   update CTAs  trailing update A_IJ -= L_I L_J^T of one or two earlier
+//                panels, a run of tiles per CTA, warp-specialised:
+//                bulk-async operand copies, six BF16 products (hi.hi,
+//                hi.mid, mid.hi, hi.lo, mid.mid, lo.hi) per panel into one of
+//                two FP32 tensor-memory accumulators (tcgen05.mma,
+//                M = N = 128, K = 16 per instruction), tcgen05.ld epilogue
+//                subtracting into the double-float tile.  The dropped
+//                products are below 2^-24 of the kept ones: FP32-class
+//                products.
+// The launches run on one stream, one at a time (the schedule is at
+// potrf_mixed).  Every mbarrier wait is bounded; on a timeout the kernel
+// records an error code, frees its tensor memory and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -67,95 +69,160 @@ __device__ __forceinline__ float2 df_sub(float2 a, float v) {
 }
 
 // ------------------------------------------------------------ diagonal block + panel
-// One launch per panel k.  Every CTA loads the 128 x 128 diagonal block and
-// factors it in shared memory (the factor is recomputed by each CTA instead
-// of being passed between launches); CTA 0 writes L_kk back, CTA b >= 1
-// solves the 128-row tile k + b:  X L_kk^T = A_ik.
+// Panel k runs in CTAs of the step launch: every panel CTA loads the
+// 128 x 128 diagonal block and factors it in shared memory (the factor is
+// recomputed by each CTA instead of being passed between CTAs); CTA 0 keeps
+// L_kk, CTA b >= 1 also solves the 128-row tile k + b:  X L_kk^T = A_ik.
 //
-// Both factorisations work on 32-column blocks, left-looking across blocks:
-// block column j first takes  S[r][c] -= sum_{q < 32 j} S[r][q] L[c][q]  as
-// one FP32 dot product per element (register-tiled 4 x 4 per thread), then
-// the 32 x 32 diagonal block is factored by one warp in registers and the
-// rows below it are solved by forward substitution, one row per thread.
-// A negative pivot is replaced by its absolute value and counted
-// (func.cpp:827-833), by CTA 0 only.
+// The diagonal block and the tile are one tall 256-row panel in shared memory
+// (rows 0..127 the diagonal block, 128..255 the tile), factored in 32-column
+// blocks, left-looking across blocks: block column j first takes
+//   S[r][c] -= sum_{q < 32 j} S[r][q] L[c][q]
+// as one FP32 dot product per element (register-tiled, 7 rows x 4 columns per
+// thread), then the 32 x 32 diagonal block is factored by one warp in
+// registers and every row below it (diagonal-block rows and tile rows alike)
+// is solved by forward substitution, one row per thread.  A negative pivot is
+// replaced by its absolute value and counted (func.cpp:827-833), by CTA 0 only.
 constexpr int kLd = 132;             // shared row stride (floats): 16-byte rows, conflict-free 4-wide loads
+constexpr int kLt = 36;              // row stride of the transposed 32 x 32 factor
 constexpr int kDpThreads = 256;
-constexpr size_t kDpSmem = (2 * (size_t)kT * kLd + kT) * sizeof(float);
+constexpr size_t kDpSmem = (2 * (size_t)kT * kLd + 32 * kLt) * sizeof(float);
 
-// Out[r][c] -= sum_{q < c0} In[r][q] * Lf[c][q] for r in [r0, r1), c in
-// [c0, c0 + 32) (c < cend); lower-only (r >= c) when `lower`.
-__device__ __forceinline__ void dp_block_update(float (*S)[kLd], const float (*Lf)[kLd], int r0, int r1, int c0,
-                                                int cend, bool lower) {
-  const int t = threadIdx.x;
+#ifndef DP_MARK
+#define DP_MARK(i)  // phase boundary of the panel CTAs (a timestamp hook for profiling builds)
+#endif
+
+// Row v of the block-column update: v < nd are diagonal-block rows c0 + v,
+// the rest tile rows kT + (v - nd); -1 past the end.
+__device__ __forceinline__ int dp_row(int v, int c0, int nd, int nv) {
+  return v < nd ? c0 + v : (v < nv ? kT + v - nd : -1);
+}
+
+// S[r][c] -= sum_{qlo <= q < qhi} S[r][q] * S[c][q] for the nv rows of block
+// column c0 (c in [c0, c0 + w)), lower part only inside the diagonal block;
+// t in [0, 256) is the thread's index among the 256 taking part.  NI row
+// groups of 32 (nv <= 32 NI); the operands of step q + 4 are loaded while
+// step q's products are formed, and the products are issued component by
+// component so that consecutive FMAs are independent.
+template <int NI>
+__device__ __forceinline__ void dp_block_update_n(float (*S)[kLd], int t, int c0, int w, int nd, int nv, int qlo,
+                                                  int qhi) {
   const int g = t & 7, rg = t >> 3;  // 8 column groups x 32 row groups
-  float acc[4][4];
+  int rows[NI];
+  const float* xr[NI];
+  const float* lr[4];
+  float acc[NI][4];
 #pragma unroll
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < NI; i++) {
+    rows[i] = dp_row(rg + 32 * i, c0, nd, nv);
+    xr[i] = S[rows[i] < 0 ? 0 : rows[i]];  // rows past the end read row 0; their sums are dropped
 #pragma unroll
     for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
-  for (int q = 0; q < c0; q += 4) {
-    float4 xv[4], lv[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const int r = r0 + rg + 32 * i;
-      xv[i] = (r < r1) ? *reinterpret_cast<const float4*>(&S[r][q]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++) lv[j] = *reinterpret_cast<const float4*>(&Lf[c0 + g + 8 * j][q]);
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        acc[i][j] = fmaf(xv[i].x, lv[j].x, acc[i][j]);
-        acc[i][j] = fmaf(xv[i].y, lv[j].y, acc[i][j]);
-        acc[i][j] = fmaf(xv[i].z, lv[j].z, acc[i][j]);
-        acc[i][j] = fmaf(xv[i].w, lv[j].w, acc[i][j]);
-      }
   }
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int r = r0 + rg + 32 * i;
+  for (int j = 0; j < 4; j++) lr[j] = S[c0 + g + 8 * j];
+  float4 lv[4], xv[NI];
+#pragma unroll
+  for (int j = 0; j < 4; j++) lv[j] = *reinterpret_cast<const float4*>(lr[j] + qlo);
+#pragma unroll
+  for (int i = 0; i < NI; i++) xv[i] = *reinterpret_cast<const float4*>(xr[i] + qlo);
+#pragma unroll 1
+  for (int q = qlo; q < qhi; q += 4) {
+    const int qn = (q + 4 < qhi) ? q + 4 : q;
+    float4 ln[4], xn[NI];
+#pragma unroll
+    for (int j = 0; j < 4; j++) ln[j] = *reinterpret_cast<const float4*>(lr[j] + qn);
+#pragma unroll
+    for (int i = 0; i < NI; i++) xn[i] = *reinterpret_cast<const float4*>(xr[i] + qn);
+#pragma unroll
+    for (int i = 0; i < NI; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = fmaf(xv[i].x, lv[j].x, acc[i][j]);
+#pragma unroll
+    for (int i = 0; i < NI; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = fmaf(xv[i].y, lv[j].y, acc[i][j]);
+#pragma unroll
+    for (int i = 0; i < NI; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = fmaf(xv[i].z, lv[j].z, acc[i][j]);
+#pragma unroll
+    for (int i = 0; i < NI; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = fmaf(xv[i].w, lv[j].w, acc[i][j]);
+#pragma unroll
+    for (int j = 0; j < 4; j++) lv[j] = ln[j];
+#pragma unroll
+    for (int i = 0; i < NI; i++) xv[i] = xn[i];
+  }
+#pragma unroll
+  for (int i = 0; i < NI; i++) {
+    const int r = rows[i];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       const int c = c0 + g + 8 * j;
-      if (r < r1 && c < cend && (!lower || r >= c)) S[r][c] -= acc[i][j];
+      if (r >= 0 && c < c0 + w && (r >= kT || r >= c)) S[r][c] -= acc[i][j];
     }
   }
 }
 
-// Forward substitution of one row against the 32 x 32 block of Lf at (c0, c0):
-// x[c] = (b[c] - sum_{q < c} x[q] L[c0+c][c0+q]) / L[c0+c][c0+c], right-looking in registers.
-__device__ __forceinline__ void dp_row_solve(float* row, const float (*Lf)[kLd], const float* invd, int c0, int w) {
-  float x[32];
-#pragma unroll
-  for (int j = 0; j < 32; j++) x[j] = (j < w) ? row[j] : 0.f;
-#pragma unroll
-  for (int c = 0; c < 32; c++) {
-    x[c] *= invd[c0 + c];
-#pragma unroll
-    for (int j = c + 1; j < 32; j++) x[j] = fmaf(-x[c], Lf[c0 + j][c0 + c], x[j]);
+// up to 96 diagonal-block rows + 128 tile rows: at most 7 row groups
+__device__ __forceinline__ void dp_block_update(float (*S)[kLd], int t, int c0, int w, int nd, int nv, int qlo,
+                                                int qhi) {
+  switch ((nv + 31) >> 5) {
+    case 1: dp_block_update_n<1>(S, t, c0, w, nd, nv, qlo, qhi); break;
+    case 2: dp_block_update_n<2>(S, t, c0, w, nd, nv, qlo, qhi); break;
+    case 3: dp_block_update_n<3>(S, t, c0, w, nd, nv, qlo, qhi); break;
+    case 4: dp_block_update_n<4>(S, t, c0, w, nd, nv, qlo, qhi); break;
+    case 5: dp_block_update_n<5>(S, t, c0, w, nd, nv, qlo, qhi); break;
+    case 6: dp_block_update_n<6>(S, t, c0, w, nd, nv, qlo, qhi); break;
+    default: dp_block_update_n<7>(S, t, c0, w, nd, nv, qlo, qhi); break;
   }
-#pragma unroll
-  for (int j = 0; j < 32; j++)
-    if (j < w) row[j] = x[j];
 }
 
-// Runs in a CTA of kRestThreads threads; threads >= kDpThreads only take
-// part in the barriers.  `b` is the CTA's index among the panel CTAs.
+// Forward substitution of one row (32 entries at `row`, 16-byte aligned)
+// against the factored 32 x 32 block, right-looking in registers:
+//   x[c] = (b[c] - sum_{q < c} x[q] L[c][q]) / L[c][c].
+// T is the block transposed, T[c][j] = L[j][c] (row stride kLt), with
+// 1 / L[c][c] on its diagonal, so column c of L is one contiguous row.
+__device__ __forceinline__ void dp_row_solve(float* row, const float* T, float (&x)[32]) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float4 v = reinterpret_cast<const float4*>(row)[k];
+    x[4 * k] = v.x, x[4 * k + 1] = v.y, x[4 * k + 2] = v.z, x[4 * k + 3] = v.w;
+  }
+#pragma unroll
+  for (int c = 0; c < 32; c++) {
+    float t[32];
+#pragma unroll
+    for (int k = c >> 2; k < 8; k++) {
+      const float4 v = reinterpret_cast<const float4*>(T + c * kLt)[k];
+      t[4 * k] = v.x, t[4 * k + 1] = v.y, t[4 * k + 2] = v.z, t[4 * k + 3] = v.w;
+    }
+    x[c] *= t[c];
+#pragma unroll
+    for (int j = c + 1; j < 32; j++) x[j] = fmaf(-x[c], t[j], x[j]);
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    reinterpret_cast<float4*>(row)[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+}
+
 // Cholesky of a 32 x 32 block held by one warp, lane i holding row i (a[j],
-// j <= i), right-looking in registers: pivot from lane c, 1/sqrt once
-// (rsqrt), column c scaled, rank-1 update of the columns to its right with
-// L[j][c] shuffled from lane j.  FULL (w == 32) is branch-free, so the
-// compiler can start column c+1's pivot while column c's update is in
-// flight.  Lane c keeps 1/L[c][c] in invv and flags a negative pivot
-// (replaced by its absolute value, func.cpp:827-833).
+// j <= i), right-looking in registers: 1/sqrt of the pivot once (rsqrt),
+// column c scaled, rank-1 update of the columns to its right with L[j][c]
+// shuffled from lane j.  The next pivot, A[c+1][c+1] - L[c+1][c]^2, is
+// formed by lane c + 1 from its own entries and broadcast at once, so the
+// pivot chain carries one shuffle per column; its value is the one the
+// rank-1 update leaves in lane c + 1.  FULL (w == 32) is branch-free.  Lane
+// c keeps 1/L[c][c] in invv and flags a negative pivot (replaced by its
+// absolute value, func.cpp:827-833).
 template <bool FULL>
 __device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, float& invv, int& neg) {
+  float d = __shfl_sync(0xffffffffu, a[0], 0);
 #pragma unroll
   for (int c = 0; c < 32; c++) {
     if (!FULL && c >= w) break;
-    const float d = __shfl_sync(0xffffffffu, a[c], c);
     const float ad = fabsf(d);
     const float inv = rsqrtf(ad);
     if (lane == c) {
@@ -163,126 +230,154 @@ __device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, flo
       neg = d < 0.f;
     }
     a[c] = (lane == c) ? ad * inv : ((lane > c) ? a[c] * inv : a[c]);
+    if (c + 1 < 32) d = __shfl_sync(0xffffffffu, fmaf(-a[c], a[c], a[c + 1]), c + 1);
 #pragma unroll
     for (int j = c + 1; j < 32; j++) a[j] = fmaf(-a[c], __shfl_sync(0xffffffffu, a[c], j), a[j]);
   }
 }
 
+// Row r of L_ik, columns c0 .. c0 + 31 (x[j] = 0 past column w): (L, 0)
+// pairs into A (`g` = A at column c0 of the tile's row 0) for rows inside the
+// matrix, and the 16-byte chunks of the three BF16 slices (x = hi + mid + lo
+// exactly, 8 + 8 + 8 significant bits) for every row of the tile.
+__device__ __forceinline__ void dp_emit(const float (&x)[32], int r, int nrows, int c0, int w, float2* g, int lda,
+                                        unsigned char* ps) {
+  if (r < nrows) {
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+      if (j < w) g[(size_t)j * lda + r] = make_float2(x[j], 0.f);
+  }
+#pragma unroll
+  for (int q8 = 0; q8 < 4; q8++) {
+    uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+    for (int j2 = 0; j2 < 4; j2++) {
+      uint32_t h2 = 0u, m2 = 0u, l2 = 0u;
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const float v = x[8 * q8 + 2 * j2 + e];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const float r1 = v - __bfloat162float(h);
+        const __nv_bfloat16 md = __float2bfloat16_rn(r1);
+        const float r2 = r1 - __bfloat162float(md);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+        h2 |= (uint32_t)__bfloat16_as_ushort(h) << (16 * e);
+        m2 |= (uint32_t)__bfloat16_as_ushort(md) << (16 * e);
+        l2 |= (uint32_t)__bfloat16_as_ushort(lo) << (16 * e);
+      }
+      hw[j2] = h2, mw[j2] = m2, lw[j2] = l2;
+    }
+    const uint32_t off = swz_off(r, c0 + 8 * q8);
+    *reinterpret_cast<uint4*>(ps + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(ps + kSliceBytes + off) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+    *reinterpret_cast<uint4*>(ps + 2 * kSliceBytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
+// Runs in a CTA of kRestThreads (320) threads: 256 load, update and solve;
+// while warp 0 factors a diagonal block, warps 2..9 update the next block
+// column.  `b` is the CTA's index among the panel CTAs.
 __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, int lda, int m, int k0, int kb, int tile0,
                                             int b, unsigned char* PS, int* negpiv) {
-  float (*Ls)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);
-  float (*X)[kLd] = reinterpret_cast<float (*)[kLd]>(reinterpret_cast<float*>(sm4) + kT * kLd);
-  float* invd = reinterpret_cast<float*>(sm4) + 2 * kT * kLd;
+  float (*S)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);  // rows 0..127 diagonal block, 128..255 tile
+  float* T = reinterpret_cast<float*>(sm4) + 2 * kT * kLd;  // the current 32 x 32 factor, transposed
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool work = tid < kDpThreads;
   const bool is_diag = b == 0;
   const int tile = tile0 + b - 1;
   const int row0 = tile * kT;
   const int nrows = is_diag ? 0 : min(kT, m - row0);
+  DP_MARK(0);
   if (work) {
-    // column-major walk (a warp reads 32 consecutive rows of one column),
-    // 16 columns per batch so that 32 loads per thread are in flight
-    const int r = tid & (kT - 1), cq = tid >> 7;
-    const float2* ga = A + (size_t)k0 * lda + k0 + r;
-    const float2* gx = A + (size_t)k0 * lda + row0 + r;
+    // two rows per 16-byte load; lane l takes rows 2 (l & 3) + {0, 1} of an
+    // 8-row block and column l >> 2 of an 8-column block, so a warp reads
+    // 64-byte runs of 8 columns and its shared stores hit 32 distinct banks.
+    // Row pairs start even and lda is a multiple of 32: every load is
+    // aligned and stays inside its column.  16 blocks per batch, so that 32
+    // loads per thread are in flight.
+    const int rr = 2 * (lane & 3), cc = lane >> 2;
+    const float4* ga = reinterpret_cast<const float4*>(A + (size_t)k0 * lda + k0);
+    const float4* gx = reinterpret_cast<const float4*>(A + (size_t)k0 * lda + row0);
+    const size_t ld4 = (size_t)lda / 2;
 #pragma unroll 1
-    for (int i0 = 0; i0 < kT / 2; i0 += 16) {
-      float2 va[16], vx[16];
+    for (int cb = warp; cb < kT / 8; cb += kDpThreads / 32) {
+      const int c = 8 * cb + cc;
+      float4 va[16], vx[16];
 #pragma unroll
       for (int i = 0; i < 16; i++) {
-        const int c = cq + 2 * (i0 + i);
-        va[i] = (r >= c && r < kb && c < kb) ? ga[(size_t)c * lda] : make_float2(0.f, 0.f);
-        vx[i] = (!is_diag && r < nrows && c < kb) ? gx[(size_t)c * lda] : make_float2(0.f, 0.f);
+        const int r = 8 * i + rr;
+        va[i] = (r + 1 >= c && r < kb && c < kb) ? ga[c * ld4 + r / 2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        vx[i] = (r < nrows && c < kb) ? gx[c * ld4 + r / 2] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
       for (int i = 0; i < 16; i++) {
-        const int c = cq + 2 * (i0 + i);
-        Ls[r][c] = va[i].x + va[i].y;  // nearest FP32 of the stored double-float
-        X[r][c] = vx[i].x + vx[i].y;
+        const int r = 8 * i + rr;
+        // nearest FP32 of the stored double-float; entries past the block are zero
+        S[r][c] = (r < kb && c < kb) ? va[i].x + va[i].y : 0.f;
+        S[r + 1][c] = (r + 1 < kb && c < kb) ? va[i].z + va[i].w : 0.f;
+        S[kT + r][c] = (r < nrows) ? vx[i].x + vx[i].y : 0.f;
+        S[kT + r + 1][c] = (r + 1 < nrows) ? vx[i].z + vx[i].w : 0.f;
       }
     }
   }
-  if (tid < kT) invd[tid] = 0.f;
   __syncthreads();
+  DP_MARK(1);
   const int nb = (kb + 31) >> 5;
+  const int nrt = is_diag ? 0 : kT;  // tile rows solved (rows past the matrix are zero and stay zero)
   for (int jb = 0; jb < nb; jb++) {
     const int c0 = 32 * jb, w = min(32, kb - c0);
-    if (jb > 0) {
-      if (work) dp_block_update(Ls, Ls, c0, kb, c0, c0 + w, true);
-      __syncthreads();
-    }
+    const int c1 = c0 + 32, w1 = kb - c1;  // the next block column (w1 <= 0: none)
+    const int nd = max(0, w1);             // diagonal-block rows below this block
+    // A: warp 0 factors the 32 x 32 diagonal block; warps 2..9 meanwhile
+    // apply the finished block columns (q < c0) to the next block column
     if (warp == 0) {
       float a[32];
 #pragma unroll
-      for (int j = 0; j < 32; j++) a[j] = (lane < w && j <= lane) ? Ls[c0 + lane][c0 + j] : 0.f;
+      for (int j = 0; j < 32; j++) a[j] = (lane < w && j <= lane) ? S[c0 + lane][c0 + j] : 0.f;
       float invv = 0.f;
       int neg = 0;
       if (w == 32) warp_chol32<true>(a, 32, lane, invv, neg);
       else warp_chol32<false>(a, w, lane, invv, neg);
-      if (lane < w) invd[c0 + lane] = invv;
       if (is_diag && neg) atomicAdd(negpiv, 1);
 #pragma unroll
-      for (int j = 0; j < 32; j++)
-        if (lane < w && j <= lane) Ls[c0 + lane][c0 + j] = a[j];
+      for (int j = 0; j < 32; j++) {
+        if (lane < w && j <= lane) S[c0 + lane][c0 + j] = a[j];
+        T[j * kLt + lane] = (j < lane) ? a[j] : (j == lane ? invv : 0.f);
+      }
+    } else if (warp >= 2 && w1 > 0 && c0 > 0) {
+      dp_block_update(S, tid - 64, c1, min(32, w1), nd, nd + nrows, 0, c0);
     }
     __syncthreads();
-    const int rb = c0 + 32;
-    if (rb < kb && tid < kb - rb) dp_row_solve(&Ls[rb + tid][c0], Ls, invd, c0, w);
+    DP_MARK(2 + 3 * jb);
+    // B: the rows below the block, the rest of the diagonal block, then the
+    // 128 tile rows; a tile row's 32 new entries of L_ik go out at once:
+    // back into A as (L, 0) pairs and as three BF16 slices, pre-swizzled
+    // (consecutive lanes take consecutive rows, so the pair stores are
+    // coalesced)
+    if (tid < nd + nrt) {
+      float x[32];
+      dp_row_solve(&S[tid < nd ? c1 + tid : kT + tid - nd][c0], T, x);
+      if (tid >= nd) dp_emit(x, tid - nd, nrows, c0, w, A + (size_t)(k0 + c0) * lda + row0, lda,
+                             PS + (size_t)tile * kTileBytes);
+    }
     __syncthreads();
-  }
-  if (is_diag) {
-    // L_kk goes to a side buffer, not into A: panel CTAs of this launch that
-    // start after this one has finished (more CTAs than SMs) still read A_kk
-    if (work)
-      for (int e = tid; e < kT * kT; e += kDpThreads) {
-        const int c = e >> 7, r = e & (kT - 1);
-        Ldg[e] = (r >= c && r < kb && c < kb) ? Ls[r][c] : 0.f;  // column-major
-      }
-    return;
-  }
-  for (int jb = 0; jb < nb; jb++) {
-    const int c0 = 32 * jb, w = min(32, kb - c0);
-    if (jb > 0) {
-      if (work) dp_block_update(X, Ls, 0, nrows, c0, c0 + w, false);
+    DP_MARK(3 + 3 * jb);
+    // C: this block column's contribution to the next one
+    if (w1 > 0) {
+      if (work) dp_block_update(S, tid, c1, min(32, w1), nd, nd + nrows, c0, c1);
       __syncthreads();
     }
-    if (tid < nrows) dp_row_solve(&X[tid][c0], Ls, invd, c0, w);
-    __syncthreads();
+    DP_MARK(4 + 3 * jb);
   }
-  // write L_ik back (FP64) and its three BF16 slices, pre-swizzled: each
-  // thread takes one row and 8 consecutive columns, i.e. one 16-byte chunk
-  // of each slice (consecutive lanes: consecutive rows, coalesced FP64 stores)
-  unsigned char* ps = PS + (size_t)tile * kTileBytes;
-  float2* gout = A + (size_t)k0 * lda + row0;
-#pragma unroll 1
-  for (int e = tid; work && e < kT * (kT / 8); e += kDpThreads) {
-    const int r = e & (kT - 1), c0 = (e >> 7) * 8;
-    const float4 x0 = *reinterpret_cast<const float4*>(&X[r][c0]);
-    const float4 x1 = *reinterpret_cast<const float4*>(&X[r][c0 + 4]);
-    const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-    uint32_t hw[4], mw[4], lw[4];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const bool in = r < nrows && c0 + j < kb;
-      const float x = in ? xs[j] : 0.f;
-      if (in) gout[(size_t)(c0 + j) * lda + r] = make_float2(x, 0.f);
-      // x = hi + mid + lo exactly (8 + 8 + 8 significant bits)
-      const __nv_bfloat16 h = __float2bfloat16_rn(x);
-      const float r1 = x - __bfloat162float(h);
-      const __nv_bfloat16 md = __float2bfloat16_rn(r1);
-      const float r2 = r1 - __bfloat162float(md);
-      const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
-      const uint32_t sh = (j & 1) * 16;
-      if ((j & 1) == 0) hw[j >> 1] = mw[j >> 1] = lw[j >> 1] = 0u;
-      hw[j >> 1] |= (uint32_t)__bfloat16_as_ushort(h) << sh;
-      mw[j >> 1] |= (uint32_t)__bfloat16_as_ushort(md) << sh;
-      lw[j >> 1] |= (uint32_t)__bfloat16_as_ushort(lo) << sh;
+  if (is_diag && work) {
+    // L_kk goes to a side buffer, not into A: panel CTAs of this launch that
+    // start after this one has finished (more CTAs than SMs) still read A_kk
+    for (int e = tid; e < kT * kT; e += kDpThreads) {
+      const int c = e >> 7, r = e & (kT - 1);
+      Ldg[e] = (r >= c && r < kb && c < kb) ? S[r][c] : 0.f;  // column-major
     }
-    const uint32_t off = swz_off(r, c0);
-    *reinterpret_cast<uint4*>(ps + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-    *reinterpret_cast<uint4*>(ps + kSliceBytes + off) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
-    *reinterpret_cast<uint4*>(ps + 2 * kSliceBytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
+  DP_MARK(15);
 }
 
 // ------------------------------------------------------------ tensor-core trailing update
