@@ -92,7 +92,7 @@ struct bd_ctx {
   int host_negpiv = 0;
   cudaEvent_t ev[10] = {};
   bool timing = false;
-  std::vector<cudaEvent_t> kev;   // per-launch events around the tensor-core update (timing steps only)
+  std::vector<cudaEvent_t> kev;   // events around every k_chol_step launch (timing steps only)
   int kev_pairs = 0;
   double kflop = 0.0;
   double kbytes = 0.0;
@@ -426,7 +426,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   }
   for (int k = 0; k < 10; k++) cudaEventCreate(&c->ev[k]);
   if (c->precision == BD_PREC_MIXED) {
-    c->kev.resize(2 * (size_t)bdk::mixed_tiles(c->m));
+    c->kev.resize(2 * (size_t)bdk::mixed_max_launches(c->m));
     for (auto& ev : c->kev) cudaEventCreate(&ev);
   }
   e = cudaStreamSynchronize(st);

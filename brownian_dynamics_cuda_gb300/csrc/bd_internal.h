@@ -137,6 +137,7 @@ int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* 
                 cudaEvent_t* kev = nullptr, int* kev_pairs = nullptr, double* kflop = nullptr,
                 double* kbytes = nullptr);
 int mixed_tiles(int m);
+int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at most
 
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
                    cudaStream_t st, bool df = false);

@@ -28,6 +28,8 @@
 // The launches run on one stream, one at a time (the schedule is at
 // potrf_mixed).  Every mbarrier wait is bounded; on a timeout the kernel
 // records an error code, frees its tensor memory and returns.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -47,6 +49,7 @@ constexpr int kTileBytes = kTileSlices * kSliceBytes;  // 96 KB per 128-row pane
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+__device__ __forceinline__ int cdiv_d(int a, int b) { return (a + b - 1) / b; }
 
 // byte offset of element (row r, column k) inside one pre-swizzled slice
 __device__ __forceinline__ uint32_t swz_off(int r, int k) {
@@ -209,31 +212,40 @@ __device__ __forceinline__ void dp_row_solve(float* row, const float* T, float (
 }
 
 // Cholesky of a 32 x 32 block held by one warp, lane i holding row i (a[j],
-// j <= i), right-looking in registers: 1/sqrt of the pivot once (rsqrt),
-// column c scaled, rank-1 update of the columns to its right with L[j][c]
-// shuffled from lane j.  The next pivot, A[c+1][c+1] - L[c+1][c]^2, is
-// formed by lane c + 1 from its own entries and broadcast at once, so the
-// pivot chain carries one shuffle per column; its value is the one the
-// rank-1 update leaves in lane c + 1.  FULL (w == 32) is branch-free.  Lane
-// c keeps 1/L[c][c] in invv and flags a negative pivot (replaced by its
-// absolute value, func.cpp:827-833).
+// j <= i), right-looking in registers.  Column c: 1/sqrt of the pivot once
+// (rsqrt), the column scaled, then written as row c of T (T[c][j] = L[j][c],
+// 1 / L[c][c] on the diagonal, zero above), from which every lane reads the
+// column back with 16-byte broadcast loads for its rank-1 update.  The next
+// pivot, A[c+1][c+1] - L[c+1][c]^2, is formed by lane c + 1 from its own
+// entries and shuffled to all lanes at once, so only one shuffle per column
+// is on the pivot chain.  FULL (w == 32) is branch-free; otherwise the rows
+// of T past w are zeroed.  A negative pivot is replaced by its absolute
+// value and flagged in `neg` (func.cpp:827-833).
 template <bool FULL>
-__device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, float& invv, int& neg) {
+__device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, float* T, int& neg) {
   float d = __shfl_sync(0xffffffffu, a[0], 0);
 #pragma unroll
   for (int c = 0; c < 32; c++) {
     if (!FULL && c >= w) break;
     const float ad = fabsf(d);
     const float inv = rsqrtf(ad);
-    if (lane == c) {
-      invv = inv;
-      neg = d < 0.f;
-    }
+    if (lane == c) neg |= d < 0.f;
     a[c] = (lane == c) ? ad * inv : ((lane > c) ? a[c] * inv : a[c]);
     if (c + 1 < 32) d = __shfl_sync(0xffffffffu, fmaf(-a[c], a[c], a[c + 1]), c + 1);
+    T[c * kLt + lane] = (lane > c) ? a[c] : (lane == c ? inv : 0.f);
+    __syncwarp();
 #pragma unroll
-    for (int j = c + 1; j < 32; j++) a[j] = fmaf(-a[c], __shfl_sync(0xffffffffu, a[c], j), a[j]);
+    for (int k = (c + 1) >> 2; k < 8; k++) {
+      const float4 tv = reinterpret_cast<const float4*>(T + c * kLt)[k];
+      const float t4[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        if (4 * k + e > c) a[4 * k + e] = fmaf(-a[c], t4[e], a[4 * k + e]);
+    }
   }
+  if (!FULL)
+    for (int c = w; c < 32; c++) T[c * kLt + lane] = 0.f;
+  __syncwarp();
 }
 
 // Row r of L_ik, columns c0 .. c0 + 31 (x[j] = 0 past column w): (L, 0)
@@ -333,16 +345,21 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
     if (warp == 0) {
       float a[32];
 #pragma unroll
-      for (int j = 0; j < 32; j++) a[j] = (lane < w && j <= lane) ? S[c0 + lane][c0 + j] : 0.f;
-      float invv = 0.f;
-      int neg = 0;
-      if (w == 32) warp_chol32<true>(a, 32, lane, invv, neg);
-      else warp_chol32<false>(a, w, lane, invv, neg);
-      if (is_diag && neg) atomicAdd(negpiv, 1);
+      for (int k = 0; k < 8; k++) {
+        const float4 v = lane < w ? reinterpret_cast<const float4*>(&S[c0 + lane][c0])[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        a[4 * k] = v.x, a[4 * k + 1] = v.y, a[4 * k + 2] = v.z, a[4 * k + 3] = v.w;
+      }
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        if (lane < w && j <= lane) S[c0 + lane][c0 + j] = a[j];
-        T[j * kLt + lane] = (j < lane) ? a[j] : (j == lane ? invv : 0.f);
+      for (int j = 0; j < 32; j++)
+        if (j > lane) a[j] = 0.f;  // upper part: not referenced
+      int neg = 0;
+      if (w == 32) warp_chol32<true>(a, 32, lane, T, neg);
+      else warp_chol32<false>(a, w, lane, T, neg);
+      if (is_diag) {  // L_kk is kept by CTA 0 only; the others need T alone
+        if (neg) atomicAdd(negpiv, 1);
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (lane < w && j <= lane) S[c0 + lane][c0 + j] = a[j];
       }
     } else if (warp >= 2 && w1 > 0 && c0 > 0) {
       dp_block_update(S, tid - 64, c1, min(32, w1), nd, nd + nrows, 0, c0);
@@ -400,6 +417,9 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
 #ifndef BD_REST_PREFETCH
 #define BD_REST_PREFETCH 0  // L2 prefetch of the FP64 tile ahead of the epilogue (measured slower)
 #endif
+#ifndef BD_EPI_AHEAD
+#define BD_EPI_AHEAD 8  // chunks of 8 columns whose old values are in flight per epilogue thread (4: 8 % slower bulk)
+#endif
 #ifndef BD_REST_GROUP
 #define BD_REST_GROUP 0  // tiles per CTA; 0: from the tile count
 #endif
@@ -412,8 +432,12 @@ struct RestBars {
   uint64_t fullA, emptyA, fullB[2], emptyB[2], accFull[2], accEmpty[2], done;
 };
 
-__device__ __forceinline__ void rest_tile(int t, int jlo, int col_only, int& I, int& J) {
-  if (col_only) {
+// Tile t of an update job's enumeration, from column jlo:
+//   kRowTri  the triangle I >= J >= jlo row by row (consecutive tiles share I),
+//   kCol     column jlo alone (I = jlo + t).
+enum { kRowTri = 0, kCol = 1 };
+__device__ __forceinline__ void rest_tile(int t, int jlo, int mode, int nt, int& I, int& J) {
+  if (mode == kCol) {
     I = jlo + t;
     J = jlo;
     return;
@@ -431,8 +455,8 @@ __device__ __forceinline__ void rest_tile(int t, int jlo, int col_only, int& I, 
 // of the tile (K = 256): both operands streamed in four 96 KB chunks per
 // tile (panel, K-half) through the two stages.
 template <int NPAN>
-__device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int lda, int m, int jlo, int col_only,
-                                          int ntiles, int group, int cta, const unsigned char* __restrict__ PS,
+__device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int lda, int m, int jlo, int mode,
+                                          int tlo, int thi, int group, int cta, const unsigned char* __restrict__ PS,
                                           const unsigned char* __restrict__ PS2, int* err) {
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   unsigned char* sA = sm;                 // 3 slices x 32 KB
@@ -441,7 +465,8 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t0 = cta * group, t1 = min(t0 + group, ntiles);
+  const int t0 = tlo + cta * group, t1 = min(t0 + group, thi);
+  const int nt = cdiv_d(m, kT);
   if (threadIdx.x == 0) {
     sm100::mbar_init(&bars->fullA, 1);
     sm100::mbar_init(&bars->emptyA, 1);
@@ -470,7 +495,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
       bool ok = true;
       for (int t = t0; t < t1 && ok; t++) {
         int I, J;
-        rest_tile(t, jlo, col_only, I, J);
+        rest_tile(t, jlo, mode, nt, I, J);
         if (I != curI) {
           if (nA > 0) ok = sm100::mbar_wait(&bars->emptyA, (nA - 1) & 1, kWaitLimit);
           if (!ok || *abort_flag) break;
@@ -520,7 +545,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
         bool ok = true;
         for (int t = t0; t < t1 && ok; t++) {
           int I, J;
-          rest_tile(t, jlo, col_only, I, J);
+          rest_tile(t, jlo, mode, nt, I, J);
           const bool dg = I == J;
           for (int q = 0; q < 4; q++) {
             const int st = ctot & 1;
@@ -566,7 +591,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
       int n = 0;
       for (int t = t0; t < t1; t++, n++) {
         int I, J;
-        rest_tile(t, jlo, col_only, I, J);
+        rest_tile(t, jlo, mode, nt, I, J);
         if (*abort_flag) break;
         if (I != curI) {
           ok = sm100::mbar_wait(&bars->fullA, nA & 1, kWaitLimit);
@@ -600,7 +625,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
         if (!ok) break;
         sm100::mma_commit(&bars->accFull[acc]);
         int In = -1, Jn;
-        if (t + 1 < t1) rest_tile(t + 1, jlo, col_only, In, Jn);
+        if (t + 1 < t1) rest_tile(t + 1, jlo, mode, nt, In, Jn);
         if (In != I) sm100::mma_commit(&bars->emptyA);
       }
       if (!ok) {
@@ -617,7 +642,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
         int n = 0;
         for (int t = t0; t < t1; t++, n++) {
           int I, J;
-          rest_tile(t, jlo, col_only, I, J);
+          rest_tile(t, jlo, mode, nt, I, J);
           if (*abort_flag) break;
           const bool dg = I == J;
           const int acc = n & 1;
@@ -661,11 +686,45 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
     }
   } else {
     // ---------------- epilogue
+    // Each thread owns one row of the tile and the warp's 64-column half, in
+    // chunks of kEpC columns.  The old double-float values of kEpS chunks are
+    // in flight at all times: a chunk's slot is refilled as soon as it has
+    // been written back, with a later chunk of this tile or the matching
+    // chunk of the next one, so the loads run ahead of the accumulator and
+    // across tile boundaries.
+    constexpr int kEpC = 8, kEpN = 64 / kEpC, kEpS = BD_EPI_AHEAD;
+    static_assert(kEpN % kEpS == 0, "slots must divide the chunks");
     const int q = warp & 3, ch = (warp - 2) >> 2;
+    // columns [0, jcnt) of this thread's row of tile t are inside the matrix
+    // and the lower triangle, at colp + j lda
+    auto row_of = [&](int t, float2*& colp, int& jcnt) {
+      int I, J;
+      rest_tile(t, jlo, mode, nt, I, J);
+      const int gi = I * kT + 32 * q + lane;
+      const int cbase = J * kT + 64 * ch;
+      const int jlim0 = (I == J) ? max(0, gi - cbase + 1) : 64;  // diagonal tile: columns <= gi
+      jcnt = gi < m ? min(min(jlim0, 64), m - cbase) : 0;
+      colp = A + (size_t)cbase * lda + gi;
+    };
+    float2 old[kEpS][kEpC];
+    auto load_chunk = [&](float2 (&o)[kEpC], const float2* colp, int jcnt, int c) {
+#pragma unroll
+      for (int j = 0; j < kEpC; j++)
+        o[j] = (kEpC * c + j < jcnt) ? colp[(size_t)(kEpC * c + j) * lda] : make_float2(0.f, 0.f);
+    };
+    float2* colp = A;
+    int jcnt = 0;
+    if (t0 < t1) {
+      row_of(t0, colp, jcnt);
+#pragma unroll
+      for (int s2 = 0; s2 < kEpS; s2++) load_chunk(old[s2], colp, jcnt, s2);
+    }
     int n = 0;
     for (int t = t0; t < t1; t++, n++) {
-      int I, J;
-      rest_tile(t, jlo, col_only, I, J);
+      const bool more = t + 1 < t1;
+      float2* ncolp = A;
+      int njcnt = 0;
+      if (more) row_of(t + 1, ncolp, njcnt);
       const int acc = n & 1;
       const bool ok = sm100::mbar_wait(&bars->accFull[acc], (n >> 1) & 1, kWaitLimit);
       if (!ok || *abort_flag) {
@@ -677,31 +736,24 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
       }
       sm100::tc_fence_after();
       const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * kAccCols + 64 * ch);
-      const int gi = I * kT + 32 * q + lane;
-      const bool diag = I == J;
-      const bool row_ok = gi < m;
-      // columns [jlim0, jlim1) of this thread's row are inside the matrix and the lower triangle
-      const int cbase = J * kT + 64 * ch;
-      const int jlim0 = diag ? max(0, gi - cbase + 1) : 64;  // diagonal tile: columns <= gi
-      const int jcnt = row_ok ? min(min(jlim0, 64), m - cbase) : 0;
-      float2* colp = A + (size_t)cbase * lda + gi;
 #pragma unroll
-      for (int c = 0; c < 2; c++) {
-        float2 old[32];
-        float v[32];
-#pragma unroll
-        for (int j = 0; j < 32; j++)
-          old[j] = (32 * c + j < jcnt) ? colp[(size_t)(32 * c + j) * lda] : make_float2(0.f, 0.f);
-        sm100::tmem_ld32(ta + 32 * c, v);
-        if (c == 1) {  // accumulator read out: hand it back to the MMA issuer
+      for (int c = 0; c < kEpN; c++) {
+        const int s2 = c % kEpS;
+        float v[kEpC];
+        sm100::tmem_ld8(ta + kEpC * c, v);
+        if (c == kEpN - 1) {  // accumulator read out: hand it back to the MMA issuer
           sm100::tc_fence_before();
           __syncwarp();
           if (lane == 0) sm100::mbar_arrive(&bars->accEmpty[acc]);
         }
 #pragma unroll
-        for (int j = 0; j < 32; j++)
-          if (32 * c + j < jcnt) colp[(size_t)(32 * c + j) * lda] = df_sub(old[j], v[j]);
+        for (int j = 0; j < kEpC; j++)
+          if (kEpC * c + j < jcnt) colp[(size_t)(kEpC * c + j) * lda] = df_sub(old[s2][j], v[j]);
+        if (c + kEpS < kEpN) load_chunk(old[s2], colp, jcnt, c + kEpS);
+        else if (more) load_chunk(old[s2], ncolp, njcnt, c + kEpS - kEpN);
       }
+      colp = ncolp;
+      jcnt = njcnt;
     }
   }
   sm100::tc_fence_before();
@@ -709,26 +761,44 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
   if (warp == 1) sm100::tmem_dealloc(tmem, 2 * kAccCols);
 }
 
-// One launch per panel step: CTAs [0, ndp) factor panel pk (diagonal block
-// and the tiles below it, writing its slices to PSp); the remaining CTAs
-// apply an earlier panel's trailing update (tiles from jlo, slices PSu).
-// The two parts touch disjoint columns and slice buffers.
-__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(float2* A, float* Ldg, int lda, int m, int ndp, int pk0, int pkb,
-                                                              unsigned char* PSp, int* negpiv, int jlo, int col_only,
-                                                              int ntiles, int group,
-                                                              const unsigned char* __restrict__ PSu,
-                                                              const unsigned char* __restrict__ PSu2, int* err) {
+// An update job: tiles [tlo, thi) of an enumeration (rest_tile) from column
+// jlo, panel slices ps (and ps2: two panels, K = 256), `group` tiles per CTA.
+struct UpdJob {
+  const unsigned char* ps;
+  const unsigned char* ps2;
+  int jlo, mode, tlo, thi, group, nctas;
+};
+struct StepArgs {
+  float2* A;
+  float* Ldg;           // this panel's diagonal factor
+  unsigned char* PSp;   // this panel's slice buffer
+  int* negpiv;
+  int* err;
+  int lda, m, ndp, pk0, pkb;
+  UpdJob job[2];
+};
+
+// One launch per step: CTAs [0, ndp) factor panel pk (diagonal block and the
+// tiles below it, writing its slices to PSp); then the CTAs of update job 0,
+// then those of job 1.  The parts of one launch touch disjoint tiles and
+// slice buffers.
+__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_constant__ StepArgs a) {
   extern __shared__ float4 smem4[];
-  if ((int)blockIdx.x < ndp) {
-    dpanel_body(smem4, A, Ldg, lda, m, pk0, pkb, pk0 / kT + 1, (int)blockIdx.x, PSp, negpiv);
+  int b = (int)blockIdx.x;
+  if (b < a.ndp) {
+    dpanel_body(smem4, a.A, a.Ldg, a.lda, a.m, a.pk0, a.pkb, a.pk0 / kT + 1, b, a.PSp, a.negpiv);
     return;
   }
-  if (PSu2)
-    rest_body<2>(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group,
-                 (int)blockIdx.x - ndp, PSu, PSu2, err);
+  b -= a.ndp;
+  const int jn = b < a.job[0].nctas ? 0 : 1;
+  if (jn) b -= a.job[0].nctas;
+  const UpdJob& j = a.job[jn];
+  if (j.ps2)
+    rest_body<2>(reinterpret_cast<unsigned char*>(smem4), a.A, a.lda, a.m, j.jlo, j.mode, j.tlo, j.thi, j.group, b,
+                 j.ps, j.ps2, a.err);
   else
-    rest_body<1>(reinterpret_cast<unsigned char*>(smem4), A, lda, m, jlo, col_only, ntiles, group,
-                 (int)blockIdx.x - ndp, PSu, nullptr, err);
+    rest_body<1>(reinterpret_cast<unsigned char*>(smem4), a.A, a.lda, a.m, j.jlo, j.mode, j.tlo, j.thi, j.group, b,
+                 j.ps, nullptr, a.err);
 }
 
 // After the last panel: the diagonal factors L_kk from the side buffer into
@@ -746,11 +816,13 @@ __global__ void __launch_bounds__(256) k_diag_scatter(float2* A, int lda, int m,
 
 namespace bdk {
 
-// two panel-slice buffers: panel k writes buffer k & 1 while the updates of
-// panel k - 1 still read the other
-size_t mixed_panel_bytes(int m) {  // three slice buffers, then the diagonal factors
-  return 3 * (size_t)cdiv(m, kT) * kTileBytes + (size_t)cdiv(m, kT) * kT * kT * sizeof(float);
+// kBufs panel-slice buffers, panel p in buffer p % kBufs: a pair's bulk
+// update reads panels k and k + 1 while panel k + 2 is written
+constexpr int kBufs = 3;
+size_t mixed_panel_bytes(int m) {  // the slice buffers, then the diagonal factors
+  return kBufs * (size_t)cdiv(m, kT) * kTileBytes + (size_t)cdiv(m, kT) * kT * kT * sizeof(float);
 }
+int mixed_max_launches(int m) { return 2 * cdiv(m, kT) + 2; }
 int mixed_tiles(int m) { return cdiv(m, kT); }
 
 static bool g_attr_done = false;
@@ -780,80 +852,119 @@ static int rest_group(int tiles) {
 }
 
 // Right-looking with a lookahead of one panel, on one stream, no two kernels
-// at a time.  Panel p's slices live in buffer p % 3; L_kk in a side buffer.
-// Single step k (invariant: panel k factored, columns > k hold the updates
-// of panels < k):
-//   launch 1: panel k's update of column k+1;
-//   launch 2: panel k+1 (extra CTAs) + panel k's update of the tiles right
-//             of column k+1.
-// Pair (k, k+1), used while the trailing matrix is large: the bulk tiles
-// get both panels in one read-modify-write (K = 256), half the HBM traffic:
-//   launch 1: panel k's update of column k+1;
-//   launch 2: panel k+1 + panel k's update of column k+2;
-//   launch 3: panel k+1's update of column k+2;
-//   launch 4: panel k+2 + panels k and k+1 on the tiles right of column k+2.
+// at a time; every launch is one k_chol_step (panel CTAs and up to two
+// update jobs).  Panel p's slices live in buffer p % kBufs, L_kk in a side
+// buffer.
+// Single step k (panel k factored; columns > k hold the updates of panels
+// < k):
+//   1: panel k's update of column k+1;
+//   2: panel k+1 + panel k's update of the tiles right of column k+1.
+// Pair (k, k+1), while the trailing matrix is large: the bulk tiles get both
+// panels in one read-modify-write (K = 256), half the HBM traffic:
+//   1: panel k's update of column k+1;
+//   2: panel k+1 + panel k's update of column k+2;
+//   3: panel k+1's update of column k+2;
+//   4: panel k+2 + panels k and k+1 on the tiles right of column k+2.
 // Returns the number of kernel launches.
 #ifndef BD_PAIR_MIN
 #define BD_PAIR_MIN 24  // pair while at least this many tile rows remain right of column k+2
 #endif
+namespace {
+struct Job {
+  const unsigned char* ps = nullptr;
+  const unsigned char* ps2 = nullptr;
+  int jlo = 0, mode = kCol, tiles = 0, group = 1;
+};
+}  // namespace
+
 int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
                 cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes) {
   float2* A = reinterpret_cast<float2*>(A64);  // double-float storage, 8 bytes per element
   const int nt = cdiv(m, kT);
   const size_t buf = (size_t)nt * kTileBytes;
-  int L = 0, pairs = 0;
+  int L = 0, timed = 0;
   auto kb_of = [&](int k) { return (m - k * kT < kT) ? m - k * kT : kT; };
-  auto psb = [&](int k) { return PS + (size_t)(k % 3) * buf; };
-  float* Ld = reinterpret_cast<float*>(PS + 3 * buf);  // [nt][128 x 128] diagonal factors
-  auto col = [&](int k) {  // panel k's update of column k+1
-    const int below = nt - k - 1;
-    k_chol_step<<<below, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, 0, 0, 0, nullptr, negpiv, k + 1, 1, below, 1,
-                                                         psb(k), nullptr, err);
-    L++;
-  };
-  // panel pn in extra CTAs + an update of the tiles from column jlo by panel
-  // pu (and pu + 1 when two), triangle or (col_only) one column
-  auto step = [&](int pn, int jlo, int pu, bool two, bool col_only, bool timed) {
-    const int ndp = nt - pn;
-    const int rows = nt - jlo;
-    const int tiles = rows <= 0 ? 0 : (col_only ? rows : rows * (rows + 1) / 2);
-    const int group = (tiles > 0 && !col_only) ? rest_group(tiles) : 1;
-    if (timed && kev) cudaEventRecord(kev[2 * pairs], st);
-    k_chol_step<<<ndp + cdiv(tiles, group), kRestThreads, kRestSmem, st>>>(
-        A, Ld + (size_t)pn * kT * kT, lda, m, ndp, pn * kT, kb_of(pn), (unsigned char*)psb(pn), negpiv, jlo,
-        col_only ? 1 : 0, tiles, group, psb(pu), two ? psb(pu + 1) : nullptr, err);
-    if (timed && kev) {
-      cudaEventRecord(kev[2 * pairs + 1], st);
-      pairs++;
+  auto psb = [&](int k) { return PS + (size_t)(k % kBufs) * buf; };
+  float* Ld = reinterpret_cast<float*>(PS + kBufs * buf);  // [nt][128 x 128] diagonal factors
+  // elements of the lower triangle in tile columns [j0, j1)
+  auto elems = [&](int j0, int j1) {
+    double e = 0.0;
+    for (int J = j0; J < j1 && J < nt; J++) {
+      const double cols = kb_of(J);
+      e += cols * (double)(m - J * kT) - cols * (cols - 1) / 2;
     }
-    if (timed) {
-      const double n2 = (double)(m - jlo * kT);
-      if (kflop) *kflop += 6.0 * 2.0 * kT * kT * kT * tiles * (two ? 2 : 1);  // BF16 tensor work issued
-      if (kbytes && n2 > 0) *kbytes += 16.0 * n2 * (n2 + 1) / 2;           // double-float read + write
+    return e;
+  };
+  auto col_job = [&](int p, int J) {
+    Job j;
+    j.ps = psb(p), j.jlo = J, j.mode = kCol, j.tiles = nt - J, j.group = 1;
+    return j;
+  };
+  auto tri_job = [&](int p, bool two, int jlo) {
+    Job j;
+    const int n = nt - jlo;
+    j.ps = psb(p), j.ps2 = two ? psb(p + 1) : nullptr, j.jlo = jlo, j.mode = kRowTri;
+    j.tiles = n > 0 ? n * (n + 1) / 2 : 0;
+    j.group = rest_group(j.tiles);
+    return j;
+  };
+  auto launch = [&](int pn, const Job& j0, const Job& j1) {
+    StepArgs a{};
+    a.A = A, a.negpiv = negpiv, a.err = err, a.lda = lda, a.m = m;
+    a.Ldg = Ld, a.PSp = PS;
+    if (pn >= 0) {
+      a.ndp = nt - pn, a.pk0 = pn * kT, a.pkb = kb_of(pn);
+      a.Ldg = Ld + (size_t)pn * kT * kT, a.PSp = psb(pn);
+    }
+    const Job* js[2] = {&j0, &j1};
+    int grid = a.ndp;
+    for (int q = 0; q < 2; q++) {
+      const Job& j = *js[q];
+      UpdJob& u = a.job[q];
+      u.ps = j.ps, u.ps2 = j.ps2, u.jlo = j.jlo, u.mode = j.mode, u.tlo = 0, u.thi = j.tiles, u.group = j.group;
+      u.nctas = j.tiles > 0 ? cdiv(j.tiles, j.group) : 0;
+      grid += u.nctas;
+    }
+    if (grid == 0) return;
+    if (kev) cudaEventRecord(kev[2 * timed], st);
+    k_chol_step<<<grid, kRestThreads, kRestSmem, st>>>(a);
+    if (kev) {
+      cudaEventRecord(kev[2 * timed + 1], st);
+      timed++;
     }
     L++;
+    if (kbytes || kflop) {
+      double by = pn >= 0 ? 16.0 * (double)(m - pn * kT) * kb_of(pn) : 0.0;  // panel read and written back
+      double fl = 0.0;
+      for (int q = 0; q < 2; q++) {
+        const Job& j = *js[q];
+        if (j.tiles <= 0) continue;
+        by += 16.0 * elems(j.jlo, j.mode == kCol ? j.jlo + 1 : nt);  // double-float tile read + write
+        fl += 6.0 * 2.0 * kT * kT * kT * j.tiles * (j.ps2 ? 2 : 1);  // BF16 tensor work issued
+      }
+      if (kbytes) *kbytes += by;
+      if (kflop) *kflop += fl;
+    }
   };
-  // panel 0 alone
-  k_chol_step<<<nt, kRestThreads, kRestSmem, st>>>(A, Ld, lda, m, nt, 0, kb_of(0), PS, negpiv, 0, 0, 0, 1, PS,
-                                                   nullptr, err);
-  L++;
+  const Job none;
+  launch(0, none, none);  // panel 0 alone
   int k = 0;
   while (k + 1 < nt) {
     if (nt - (k + 3) >= BD_PAIR_MIN) {
-      col(k);
-      step(k + 1, k + 2, k, false, true, false);
-      col(k + 1);
-      step(k + 2, k + 3, k, true, false, true);
+      launch(-1, col_job(k, k + 1), none);
+      launch(k + 1, col_job(k, k + 2), none);
+      launch(-1, col_job(k + 1, k + 2), none);
+      launch(k + 2, tri_job(k, true, k + 3), none);
       k += 2;
     } else {
-      col(k);
-      step(k + 1, k + 2, k, false, false, true);
+      launch(-1, col_job(k, k + 1), none);
+      launch(k + 1, tri_job(k, false, k + 2), none);
       k += 1;
     }
   }
   k_diag_scatter<<<nt, 256, 0, st>>>(A, lda, m, Ld);
   L++;
-  if (kev_pairs) *kev_pairs = pairs;
+  if (kev_pairs) *kev_pairs = timed;
   return L;
 }
 
