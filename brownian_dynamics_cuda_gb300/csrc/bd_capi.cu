@@ -139,10 +139,10 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   cudaStream_t st = c->stream;
   int L = 0;
   record(c, 0);
-  bdk::gather_rall(M, c->X, c->r_all, st);
-  L++;
-  bool rebuild = (c->step_count % c->freq_rp) == 0;
   const bool mixed = c->precision == BD_PREC_MIXED;
+  bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
+  L += mixed ? 2 : 1;
+  bool rebuild = (c->step_count % c->freq_rp) == 0;
   if (rebuild) {
     bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed);
     L++;
@@ -167,17 +167,17 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   record(c, 3);
   L += bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
   record(c, 4);
-  bdk::rotate_translate(M, c->X, c->Y, c->F0, d_rr, c->rd, c->r_all, c->precision, st);
-  L += 2;
+  bdk::rotate_translate(M, c->X, c->Y, c->F0, d_rr, c->rd, c->r_all, c->precision, c->S, st);
+  L += mixed ? 3 : 2;
   record(c, 5);
   bdk::frames(M, c->Y, st);
-  L++;
+  L += 2;
   record(c, 6);
   L += bdk::forces(M, c->Y, c->F1, c->S, c->precision, st);
   record(c, 7);
   bdk::average_forces(M, c->F0, c->F1, c->Fa, st);
-  bdk::rotate_translate(M, c->X, c->Y, c->Fa, d_rr, c->rd, c->r_all, c->precision, st);
-  L += 3;
+  bdk::rotate_translate(M, c->X, c->Y, c->Fa, d_rr, c->rd, c->r_all, c->precision, c->S, st);
+  L += mixed ? 4 : 3;
   // X <- Y (final_updates, func_cuda.cu:2643-2662), then refresh frames
   size_t n3 = 3 * (size_t)M.n;
   CK(cudaMemcpyAsync(c->X.r, c->Y.r, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -187,7 +187,7 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   if (M.n_tail) CK(cudaMemcpyAsync(c->X.r_t, c->Y.r_t, 3 * (size_t)M.n_tail * sizeof(double), cudaMemcpyDeviceToDevice, st));
   if (M.n_LH) CK(cudaMemcpyAsync(c->X.r_lh, c->Y.r_lh, 3 * (size_t)M.n_LH * sizeof(double), cudaMemcpyDeviceToDevice, st));
   bdk::frames(M, c->X, st);
-  L++;
+  L += 2;
   record(c, 8);
   CK(cudaGetLastError());
   c->last_launches = L;
@@ -299,7 +299,8 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   addD((size_t)nc * nc * 10); addD(ndna * nc * 7); addD(nlhc * nc * 10); addD(ebuf);
   addD(3 * (size_t)M.n_D); addD(c->m); addD(c->m); addD(3 * n); addD(bdk::trmv_scratch_doubles(c->m)); addD(1); addI(1);
   const int npos = n + nt + nL + nlhc * M.n_lh_g;
-  addD((nt + 1) / 2); addD(2 * (size_t)npos); addD(2 * (size_t)npos);
+  addD((nt + 4 * (size_t)M.Nq + 1) / 2); addD(2 * (size_t)npos); addD(2 * (size_t)npos);
+  for (int q = 0; q < 3; q++) addD(2 * (size_t)M.n_D);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
   if (c->precision != BD_PREC_MIXED && c->precision != BD_PREC_FP64)
@@ -352,9 +353,12 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   c->rr = ar.take<double>(3 * n);
   c->rd_part = ar.take<double>(bdk::trmv_scratch_doubles(c->m));
   c->energy = ar.take<double>(1);
-  float* d_tqf = ar.take<float>(nt);
+  float* d_tqf = ar.take<float>(nt + 4 * (size_t)m->Nq);  // tail charges, core sites, core charges (FP32)
   c->S.ph = ar.take<float4>(npos);
   c->S.pl = ar.take<float4>(npos);
+  c->S.qh = ar.take<float4>(M.n_D);
+  c->S.ql = ar.take<float4>(M.n_D);
+  c->S.qf = ar.take<float4>(M.n_D);
   c->S.ot = n; c->S.ol = n + nt; c->S.og = n + nt + nL; c->S.npos = npos;
   c->negpiv = ar.take<int>(1);
   cudaStream_t st = c->stream;
@@ -384,12 +388,19 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   M.LH_q = d_lhp[0]; M.LH_vdw_hh = d_lhp[1]; M.LH_vdw_hc = d_lhp[2]; M.LH_vdw_hl = d_lhp[3]; M.LH_vdw_ht = d_lhp[4];
   M.LH_kstr = d_lhp[5]; M.LH_kben = d_lhp[6]; M.LH_streq = d_lhp[7]; M.LH_betaeq = d_lhp[8];
   {
-    std::vector<float> tqf(nt);
+    const int nq = m->Nq;
+    std::vector<float> tqf(nt + 4 * (size_t)nq);
     for (int t = 0; t < nt; t++) tqf[t] = (float)m->t_q[t];
-    if (nt && cudaMemcpyAsync(d_tqf, tqf.data(), nt * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    for (int k = 0; k < 3 * nq; k++) tqf[nt + k] = (float)m->core_pos[k];
+    for (int k = 0; k < nq; k++) tqf[nt + 3 * nq + k] = (float)m->core_q[k];
+    if (!tqf.empty() &&
+        cudaMemcpyAsync(d_tqf, tqf.data(), tqf.size() * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess)
       return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
-    if (nt && cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
+    if (!tqf.empty() && cudaStreamSynchronize(st) != cudaSuccess)
+      return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
     M.t_qf = d_tqf;
+    M.core_pf = d_tqf + nt;
+    M.core_qf = d_tqf + nt + 3 * nq;
     M.tails_by_core = M.n_t > 0;
     for (int t = 0; t < nt && M.tails_by_core; t++)
       if (t_core_bead[t] != -1 && (t / M.n_t >= nc || t_core_bead[t] != core_bead[t / M.n_t])) M.tails_by_core = 0;
@@ -572,7 +583,7 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
 }
 
 static void assemble_now(bd_ctx* c) {
-  bdk::gather_rall(c->M, c->X, c->r_all, c->stream);
+  bdk::gather_rall(c->M, c->X, c->r_all, nullptr, c->stream);
   bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream,
                     c->precision == BD_PREC_MIXED);
 }

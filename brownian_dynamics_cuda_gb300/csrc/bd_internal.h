@@ -76,6 +76,8 @@ struct DevModel {
   double qmax_core;        // max |core_pos| (nm), for exact far-pair skipping
   double gmax;             // max |LH_g_pos|
   const float* t_qf;       // [n_tail] tail charges in FP32 (mixed path)
+  const float* core_pf;    // [3 Nq] core_pos in FP32 (mixed path)
+  const float* core_qf;    // [Nq] core_q in FP32 (mixed path)
   int tails_by_core;       // tail t belongs to core t / n_t (or to none): anchored-tail scans per core
 };
 
@@ -107,15 +109,20 @@ struct DevScratch {
   // (hi, lo) of FP32 xyz, chain | tails | LH | G-heads
   float4 *ph, *pl;
   int ot, ol, og, npos;
+  // mixed path: the move's start positions as double-float pairs (radius in
+  // qh.w) and the move's forces in FP32, per bead of the tensor
+  float4 *qh, *ql, *qf;
 };
 
 namespace bdk {
 // frames.cu
 void frames(const DevModel& M, DevState& S, cudaStream_t st);
+// mixed: the drift from S.qh / S.ql (filled by gather_rall) and S.qf
 void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const DevForces& Fo, const double* rr,
-                      const double* rd, const double* r_all, int mixed, cudaStream_t st);
+                      const double* rd, const double* r_all, int mixed, const DevScratch& S, cudaStream_t st);
 void average_forces(const DevModel& M, const DevForces& A, const DevForces& B, DevForces& out, cudaStream_t st);
-void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream_t st);
+// r_all: every tensor bead's position; with S (mixed path) also S->qh / S->ql
+void gather_rall(const DevModel& M, const DevState& X, double* r_all, const DevScratch* S, cudaStream_t st);
 // forces.cu
 // returns the number of kernels launched
 int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);

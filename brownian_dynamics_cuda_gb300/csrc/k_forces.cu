@@ -386,26 +386,34 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevStat
   double* red = sm + (14 * Nq + 1) / 2;
   const V3 ai = ld3(X.a + 3 * i), bi = ld3(X.b + 3 * i), ci = ld3(X.c + 3 * i);
   const V3 aj = ld3(X.a + 3 * j), bj = ld3(X.b + 3 * j), cj = ld3(X.c + 3 * j);
-  const V3 mid{0.5 * (ri.x + rj.x), 0.5 * (ri.y + rj.y), 0.5 * (ri.z + rj.z)};
+  // sites relative to the pair's midpoint, in FP32: the two centre offsets
+  // in FP64 once, the frames converted once, the lever arms in FP32 (no
+  // FP64 per site)
+  const float oix = (float)(0.5 * (ri.x - rj.x)), oiy = (float)(0.5 * (ri.y - rj.y)), oiz = (float)(0.5 * (ri.z - rj.z));
+  const float aix = (float)ai.x, aiy = (float)ai.y, aiz = (float)ai.z, bix = (float)bi.x, biy = (float)bi.y,
+              biz = (float)bi.z, cix = (float)ci.x, ciy = (float)ci.y, ciz = (float)ci.z;
+  const float ajx = (float)aj.x, ajy = (float)aj.y, ajz = (float)aj.z, bjx = (float)bj.x, bjy = (float)bj.y,
+              bjz = (float)bj.z, cjx = (float)cj.x, cjy = (float)cj.y, cjz = (float)cj.z;
+  const float kef = (float)M.k_e;
   for (int k = threadIdx.x; k < Nq; k += blockDim.x) {
-    const double* p = M.core_pos + 3 * k;
-    const V3 li{ai.x * p[0] + bi.x * p[1] + ci.x * p[2], ai.y * p[0] + bi.y * p[1] + ci.y * p[2],
-                ai.z * p[0] + bi.z * p[1] + ci.z * p[2]};
-    const V3 lj{aj.x * p[0] + bj.x * p[1] + cj.x * p[2], aj.y * p[0] + bj.y * p[1] + cj.y * p[2],
-                aj.z * p[0] + bj.z * p[1] + cj.z * p[2]};
-    sIx[k] = (float)((ri.x - mid.x) + li.x); sIy[k] = (float)((ri.y - mid.y) + li.y); sIz[k] = (float)((ri.z - mid.z) + li.z);
-    sJx[k] = (float)((rj.x - mid.x) + lj.x); sJy[k] = (float)((rj.y - mid.y) + lj.y); sJz[k] = (float)((rj.z - mid.z) + lj.z);
-    lIx[k] = (float)li.x; lIy[k] = (float)li.y; lIz[k] = (float)li.z;
-    lJx[k] = (float)lj.x; lJy[k] = (float)lj.y; lJz[k] = (float)lj.z;
-    qI[k] = (float)(M.k_e * M.core_q[k]);
-    qJ[k] = (float)M.core_q[k];
+    const float p0 = M.core_pf[3 * k], p1 = M.core_pf[3 * k + 1], p2 = M.core_pf[3 * k + 2];
+    const float lix = aix * p0 + bix * p1 + cix * p2, liy = aiy * p0 + biy * p1 + ciy * p2,
+                liz = aiz * p0 + biz * p1 + ciz * p2;
+    const float ljx = ajx * p0 + bjx * p1 + cjx * p2, ljy = ajy * p0 + bjy * p1 + cjy * p2,
+                ljz = ajz * p0 + bjz * p1 + cjz * p2;
+    sIx[k] = oix + lix; sIy[k] = oiy + liy; sIz[k] = oiz + liz;
+    sJx[k] = ljx - oix; sJy[k] = ljy - oiy; sJz[k] = ljz - oiz;
+    lIx[k] = lix; lIy[k] = liy; lIz[k] = liz;
+    lJx[k] = ljx; lJy[k] = ljy; lJz[k] = ljz;
+    qI[k] = kef * M.core_qf[k];
+    qJ[k] = M.core_qf[k];
   }
   __syncthreads();
   const float kap = (float)M.debye, kex = (float)M.k_ex, sg = (float)M.sCC;
-  float a[10];
-  double v[10];
+  // runs of kCCFlush terms in FP32, the runs added with Kahan compensation
+  float a[10], ks[10], kc[10];
 #pragma unroll
-  for (int q = 0; q < 10; q++) a[q] = 0.f, v[q] = 0.0;
+  for (int q = 0; q < 10; q++) a[q] = 0.f, ks[q] = 0.f, kc[q] = 0.f;
   int cnt = 0;
   for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
     const int k = p / Nq, l = p - k * Nq;
@@ -433,12 +441,21 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevStat
     a[9] += e;
     if (++cnt == kCCFlush) {
 #pragma unroll
-      for (int q = 0; q < 10; q++) v[q] += (double)a[q], a[q] = 0.f;
+      for (int q = 0; q < 10; q++) {
+        const float y = a[q] - kc[q], t = ks[q] + y;
+        kc[q] = (t - ks[q]) - y;
+        ks[q] = t;
+        a[q] = 0.f;
+      }
       cnt = 0;
     }
   }
+  double v[10];
 #pragma unroll
-  for (int q = 0; q < 10; q++) v[q] += (double)a[q];
+  for (int q = 0; q < 10; q++) {
+    const float y = a[q] - kc[q], t = ks[q] + y;
+    v[q] = (double)t - (double)((t - ks[q]) - y);
+  }
   bsum<10>(v, red);
   if (threadIdx.x == 0) {
     out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
@@ -477,35 +494,41 @@ __global__ void k_dna_core(DevModel M, DevState X, double* slots) {
   const double ke = M.k_e, kap = M.debye, kex = M.k_ex, sg = M.sDC, ql = M.q_l;
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
   if constexpr (MX) {
-    const float kapf = (float)kap, kexf = (float)kex, sgf = (float)sg;
+    // FP32: the core centre relative to the DNA bead once in FP64, the site
+    // lever arms from the FP32 core sites and frames; ~Nq / 32 terms per lane
+    const float kapf = (float)kap, kexf = (float)kex, sgf = (float)sg, qlk = (float)(ke * ql);
     const float acx = (float)ac.x, acy = (float)ac.y, acz = (float)ac.z, bcx = (float)bc.x, bcy = (float)bc.y,
                 bcz = (float)bc.z, ccx = (float)cc.x, ccy = (float)cc.y, ccz = (float)cc.z;
+    const float ox = (float)(rc.x - rd_.x), oy = (float)(rc.y - rd_.y), oz = (float)(rc.z - rd_.z);
+    float a[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int k = lane; k < M.Nq; k += 32) {
-      V3 s = body(rc, ac, bc, cc, cp + 3 * k);
-      float zx = (float)(rd_.x - s.x), zy = (float)(rd_.y - s.y), zz = (float)(rd_.z - s.z);
+      const float c0 = M.core_pf[3 * k], c1 = M.core_pf[3 * k + 1], c2 = M.core_pf[3 * k + 2];
+      float zx = -(ox + (acx * c0 + bcx * c1 + ccx * c2));
+      float zy = -(oy + (acy * c0 + bcy * c1 + ccy * c2));
+      float zz = -(oz + (acz * c0 + bcz * c1 + ccz * c2));
       float dd = sqrtf(zx * zx + zy * zy + zz * zz);
       float mi = 1.f / dd;
       zx *= mi; zy *= mi; zz *= mi;
-      double q = M.core_q[k];
+      const float q = M.core_qf[k];
       float g = 0.f, e = 0.f;
       if (adj) {
         float ex = expf(-kapf * dd);
-        float qq = (float)(ke * ql * q);
+        float qq = qlk * q;
         g = qq * ex * (kapf * dd + 1.f) / (dd * dd);
         e = qq * ex / dd;
       }
-      if (dd <= 8.f && q > 0) {
+      if (dd <= 8.f && q > 0.f) {
         float sr = sgf / dd, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
         g += kexf * (12.f * sr12 - 6.f * sr6) / dd;
         e += kexf * (sr12 - sr6);
       }
-      v[6] += (double)e;
-      v[0] += (double)(g * zx); v[1] += (double)(g * zy); v[2] += (double)(g * zz);
-      const float c0 = (float)cp[3 * k], c1 = (float)cp[3 * k + 1], c2 = (float)cp[3 * k + 2];
+      a[6] += e;
+      a[0] += g * zx; a[1] += g * zy; a[2] += g * zz;
       float fa = -g * (acx * zx + acy * zy + acz * zz), fb = -g * (bcx * zx + bcy * zy + bcz * zz),
             fc = -g * (ccx * zx + ccy * zy + ccz * zz);
-      v[3] += (double)(fc * c1 - fb * c2); v[4] += (double)(fa * c2 - fc * c0); v[5] += (double)(fb * c0 - fa * c1);
+      a[3] += fc * c1 - fb * c2; a[4] += fa * c2 - fc * c0; a[5] += fb * c0 - fa * c1;
     }
+    for (int q = 0; q < 7; q++) v[q] = (double)a[q];
   } else {
   for (int k = lane; k < M.Nq; k += 32) {
       V3 s = body(rc, ac, bc, cc, cp + 3 * k);
@@ -1018,23 +1041,37 @@ __device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float si
   return make_float3(clamp09f(w * d.x), clamp09f(w * d.y), clamp09f(w * d.z));
 }
 
-// FP32 partial sums of force, world torque and energy, flushed to FP64
+// Partial sums of force, world torque and energy: runs of up to 32 terms in
+// plain FP32, the runs added with Kahan compensation (still FP32: an FP64
+// operation costs as much as ~64 FP32 ones on GB300); finish() forms the
+// FP64 totals s[] once.  Compiled without FMA contraction, so the
+// compensation is exact.
 struct FAcc {
-  float f[7];
+  float f[7], k[7], c[7];
   double s[7];
   int n;
   __device__ void init() {
 #pragma unroll
-    for (int q = 0; q < 7; q++) f[q] = 0.f, s[q] = 0.0;
+    for (int q = 0; q < 7; q++) f[q] = 0.f, k[q] = 0.f, c[q] = 0.f;
     n = 0;
   }
   __device__ void flush() {
 #pragma unroll
-    for (int q = 0; q < 7; q++) s[q] += (double)f[q], f[q] = 0.f;
+    for (int q = 0; q < 7; q++) {
+      const float y = f[q] - c[q], t = k[q] + y;
+      c[q] = (t - k[q]) - y;
+      k[q] = t;
+      f[q] = 0.f;
+    }
     n = 0;
   }
   __device__ void tick() {
     if (++n == 32) flush();
+  }
+  __device__ void finish() {
+    flush();
+#pragma unroll
+    for (int q = 0; q < 7; q++) s[q] = (double)k[q] - (double)c[q];
   }
   __device__ void force(const float3& v) { f[0] += v.x; f[1] += v.y; f[2] += v.z; }
   __device__ void torque(const float3& v) { f[3] += v.x; f[4] += v.y; f[5] += v.z; }
@@ -1120,7 +1157,7 @@ __global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces
       A.tick();
     }
   }
-  A.flush();
+  A.finish();
   F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
   F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
   if (lane == 0) {
@@ -1209,7 +1246,7 @@ __global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces o
     A.force(pairf<true, true>(qb * P.q[m], kap, kex, (P.hh[m] + P.hh[pb]) * 0.5f, sepf(pp, ldpf(S, S.og + s)), dummy));
     A.tick();
   }
-  A.flush();
+  A.finish();
   F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
   F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
   if (lane == 0) {
@@ -1376,7 +1413,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
       }
     }
   }
-  A.flush();
+  A.finish();
   F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
   // world-frame torques of the pair terms into the body frame
   T.x += aj.x * A.s[3] + aj.y * A.s[4] + aj.z * A.s[5];
@@ -1417,7 +1454,7 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
 #undef KSEL
   if (M.n_lhcore > 0) { k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X); L++; }
   if (mixed) { k_mirror<<<cdiv(S.npos, 128), 128, 0, st>>>(M, X, S.ph, S.pl, S.npos); L++; }
-  k_chain_bonded<<<cdiv(M.n, 128), 128, 0, st>>>(M, X, Fm, Tm, Ebond);
+  k_chain_bonded<<<cdiv(M.n, 32), 32, 0, st>>>(M, X, Fm, Tm, Ebond);  // FP64: one warp per SM
   L++;
   if (M.n_c > 1) {
     if (mixed) {

@@ -21,17 +21,21 @@ using namespace bdp;
 
 namespace {
 
-constexpr int kFrameThreads = 1024;
+// FP64 throughout (GB300 runs ~2 FP64 operations per clock per SM), so the
+// beads are spread over many small CTAs: one warp per CTA, 32 beads each.
+constexpr int kFrameThreads = 32;
 
-__global__ void __launch_bounds__(kFrameThreads) k_frames(DevModel M, DevState S) {
+// pass 1: DNA frames follow their bond; lengths (func.cpp:448-505)
+__global__ void __launch_bounds__(kFrameThreads) k_frames_dna(DevModel M, DevState S) {
   const int n = M.n;
   double* r = S.r;
   double* a = S.a;
   double* b = S.b;
   double* c = S.c;
   const double si = sin(kTheta), co = cos(kTheta);
-  // pass 1: DNA frames follow their bond; lengths (func.cpp:448-505)
-  for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+  {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
     int i1 = 3 * i, i2 = i1 + 1, i3 = i2 + 1, f1 = i1 + 3, f2 = f1 + 1, f3 = f2 + 1;
     double rf[3];
     if (M.type[i] == 0) {
@@ -68,9 +72,21 @@ __global__ void __launch_bounds__(kFrameThreads) k_frames(DevModel M, DevState S
       S.length[i] = sqrt(rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2]);
     }
   }
-  __syncthreads();
-  // pass 2: angles (func.cpp:507-681)
-  for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+}
+
+// pass 2 (after pass 1 has finished for every bead): angles
+// (func.cpp:507-681), then the tail and LH bend angles; thread index over
+// the n - 1 chain beads, the tail beads, the LH beads in turn
+__global__ void __launch_bounds__(kFrameThreads) k_frames_angles(DevModel M, DevState S) {
+  const int n = M.n;
+  double* r = S.r;
+  double* a = S.a;
+  double* b = S.b;
+  double* c = S.c;
+  const double si = sin(kTheta), co = cos(kTheta);
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n - 1) {
+    const int i = g;
     int i1 = 3 * i, i2 = i1 + 1, i3 = i2 + 1, f1 = i1 + 3, f2 = f1 + 1, f3 = f2 + 1;
     if (M.type[i] == 0) {
       double af[3], bf[3], cf[3] = {c[f1], c[f2], c[f3]};
@@ -151,7 +167,8 @@ __global__ void __launch_bounds__(kFrameThreads) k_frames(DevModel M, DevState S
     }
   }
   // tail bend angles (func.cpp:1763-1790, bounds test first)
-  for (int i = threadIdx.x; i < M.n_tail; i += blockDim.x) {
+  else if (g < n - 1 + M.n_tail) {
+    const int i = g - (n - 1);
     const double* rt = S.r_t;
     double v = 0.0;
     if (i < M.n_tail - 2 && M.t_grp[i] == M.t_grp[i + 1] && M.t_grp[i] == M.t_grp[i + 2]) {
@@ -164,7 +181,8 @@ __global__ void __launch_bounds__(kFrameThreads) k_frames(DevModel M, DevState S
     S.beta_t[i] = v;
   }
   // LH bend angles (func.cpp:2062-2089)
-  for (int i = threadIdx.x; i < M.n_LH; i += blockDim.x) {
+  else if (g < n - 1 + M.n_tail + M.n_LH) {
+    const int i = g - (n - 1) - M.n_tail;
     const double* rl = S.r_lh;
     double v = 0.0;
     if ((i % M.n_lh_c != 0) && (i % M.n_lh_c != M.n_lh_c - 1)) {
@@ -212,7 +230,6 @@ __global__ void k_rotate(DevModel M, const double* __restrict__ T, const double*
 // D_ss the RPY block of the bead's own species (chain, tails or LH).
 // The lanes split the partner loop; partial sums are combined in a fixed
 // butterfly order so the result is deterministic.
-template <bool MX>
 __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const double* __restrict__ Fc,
                             const double* __restrict__ Ft, const double* __restrict__ Fl, const double* __restrict__ rd,
                             const double* __restrict__ r0, const double* __restrict__ rt0,
@@ -228,50 +245,29 @@ __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const 
   V3 ri = ld3(r_all + 3 * i);
   double radi = M.rad_all[i];
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-  if constexpr (MX) {
-    const float a1f = (float)M.a1, a2f = (float)M.a2, radf = (float)radi, delf = (float)M.del;
-    for (int j = lo + lane; j < hi; j += 32) {
-      const double* f = F + 3 * (j - lo);
-      float Db[3][3];
-      if (j == i) {
-        const float d = a1f / radf;
-        s0 += (double)(delf * d * (float)f[0]);
-        s1 += (double)(delf * d * (float)f[1]);
-        s2 += (double)(delf * d * (float)f[2]);
-        continue;
-      }
-      rpy_block_f((float)(ri.x - r_all[3 * j]), (float)(ri.y - r_all[3 * j + 1]), (float)(ri.z - r_all[3 * j + 2]), radf,
-                  (float)M.rad_all[j], a1f, a2f, Db);
-      const float fx = (float)f[0], fy = (float)f[1], fz = (float)f[2];
-      s0 += (double)(delf * (Db[0][0] * fx + Db[0][1] * fy + Db[0][2] * fz));
-      s1 += (double)(delf * (Db[1][0] * fx + Db[1][1] * fy + Db[1][2] * fz));
-      s2 += (double)(delf * (Db[2][0] * fx + Db[2][1] * fy + Db[2][2] * fz));
-    }
-  } else {
   for (int j = lo + lane; j < hi; j += 32) {
-      const double* f = F + 3 * (j - lo);
-      if (j == i) {
-        double d = M.a1 / radi;
-        s0 = s0 + M.del * d * f[0];
-        s1 = s1 + M.del * d * f[1];
-        s2 = s2 + M.del * d * f[2];
-        continue;
-      }
-      V3 rj = ld3(r_all + 3 * j);
-      V3 sij{ri.x - rj.x, ri.y - rj.y, ri.z - rj.z};
-      double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
-      double s = sqrt(ssq);
-      double radj = M.rad_all[j];
-      double Db[3][3];
-      rpy_block(sij, ssq, s, radi, radj, M.a1, M.a2, Db);
-      for (int l = 0; l < 3; l++) {
-        double fl = f[l];
-        s0 = s0 + M.del * Db[0][l] * fl;
-        s1 = s1 + M.del * Db[1][l] * fl;
-        s2 = s2 + M.del * Db[2][l] * fl;
-      }
+    const double* f = F + 3 * (j - lo);
+    if (j == i) {
+      double d = M.a1 / radi;
+      s0 = s0 + M.del * d * f[0];
+      s1 = s1 + M.del * d * f[1];
+      s2 = s2 + M.del * d * f[2];
+      continue;
     }
-  }
+    V3 rj = ld3(r_all + 3 * j);
+    V3 sij{ri.x - rj.x, ri.y - rj.y, ri.z - rj.z};
+    double ssq = sij.x * sij.x + sij.y * sij.y + sij.z * sij.z;
+    double s = sqrt(ssq);
+    double radj = M.rad_all[j];
+    double Db[3][3];
+    rpy_block(sij, ssq, s, radi, radj, M.a1, M.a2, Db);
+    for (int l = 0; l < 3; l++) {
+      double fl = f[l];
+      s0 = s0 + M.del * Db[0][l] * fl;
+      s1 = s1 + M.del * Db[1][l] * fl;
+      s2 = s2 + M.del * Db[2][l] * fl;
+    }
+    }
   for (int o = 16; o > 0; o >>= 1) {
     s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, o);
     s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, o);
@@ -288,6 +284,96 @@ __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const 
     out[3 * li + 1] = x0[3 * li + 1] + rd[3 * i + 1] + s1;
     out[3 * li + 2] = x0[3 * li + 2] + rd[3 * i + 2] + s2;
   }
+}
+
+// Mixed path: the same drift in FP32 arithmetic.  Separations from the
+// double-float positions (hi differences plus lo differences), RPY blocks in
+// FP32, each lane's terms summed in runs of 32 with the runs added under
+// Kahan compensation (no FP64 in the pair loop: an FP64 operation costs as
+// much as ~64 FP32 ones on GB300); the lane totals are reduced in FP64.
+__global__ void k_translate_mx(DevModel M, const float4* __restrict__ qh, const float4* __restrict__ ql,
+                               const float4* __restrict__ qf, const double* __restrict__ rd,
+                               const double* __restrict__ r0, const double* __restrict__ rt0,
+                               const double* __restrict__ rl0, double* r1, double* rt1, double* rl1) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= M.n_D) return;
+  int lo, hi;
+  if (i < M.n) { lo = 0; hi = M.n; }
+  else if (i < M.n + M.n_tail) { lo = M.n; hi = M.n + M.n_tail; }
+  else { lo = M.n + M.n_tail; hi = M.n_D; }
+  const float4 hi_i = qh[i], lo_i = ql[i];
+  const float a1f = (float)M.a1, a2f = (float)M.a2, delf = (float)M.del;
+  float run[3] = {0.f, 0.f, 0.f}, ks[3] = {0.f, 0.f, 0.f}, kc[3] = {0.f, 0.f, 0.f};
+  int cnt = 0;
+  for (int j = lo + lane; j < hi; j += 32) {
+    const float4 f = qf[j];
+    if (j == i) {
+      const float d = delf * (a1f / hi_i.w);
+      run[0] += d * f.x;
+      run[1] += d * f.y;
+      run[2] += d * f.z;
+    } else {
+      const float4 hj = qh[j], lj = ql[j];
+      float Db[3][3];
+      rpy_block_f((hi_i.x - hj.x) + (lo_i.x - lj.x), (hi_i.y - hj.y) + (lo_i.y - lj.y),
+                  (hi_i.z - hj.z) + (lo_i.z - lj.z), hi_i.w, hj.w, a1f, a2f, Db);
+      run[0] += delf * (Db[0][0] * f.x + Db[0][1] * f.y + Db[0][2] * f.z);
+      run[1] += delf * (Db[1][0] * f.x + Db[1][1] * f.y + Db[1][2] * f.z);
+      run[2] += delf * (Db[2][0] * f.x + Db[2][1] * f.y + Db[2][2] * f.z);
+    }
+    if (++cnt == 32) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const float y = run[q] - kc[q], t = ks[q] + y;
+        kc[q] = (t - ks[q]) - y;
+        ks[q] = t;
+        run[q] = 0.f;
+      }
+      cnt = 0;
+    }
+  }
+  double s[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const float y = run[q] - kc[q], t = ks[q] + y;
+    s[q] = (double)t - (double)((t - ks[q]) - y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) s[q] = s[q] + __shfl_xor_sync(0xffffffffu, s[q], o);
+  }
+  if (lane == 0) {
+    double* out;
+    const double* x0;
+    int li;
+    if (i < M.n) { out = r1; x0 = r0; li = i; }
+    else if (i < M.n + M.n_tail) { out = rt1; x0 = rt0; li = i - M.n; }
+    else { out = rl1; x0 = rl0; li = i - M.n - M.n_tail; }
+    out[3 * li] = x0[3 * li] + rd[3 * i] + s[0];
+    out[3 * li + 1] = x0[3 * li + 1] + rd[3 * i + 1] + s[1];
+    out[3 * li + 2] = x0[3 * li + 2] + rd[3 * i + 2] + s[2];
+  }
+}
+
+// the move's forces in FP32, per bead of the tensor (chain | tails | LH)
+__global__ void k_forces_f32(int n, int nt, int nl, const double* __restrict__ F, const double* __restrict__ tF,
+                             const double* __restrict__ lF, float4* qf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n + nt + nl) return;
+  const double* p = i < n ? F + 3 * i : (i < n + nt ? tF + 3 * (i - n) : lF + 3 * (i - n - nt));
+  qf[i] = make_float4((float)p[0], (float)p[1], (float)p[2], 0.f);
+}
+
+// the tensor beads' positions as double-float pairs, radius in .w
+__global__ void k_rall_mirror(int nD, const double* __restrict__ r_all, const double* __restrict__ rad, float4* qh,
+                              float4* ql) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nD) return;
+  const double x = r_all[3 * i], y = r_all[3 * i + 1], z = r_all[3 * i + 2];
+  const float hx = (float)x, hy = (float)y, hz = (float)z;
+  qh[i] = make_float4(hx, hy, hz, (float)rad[i]);
+  ql[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.f);
 }
 
 __global__ void k_average(int n3, int nt3, int nl3, const double* F0, const double* T0, const double* tF0,
@@ -315,22 +401,31 @@ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 namespace bdk {
 
 void frames(const DevModel& M, DevState& S, cudaStream_t st) {
-  k_frames<<<1, kFrameThreads, 0, st>>>(M, S);
+  const int nb = M.n - 1 > 0 ? M.n - 1 : 0;
+  if (nb > 0) k_frames_dna<<<cdiv(nb, kFrameThreads), kFrameThreads, 0, st>>>(M, S);
+  const int tot = nb + M.n_tail + M.n_LH;
+  if (tot > 0) k_frames_angles<<<cdiv(tot, kFrameThreads), kFrameThreads, 0, st>>>(M, S);
 }
 
-void gather_rall(const DevModel& M, const DevState& X, double* r_all, cudaStream_t st) {
+void gather_rall(const DevModel& M, const DevState& X, double* r_all, const DevScratch* S, cudaStream_t st) {
   int tot = 3 * M.n_D;
   k_gather_rall<<<cdiv(tot, 256), 256, 0, st>>>(M.n, M.n_tail, M.n_LH, X.r, X.r_t, X.r_lh, r_all);
+  if (S) k_rall_mirror<<<cdiv(M.n_D, 256), 256, 0, st>>>(M.n_D, r_all, M.rad_all, S->qh, S->ql);
 }
 
 // X: state the move starts from; Y: receives the moved state.  r_all must
 // hold X's positions (the tensor is evaluated at the start configuration).
 void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const DevForces& Fo, const double* rr,
-                      const double* rd, const double* r_all, int mixed, cudaStream_t st) {
-  k_rotate<<<cdiv(M.n, 128), 128, 0, st>>>(M, Fo.T, rr, X.a, X.b, X.c, Y.a, Y.b, Y.c);
-  auto kt = mixed ? k_translate<true> : k_translate<false>;
-  kt<<<cdiv(M.n_D * 32, 256), 256, 0, st>>>(M, r_all, Fo.F, Fo.tF, Fo.lF, rd, X.r, X.r_t, X.r_lh, Y.r,
-                                                      Y.r_t, Y.r_lh);
+                      const double* rd, const double* r_all, int mixed, const DevScratch& S, cudaStream_t st) {
+  k_rotate<<<cdiv(M.n, 32), 32, 0, st>>>(M, Fo.T, rr, X.a, X.b, X.c, Y.a, Y.b, Y.c);  // FP64: one warp per SM
+  if (mixed) {
+    k_forces_f32<<<cdiv(M.n_D, 256), 256, 0, st>>>(M.n, M.n_tail, M.n_LH, Fo.F, Fo.tF, Fo.lF, S.qf);
+    k_translate_mx<<<cdiv(M.n_D * 32, 256), 256, 0, st>>>(M, S.qh, S.ql, S.qf, rd, X.r, X.r_t, X.r_lh, Y.r, Y.r_t,
+                                                           Y.r_lh);
+  } else {
+    k_translate<<<cdiv(M.n_D * 32, 256), 256, 0, st>>>(M, r_all, Fo.F, Fo.tF, Fo.lF, rd, X.r, X.r_t, X.r_lh, Y.r,
+                                                        Y.r_t, Y.r_lh);
+  }
 }
 
 void average_forces(const DevModel& M, const DevForces& A, const DevForces& B, DevForces& o, cudaStream_t st) {
