@@ -301,6 +301,8 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   const int npos = n + nt + nL + nlhc * M.n_lh_g;
   addD((nt + 4 * (size_t)M.Nq + 1) / 2); addD(2 * (size_t)npos); addD(2 * (size_t)npos);
   for (int q = 0; q < 3; q++) addD(2 * (size_t)M.n_D);
+  addD(4 * ((size_t)nt + nL));
+  addI(nL);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
   if (c->precision != BD_PREC_MIXED && c->precision != BD_PREC_FP64)
@@ -359,6 +361,8 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   c->S.qh = ar.take<float4>(M.n_D);
   c->S.ql = ar.take<float4>(M.n_D);
   c->S.qf = ar.take<float4>(M.n_D);
+  c->S.bond = ar.take<double>(4 * ((size_t)nt + nL));
+  int* d_lhp_idx = ar.take<int>(nL);
   c->S.ot = n; c->S.ol = n + nt; c->S.og = n + nt + nL; c->S.npos = npos;
   c->negpiv = ar.take<int>(1);
   cudaStream_t st = c->stream;
@@ -398,6 +402,15 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
       return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
     if (!tqf.empty() && cudaStreamSynchronize(st) != cudaSuccess)
       return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
+    std::vector<int> lhp(nL);
+    for (int b = 0; b < nL; b++) {  // as the bead-type lookup of the FP64 path: position in the molecule
+      const int idx = b % M.nlh;
+      lhp[b] = idx < M.n_lh_n ? idx : idx + M.n_lh_g;
+    }
+    if (nL && (cudaMemcpyAsync(d_lhp_idx, lhp.data(), nL * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+               cudaStreamSynchronize(st) != cudaSuccess))
+      return fail(set_error(BD_ERR_CUDA, "bd_create: upload failed"));
+    M.lh_p = d_lhp_idx;
     M.t_qf = d_tqf;
     M.core_pf = d_tqf + nt;
     M.core_qf = d_tqf + nt + 3 * nq;

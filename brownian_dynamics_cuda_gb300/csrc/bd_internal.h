@@ -78,6 +78,7 @@ struct DevModel {
   const float* t_qf;       // [n_tail] tail charges in FP32 (mixed path)
   const float* core_pf;    // [3 Nq] core_pos in FP32 (mixed path)
   const float* core_qf;    // [Nq] core_q in FP32 (mixed path)
+  const int* lh_p;         // [n_LH] bead-type parameter index of each LH bead
   int tails_by_core;       // tail t belongs to core t / n_t (or to none): anchored-tail scans per core
 };
 
@@ -112,6 +113,7 @@ struct DevScratch {
   // mixed path: the move's start positions as double-float pairs (radius in
   // qh.w) and the move's forces in FP32, per bead of the tensor
   float4 *qh, *ql, *qf;
+  double* bond;  // [4 (n_tail + n_LH)] mixed path: per-bead bonded force and energy of tails, LH beads
 };
 
 namespace bdk {

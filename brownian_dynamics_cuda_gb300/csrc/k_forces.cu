@@ -40,6 +40,20 @@ __device__ __forceinline__ V3 site(const DevState& X, int bead, const double* p)
   return body(ld3(X.r + 3 * bead), ld3(X.a + 3 * bead), ld3(X.b + 3 * bead), ld3(X.c + 3 * bead), p);
 }
 
+// Mixed path: a position as a double-float pair (hi, lo) of FP32 xyz.
+struct PF {
+  float4 h, l;
+};
+__device__ __forceinline__ PF ldpf(const DevScratch& S, int i) { return PF{S.ph[i], S.pl[i]}; }
+// a - b
+__device__ __forceinline__ float3 sepf(const PF& a, const PF& b) {
+  return make_float3((a.h.x - b.h.x) + (a.l.x - b.l.x), (a.h.y - b.h.y) + (a.l.y - b.l.y),
+                     (a.h.z - b.h.z) + (a.l.z - b.l.z));
+}
+__device__ __forceinline__ float3 crossf(const float3& u, const float3& v) {
+  return make_float3(fmaf(u.y, v.z, -u.z * v.y), fmaf(u.z, v.x, -u.x * v.z), fmaf(u.x, v.y, -u.y * v.x));
+}
+
 // deterministic warp sum (fixed butterfly order)
 __device__ __forceinline__ double wsum(double v) {
   for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
@@ -65,6 +79,48 @@ __device__ void bsum(double (&v)[NV], double* sm /* [32*NV] */) {
       for (int q = 0; q < nw; q++) s = s + sm[q * NV + k];
       v[k] = s;
     }
+  }
+  __syncthreads();
+}
+
+// Double-float (hi, lo) addition in FP32 (two-sum, then renormalised).
+__device__ __forceinline__ void df_add(float& h, float& l, float h2, float l2) {
+  const float s = h + h2, bb = s - h, e = (h - (s - bb)) + (h2 - bb);
+  const float t = e + l + l2;
+  h = s + t;
+  l = t - (h - s);
+}
+
+// Deterministic block sum of NV double-float values per thread, in FP32
+// two-sum arithmetic (fixed butterfly, then warps in order); the FP64
+// totals are valid in thread 0.  sm: 32 * NV doubles.
+template <int NV>
+__device__ void bsum_df(float (&h)[NV], float (&l)[NV], double (&out)[NV], double* sm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, h[k], o), l2 = __shfl_xor_sync(0xffffffffu, l[k], o);
+      df_add(h[k], l[k], h2, l2);
+    }
+  float2* smf = reinterpret_cast<float2*>(sm);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) smf[w * NV + k] = make_float2(h[k], l[k]);
+  }
+  __syncthreads();
+  double* res = sm + 16 * NV;  // past the float2 table of up to 32 warps
+  if (threadIdx.x < NV) {
+    const int k = threadIdx.x;
+    float H = 0.f, L = 0.f;
+    for (int q = 0; q < nw; q++) df_add(H, L, smf[q * NV + k].x, smf[q * NV + k].y);
+    res[k] = (double)H + (double)L;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = res[k];
   }
   __syncthreads();
 }
@@ -364,15 +420,15 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
 // 32 pairs, then FP64.
 constexpr int kCCFlush = 32;
 
-__global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevState X, double* slots) {
+__global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevState X, DevScratch S, double* slots) {
   extern __shared__ double sm[];
   const int I = blockIdx.x, J = blockIdx.y;
   double* out = slots + ((size_t)I * M.n_c + J) * 10;
   if (I >= J) return;
   const int i = M.core_bead[I], j = M.core_bead[J];
-  const V3 ri = ld3(X.r + 3 * i), rj = ld3(X.r + 3 * j);
-  const double d0 = sqrt((rj.x - ri.x) * (rj.x - ri.x) + (rj.y - ri.y) * (rj.y - ri.y) + (rj.z - ri.z) * (rj.z - ri.z));
-  if (d0 > 25.0 || !chain_ok(M, i) || !chain_ok(M, j)) {
+  // far-pair test and the centre offset in FP32, from the double-float mirror
+  const float3 oij = sepf(ldpf(S, i), ldpf(S, j));  // r_i - r_j
+  if (oij.x * oij.x + oij.y * oij.y + oij.z * oij.z > 625.f || !chain_ok(M, i) || !chain_ok(M, j)) {
     if (threadIdx.x < 10) out[threadIdx.x] = 0.0;
     return;
   }
@@ -386,10 +442,10 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevStat
   double* red = sm + (14 * Nq + 1) / 2;
   const V3 ai = ld3(X.a + 3 * i), bi = ld3(X.b + 3 * i), ci = ld3(X.c + 3 * i);
   const V3 aj = ld3(X.a + 3 * j), bj = ld3(X.b + 3 * j), cj = ld3(X.c + 3 * j);
-  // sites relative to the pair's midpoint, in FP32: the two centre offsets
-  // in FP64 once, the frames converted once, the lever arms in FP32 (no
-  // FP64 per site)
-  const float oix = (float)(0.5 * (ri.x - rj.x)), oiy = (float)(0.5 * (ri.y - rj.y)), oiz = (float)(0.5 * (ri.z - rj.z));
+  // sites relative to the pair's midpoint, in FP32: the centre offset from
+  // the mirror, the frames converted once, the lever arms in FP32 (no FP64
+  // per site)
+  const float oix = 0.5f * oij.x, oiy = 0.5f * oij.y, oiz = 0.5f * oij.z;
   const float aix = (float)ai.x, aiy = (float)ai.y, aiz = (float)ai.z, bix = (float)bi.x, biy = (float)bi.y,
               biz = (float)bi.z, cix = (float)ci.x, ciy = (float)ci.y, ciz = (float)ci.z;
   const float ajx = (float)aj.x, ajy = (float)aj.y, ajz = (float)aj.z, bjx = (float)bj.x, bjy = (float)bj.y,
@@ -415,48 +471,57 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevStat
 #pragma unroll
   for (int q = 0; q < 10; q++) a[q] = 0.f, ks[q] = 0.f, kc[q] = 0.f;
   int cnt = 0;
-  for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
-    const int k = p / Nq, l = p - k * Nq;
-    const float zx = sIx[k] - sJx[l], zy = sIy[k] - sJy[l], zz = sIz[k] - sJz[l];
-    const float ssq = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
-    const float rinv = rsqrtf(ssq);
-    const float dd = ssq * rinv;
-    const float ex = expf(-kap * dd);
-    float e = qI[k] * qJ[l] * ex * rinv;          // k_e q_k q_l e^{-kappa d} / d
-    float g = e * fmaf(kap, dd, 1.f) * rinv;      // ... (kappa d + 1) / d^2
-    if (dd <= 8.f) {
-      const float sr = sg * rinv, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-      g = fmaf(kex * (12.f * sr12 - 6.f * sr6), rinv, g);
-      e = fmaf(kex, sr12 - sr6, e);
-    }
-    const float gz = g * rinv;
-    const float fx = gz * zx, fy = gz * zy, fz = gz * zz;
-    a[0] += fx; a[1] += fy; a[2] += fz;
-    a[3] = fmaf(lIy[k], fz, fmaf(-lIz[k], fy, a[3]));
-    a[4] = fmaf(lIz[k], fx, fmaf(-lIx[k], fz, a[4]));
-    a[5] = fmaf(lIx[k], fy, fmaf(-lIy[k], fx, a[5]));
-    a[6] = fmaf(-lJy[l], fz, fmaf(lJz[l], fy, a[6]));
-    a[7] = fmaf(-lJz[l], fx, fmaf(lJx[l], fz, a[7]));
-    a[8] = fmaf(-lJx[l], fy, fmaf(lJy[l], fx, a[8]));
-    a[9] += e;
-    if (++cnt == kCCFlush) {
-#pragma unroll
-      for (int q = 0; q < 10; q++) {
-        const float y = a[q] - kc[q], t = ks[q] + y;
-        kc[q] = (t - ks[q]) - y;
-        ks[q] = t;
-        a[q] = 0.f;
+  // warp w takes sites k = w, w + nw, ... of core I against all sites l of
+  // core J (lanes); the force and torque on I are summed per k first
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int k = threadIdx.x >> 5; k < Nq; k += nw) {
+    const float sx = sIx[k], sy = sIy[k], sz = sIz[k], qk = qI[k];
+    float fkx = 0.f, fky = 0.f, fkz = 0.f;
+    for (int l = lane; l < Nq; l += 32) {
+      const float zx = sx - sJx[l], zy = sy - sJy[l], zz = sz - sJz[l];
+      const float ssq = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+      const float rinv = rsqrtf(ssq);
+      const float dd = ssq * rinv;
+      const float ex = expf(-kap * dd);
+      float e = qk * qJ[l] * ex * rinv;             // k_e q_k q_l e^{-kappa d} / d
+      float g = e * fmaf(kap, dd, 1.f) * rinv;      // ... (kappa d + 1) / d^2
+      if (dd <= 8.f) {
+        const float sr = sg * rinv, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+        g = fmaf(kex * (12.f * sr12 - 6.f * sr6), rinv, g);
+        e = fmaf(kex, sr12 - sr6, e);
       }
-      cnt = 0;
+      const float gz = g * rinv;
+      const float fx = gz * zx, fy = gz * zy, fz = gz * zz;
+      fkx += fx; fky += fy; fkz += fz;
+      a[6] = fmaf(-lJy[l], fz, fmaf(lJz[l], fy, a[6]));
+      a[7] = fmaf(-lJz[l], fx, fmaf(lJx[l], fz, a[7]));
+      a[8] = fmaf(-lJx[l], fy, fmaf(lJy[l], fx, a[8]));
+      a[9] += e;
+      if (++cnt == kCCFlush) {
+#pragma unroll
+        for (int q = 0; q < 10; q++) {
+          const float y = a[q] - kc[q], t = ks[q] + y;
+          kc[q] = (t - ks[q]) - y;
+          ks[q] = t;
+          a[q] = 0.f;
+        }
+        cnt = 0;
+      }
     }
+    a[0] += fkx; a[1] += fky; a[2] += fkz;
+    a[3] = fmaf(lIy[k], fkz, fmaf(-lIz[k], fky, a[3]));
+    a[4] = fmaf(lIz[k], fkx, fmaf(-lIx[k], fkz, a[4]));
+    a[5] = fmaf(lIx[k], fky, fmaf(-lIy[k], fkx, a[5]));
   }
-  double v[10];
+  float vh[10], vl[10];
 #pragma unroll
   for (int q = 0; q < 10; q++) {
     const float y = a[q] - kc[q], t = ks[q] + y;
-    v[q] = (double)t - (double)((t - ks[q]) - y);
+    vh[q] = t;
+    vl[q] = -((t - ks[q]) - y);
   }
-  bsum<10>(v, red);
+  double v[10];
+  bsum_df<10>(vh, vl, v, red);
   if (threadIdx.x == 0) {
     out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
     out[3] = ai.x * v[3] + ai.y * v[4] + ai.z * v[5];
@@ -472,7 +537,7 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevStat
 // DNA/core (func.cpp:1355-1488): one warp per (linker bead d, core J).
 // Slot: force on the DNA bead (3), torque on the core (3), energy.
 template <bool MX>
-__global__ void k_dna_core(DevModel M, DevState X, double* slots) {
+__global__ void k_dna_core(DevModel M, DevState X, DevScratch S, double* slots) {
   int lane = threadIdx.x & 31;
   int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= M.n_dna * M.n_c) return;
@@ -480,10 +545,16 @@ __global__ void k_dna_core(DevModel M, DevState X, double* slots) {
   double* out = slots + (size_t)w * 7;
   int i = M.dna_bead[D], j = M.core_bead[J];
   V3 rd_ = ld3(X.r + 3 * i), rc = ld3(X.r + 3 * j);
-  int lo = i < j ? i : j, hi = i < j ? j : i;
-  V3 rl = ld3(X.r + 3 * lo), rh = ld3(X.r + 3 * hi);
-  double d0 = sqrt((rh.x - rl.x) * (rh.x - rl.x) + (rh.y - rl.y) * (rh.y - rl.y) + (rh.z - rl.z) * (rh.z - rl.z));
-  bool ok = !(d0 > 25.0) && chain_ok(M, i) && chain_ok(M, j);
+  bool ok;
+  if constexpr (MX) {  // far-pair test in FP32 from the double-float mirror
+    const float3 z = sepf(ldpf(S, i), ldpf(S, j));
+    ok = !(z.x * z.x + z.y * z.y + z.z * z.z > 625.f) && chain_ok(M, i) && chain_ok(M, j);
+  } else {
+    int lo = i < j ? i : j, hi = i < j ? j : i;
+    V3 rl = ld3(X.r + 3 * lo), rh = ld3(X.r + 3 * hi);
+    double d0 = sqrt((rh.x - rl.x) * (rh.x - rl.x) + (rh.y - rl.y) * (rh.y - rl.y) + (rh.z - rl.z) * (rh.z - rl.z));
+    ok = !(d0 > 25.0) && chain_ok(M, i) && chain_ok(M, j);
+  }
   if (!ok) {
     if (lane < 7) out[lane] = 0.0;
     return;
@@ -499,7 +570,8 @@ __global__ void k_dna_core(DevModel M, DevState X, double* slots) {
     const float kapf = (float)kap, kexf = (float)kex, sgf = (float)sg, qlk = (float)(ke * ql);
     const float acx = (float)ac.x, acy = (float)ac.y, acz = (float)ac.z, bcx = (float)bc.x, bcy = (float)bc.y,
                 bcz = (float)bc.z, ccx = (float)cc.x, ccy = (float)cc.y, ccz = (float)cc.z;
-    const float ox = (float)(rc.x - rd_.x), oy = (float)(rc.y - rd_.y), oz = (float)(rc.z - rd_.z);
+    const float3 o = sepf(ldpf(S, j), ldpf(S, i));  // core centre relative to the DNA bead
+    const float ox = o.x, oy = o.y, oz = o.z;
     float a[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int k = lane; k < M.Nq; k += 32) {
       const float c0 = M.core_pf[3 * k], c1 = M.core_pf[3 * k + 1], c2 = M.core_pf[3 * k + 2];
@@ -667,6 +739,63 @@ __device__ void chain_finish(const DevModel& M, const DevScratch& S, const doubl
   st3(out.F + 3 * j, V3{Fb.x + F.x, Fb.y + F.y, Fb.z + F.z});
   st3(out.T + 3 * j, V3{Tb.x + T.x, Tb.y + T.y, Tb.z + T.z});
   Eout[j] = Ech[j] + E;
+}
+
+// Mixed path: chain_finish with the slot sums spread over the CTA's threads
+// (FP64, many lanes per instruction instead of one thread walking every
+// slot) and folded into the block sum; same terms, another summation order.
+__device__ void chain_finish_mx(const DevModel& M, const DevScratch& S, const double* Fm, const double* Tm,
+                                const double* Ech, DevForces& out, double* Eout, int j, V3 F, V3 T, double E,
+                                double* red) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (M.type[j] == 0) {
+    const int D = j - M.core_rank[j] - 1;  // linker beads before j
+    for (int J = tid; J < M.n_c; J += nt) {
+      const double* s = S.dc + ((size_t)D * M.n_c + J) * 7;
+      F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
+    }
+  } else {
+    const int J = M.core_rank[j];
+    for (int K = tid; K < M.n_c; K += nt) {
+      if (K < J) {
+        const double* s = S.cc + ((size_t)K * M.n_c + J) * 10;
+        F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
+        T.x = T.x + s[6]; T.y = T.y + s[7]; T.z = T.z + s[8];
+      } else if (K > J) {
+        const double* s = S.cc + ((size_t)J * M.n_c + K) * 10;
+        F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
+        T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
+        E = E + s[9];
+      }
+    }
+    for (int D = tid; D < M.n_dna; D += nt) {
+      const double* s = S.dc + ((size_t)D * M.n_c + J) * 7;
+      F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
+      T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
+      E = E + s[6];
+    }
+    for (int I = tid; I < M.n_lhcore; I += nt) {
+      const double* s = S.gc + ((size_t)I * M.n_c + J) * 10;
+      F.x = F.x - s[0]; F.y = F.y - s[1]; F.z = F.z - s[2];
+      T.x = T.x + s[6]; T.y = T.y + s[7]; T.z = T.z + s[8];
+    }
+    const int lc = M.core_lh[J];
+    if (lc >= 0) {
+      for (int L = tid; L < M.n_c; L += nt) {
+        const double* s = S.gc + ((size_t)lc * M.n_c + L) * 10;
+        F.x = F.x + s[0]; F.y = F.y + s[1]; F.z = F.z + s[2];
+        T.x = T.x + s[3]; T.y = T.y + s[4]; T.z = T.z + s[5];
+        E = E + s[9];
+      }
+    }
+  }
+  double v[7] = {F.x, F.y, F.z, T.x, T.y, T.z, E};
+  bsum<7>(v, red);
+  if (tid != 0) return;
+  V3 Fb = ld3(Fm + 3 * j), Tb = ld3(Tm + 3 * j);
+  st3(out.F + 3 * j, V3{Fb.x + v[0], Fb.y + v[1], Fb.z + v[2]});
+  st3(out.T + 3 * j, V3{Tb.x + v[3], Tb.y + v[4], Tb.z + v[5]});
+  Eout[j] = Ech[j] + v[6];
 }
 
 constexpr int kGatherThreads = 256;
@@ -1008,19 +1137,6 @@ __global__ void k_mirror(DevModel M, DevState X, float4* ph, float4* pl, int npo
   pl[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.f);
 }
 
-struct PF {
-  float4 h, l;
-};
-__device__ __forceinline__ PF ldpf(const DevScratch& S, int i) { return PF{S.ph[i], S.pl[i]}; }
-// a - b
-__device__ __forceinline__ float3 sepf(const PF& a, const PF& b) {
-  return make_float3((a.h.x - b.h.x) + (a.l.x - b.l.x), (a.h.y - b.h.y) + (a.l.y - b.l.y),
-                     (a.h.z - b.h.z) + (a.l.z - b.l.z));
-}
-__device__ __forceinline__ float3 crossf(const float3& u, const float3& v) {
-  return make_float3(fmaf(u.y, v.z, -u.z * v.y), fmaf(u.z, v.x, -u.x * v.z), fmaf(u.x, v.y, -u.y * v.x));
-}
-
 // force on particle 1 from particle 2, d = c1 - c2; qq = k_e q1 q2
 template <bool DH, bool LJ>
 __device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float sig, float3 d, float& E) {
@@ -1040,6 +1156,25 @@ __device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float si
   const float w = t / dd;
   return make_float3(clamp09f(w * d.x), clamp09f(w * d.y), clamp09f(w * d.z));
 }
+
+// s = start, start + step, ... split as s = hi n + lo, advanced without a
+// division per step (an integer division costs several conversion
+// instructions).
+struct Idx2 {
+  int s, hi, lo, dh, dl, n;
+  __device__ Idx2(int start, int step, int n_) : s(start), n(n_) {
+    hi = start / n_;
+    lo = start - hi * n_;
+    dh = step / n_;
+    dl = step - dh * n_;
+  }
+  __device__ void next() {
+    s += dh * n + dl;
+    hi += dh;
+    lo += dl;
+    if (lo >= n) lo -= n, hi++;
+  }
+};
 
 // Partial sums of force, world torque and energy: runs of up to 32 terms in
 // plain FP32, the runs added with Kahan compensation (still FP32: an FP64
@@ -1092,19 +1227,19 @@ __device__ void load_lhf(const DevModel& M, LHf& P) {
   __syncthreads();
 }
 
-// Tail beads, one warp each (func.cpp:1809-1917, 2343-2476 for the LH side).
-__global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
-  __shared__ LHf P;
-  load_lhf(M, P);
-  const int lane = threadIdx.x & 31;
-  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Bonded terms and the anchor of each tail bead (func.cpp:1809-1862), FP64,
+// one thread per bead: on GB300 an FP64 warp instruction costs the same
+// with one active lane as with 32, so these per-bead terms are taken out
+// of the one-warp-per-bead pair kernel.
+__global__ void k_tail_bonded_mx(DevModel M, DevState X, DevScratch S) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.n_tail) return;
   V3 rt = ld3(X.r_t + 3 * t);
   V3 F{0.0, 0.0, 0.0};
   double E = 0.0;
   const int* grp = M.t_grp;
   const int nt = M.n_tail;
-  if (lane == 0) {  // bonded terms and the anchor, as the FP64 path
+  {
     if (t >= 1 && grp[t - 1] == grp[t]) acc(F, stretch_f2(M.h_t[t - 1], ld3(X.r_t + 3 * t - 3), rt, M.lo_t[t - 1]));
     if (t + 1 < nt && grp[t] == grp[t + 1]) acc(F, stretch_f1(M.h_t[t], rt, ld3(X.r_t + 3 * t + 3), M.lo_t[t], E));
     for (int s = t - 2; s <= t; s++) {
@@ -1124,6 +1259,27 @@ __global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces
       V3 st{rt.x - ro.x, rt.y - ro.y, rt.z - ro.z};
       F.x = F.x - M.h * st.x; F.y = F.y - M.h * st.y; F.z = F.z - M.h * st.z;
     }
+  }
+  double* bt = S.bond + 4 * (size_t)t;
+  bt[0] = F.x; bt[1] = F.y; bt[2] = F.z; bt[3] = E;
+}
+
+// Tail beads, one warp each (func.cpp:1809-1917, 2343-2476 for the LH side).
+__global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
+  __shared__ LHf P;
+  load_lhf(M, P);
+  const int lane = threadIdx.x & 31;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (t >= M.n_tail) return;
+  V3 rt = ld3(X.r_t + 3 * t);
+  V3 F{0.0, 0.0, 0.0};
+  double E = 0.0;
+  const int* grp = M.t_grp;
+  const int nt = M.n_tail;
+  if (lane == 0) {  // bonded terms and the anchor (k_tail_bonded_mx)
+    const double* bt = S.bond + 4 * (size_t)t;
+    F = V3{bt[0], bt[1], bt[2]};
+    E = bt[3];
   }
   const float ke = (float)M.k_e, kap = (float)M.debye, kex = (float)M.k_ex;
   const float qt = ke * M.t_qf[t];
@@ -1147,13 +1303,13 @@ __global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces
   }
   if (M.t_fix[t] == 0) {  // LH beads and globular heads on free tail beads (energies on their side)
     for (int b = lane; b < M.n_LH; b += 32) {
-      int p = lh_param(M, b);
+      int p = M.lh_p[b];
       A.force(pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], sepf(pt, ldpf(S, S.ol + b)), dummy));
       A.tick();
     }
-    for (int s = lane; s < M.n_lhcore * M.n_lh_g; s += 32) {
-      int m = s % M.n_lh_g;
-      A.force(pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + s)), dummy));
+    for (Idx2 x(lane, 32, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {
+      const int m = x.lo;
+      A.force(pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + x.s)), dummy));
       A.tick();
     }
   }
@@ -1166,28 +1322,27 @@ __global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces
   }
 }
 
-// Mobile LH beads, one warp each (func.cpp:2109-2398, 2588-2644, 2725-2777).
-__global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
-  __shared__ LHf P;
-  load_lhf(M, P);
-  const int lane = threadIdx.x & 31;
-  const int bI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Bonded terms and the globular-head anchor of each LH bead
+// (func.cpp:2109-2185, 2725-2777), FP64, one thread per bead (as
+// k_tail_bonded_mx).
+__global__ void k_lh_bonded_mx(DevModel M, DevState X, DevScratch S) {
+  const int bI = blockIdx.x * blockDim.x + threadIdx.x;
   if (bI >= M.n_LH) return;
   const int nL = M.n_LH, nlh = M.nlh;
   V3 rb = ld3(X.r_lh + 3 * bI);
-  const int pb = lh_param(M, bI);
+  const int pb = M.lh_p[bI];
   V3 F{0.0, 0.0, 0.0};
   double E = 0.0;
-  if (lane == 0) {  // bonded terms and the globular-head anchor, as the FP64 path
+  {
     if (bI >= 1) {
-      int p = lh_param(M, bI - 1);
+      int p = M.lh_p[bI - 1];
       if (M.LH_conn[p] == 1) acc(F, stretch_f2(M.LH_kstr[p], ld3(X.r_lh + 3 * bI - 3), rb, M.LH_streq[p]));
     }
     if (M.LH_conn[pb] == 1 && bI + 1 < nL) acc(F, stretch_f1(M.LH_kstr[pb], rb, ld3(X.r_lh + 3 * bI + 3), M.LH_streq[pb], E));
     for (int s = bI - 1; s <= bI + 1; s++) {
       if (s < 0 || s >= nL) continue;
       if (!((s % M.n_lh_c != 0) && (s % M.n_lh_c != M.n_lh_c - 1))) continue;
-      int ps = lh_param(M, s);
+      int ps = M.lh_p[s];
       V3 f1, f2, f3;
       double e = 0.0;
       bend3(M.LH_kben[ps], X.beta_lh[s], M.LH_betaeq[ps], ld3(X.r_lh + 3 * s - 3), ld3(X.r_lh + 3 * s),
@@ -1208,19 +1363,41 @@ __global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces o
       }
     }
   }
+  double* bt = S.bond + 4 * ((size_t)M.n_tail + bI);
+  bt[0] = F.x; bt[1] = F.y; bt[2] = F.z; bt[3] = E;
+}
+
+// Mobile LH beads, one warp each (func.cpp:2109-2398, 2588-2644, 2725-2777).
+__global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
+  __shared__ LHf P;
+  load_lhf(M, P);
+  const int lane = threadIdx.x & 31;
+  const int bI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (bI >= M.n_LH) return;
+  const int nL = M.n_LH, nlh = M.nlh;
+  V3 rb = ld3(X.r_lh + 3 * bI);
+  const int pb = M.lh_p[bI];
+  V3 F{0.0, 0.0, 0.0};
+  double E = 0.0;
+  if (lane == 0) {  // bonded terms and the globular-head anchor (k_lh_bonded_mx)
+    const double* bt = S.bond + 4 * ((size_t)M.n_tail + bI);
+    F = V3{bt[0], bt[1], bt[2]};
+    E = bt[3];
+  }
   const float ke = (float)M.k_e, kap = (float)M.debye, kex = (float)M.k_ex;
   const float qb = ke * P.q[pb];
   const PF pp = ldpf(S, S.ol + bI);
   FAcc A;
   A.init();
   float dummy = 0.f;
+  const int own0 = (bI / nlh) * nlh;
   for (int u = lane; u < nL; u += 32) {  // LH/LH (func.cpp:2190-2244); energy on the lower index
     if (u == bI) continue;
-    const int pu = lh_param(M, u);
+    const int pu = M.lh_p[u];
     const float sig = (P.hh[pb] + P.hh[pu]) * 0.5f;
     float e = 0.f;
     const float3 d = sepf(pp, ldpf(S, S.ol + u));
-    if (bI / nlh == u / nlh) {
+    if ((unsigned)(u - own0) < (unsigned)nlh) {  // same LH molecule
       int lo = bI < u ? bI : u, hi = bI < u ? u : bI;
       if (!(hi > lo + 1)) continue;
       A.force(pairf<false, true>(0.f, kap, kex, sig, d, e));
@@ -1240,10 +1417,10 @@ __global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces o
     A.tick();
   }
   const int own = bI / nlh;
-  for (int s = lane; s < M.n_lhcore * M.n_lh_g; s += 32) {  // other LHs' globular heads; energy on the core
-    int K = s / M.n_lh_g, m = s - K * M.n_lh_g;
+  for (Idx2 x(lane, 32, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {  // other LHs' globular heads; energy on the core
+    const int K = x.hi, m = x.lo;
     if (K == own) continue;
-    A.force(pairf<true, true>(qb * P.q[m], kap, kex, (P.hh[m] + P.hh[pb]) * 0.5f, sepf(pp, ldpf(S, S.og + s)), dummy));
+    A.force(pairf<true, true>(qb * P.q[m], kap, kex, (P.hh[m] + P.hh[pb]) * 0.5f, sepf(pp, ldpf(S, S.og + x.s)), dummy));
     A.tick();
   }
   A.finish();
@@ -1298,12 +1475,12 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
       A.tick();
     }
     for (int b = tid; b < M.n_LH; b += nt) {  // LH beads; energy on the LH side
-      int p = lh_param(M, b);
+      int p = M.lh_p[b];
       A.force(pairf<true, true>(qlk * P.q[p], kap, kex, P.hl[p], sepf(pj, ldpf(S, S.ol + b)), dummy));
       A.tick();
     }
-    for (int s = tid; s < M.n_lhcore * M.n_lh_g; s += nt) {  // globular heads; energy on the core side
-      int m = s % M.n_lh_g;
+    for (Idx2 x(tid, nt, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {  // globular heads; energy on the core side
+      const int m = x.lo, s = x.s;
       A.force(pairf<true, true>(qlk * P.q[m], kap, kex, P.hl[m], sepf(pj, ldpf(S, S.og + s)), dummy));
       A.tick();
     }
@@ -1312,8 +1489,8 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
     const int lc = M.core_lh[J];
     if (lc >= 0) {
       const int ng = M.n_lh_g;
-      for (int s = tid; s < ng * M.n; s += nt) {  // G-head vs linker DNA (func.cpp:2481-2522); energy here
-        int m = s / M.n, l = s - m * M.n;
+      for (Idx2 x(tid, nt, M.n); x.s < ng * M.n; x.next()) {  // G-head vs linker DNA (func.cpp:2481-2522); energy here
+        const int m = x.hi, l = x.lo;
         if (M.type[l] != 0) continue;
         const PF g = ldpf(S, S.og + lc * ng + m);
         const float3 f1 = pairf<true, true>(ke * P.q[m] * ql, kap, kex, P.hl[m], sepf(g, ldpf(S, l)), A.f[6]);
@@ -1321,8 +1498,8 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
         A.torque(crossf(sepf(g, pj), f1));
         A.tick();
       }
-      for (int s = tid; s < ng * M.n_tail; s += nt) {  // G-head vs tails (func.cpp:2403-2476)
-        int m = s / M.n_tail, t = s - m * M.n_tail;
+      for (Idx2 x(tid, nt, M.n_tail); x.s < ng * M.n_tail; x.next()) {  // G-head vs tails (func.cpp:2403-2476)
+        const int m = x.hi, t = x.lo;
         const PF g = ldpf(S, S.og + lc * ng + m);
         const float3 f1 = pairf<true, true>(ke * P.q[m] * M.t_qf[t], kap, kex, P.ht[m], sepf(g, ldpf(S, S.ot + t)),
                                             A.f[6]);
@@ -1330,10 +1507,10 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
         A.torque(crossf(sepf(g, pj), f1));
         A.tick();
       }
-      for (int s = tid; s < ng * M.n_LH; s += nt) {  // G-head vs other LHs' beads (func.cpp:2590-2644)
-        int m = s / M.n_LH, b = s - m * M.n_LH;
-        if (b / M.nlh == lc) continue;
-        int p2 = lh_param(M, b);
+      for (Idx2 x(tid, nt, M.n_LH); x.s < ng * M.n_LH; x.next()) {  // G-head vs other LHs' beads (func.cpp:2590-2644)
+        const int m = x.hi, b = x.lo;
+        if ((unsigned)(b - lc * M.nlh) < (unsigned)M.nlh) continue;
+        int p2 = M.lh_p[b];
         const PF g = ldpf(S, S.og + lc * ng + m);
         const float3 f1 = pairf<true, true>(ke * P.q[m] * P.q[p2], kap, kex, (P.hh[m] + P.hh[p2]) * 0.5f,
                                             sepf(g, ldpf(S, S.ol + b)), A.f[6]);
@@ -1398,14 +1575,14 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
       const float3 lever = sepf(pt, pj);
       const float qt = ke * M.t_qf[t0];
       for (int b = tid; b < M.n_LH; b += nt) {
-        int p = lh_param(M, b);
+        int p = M.lh_p[b];
         const float3 f2 = pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], sepf(pt, ldpf(S, S.ol + b)), dummy);
         A.force(f2);
         A.torque(crossf(lever, f2));
         A.tick();
       }
-      for (int s = tid; s < M.n_lhcore * M.n_lh_g; s += nt) {
-        int m = s % M.n_lh_g;
+      for (Idx2 x(tid, nt, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {
+        const int m = x.lo, s = x.s;
         const float3 f2 = pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + s)), dummy);
         A.force(f2);
         A.torque(crossf(lever, f2));
@@ -1419,7 +1596,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, 
   T.x += aj.x * A.s[3] + aj.y * A.s[4] + aj.z * A.s[5];
   T.y += bj.x * A.s[3] + bj.y * A.s[4] + bj.z * A.s[5];
   T.z += cj.x * A.s[3] + cj.y * A.s[4] + cj.z * A.s[5];
-  chain_finish(M, S, Fm, Tm, Ech, out, Eout, j, F, T, E, red);
+  chain_finish_mx(M, S, Fm, Tm, Ech, out, Eout, j, F, T, E, red);
 }
 
 // Total energy: chain, tail and LH shares in a fixed order.
@@ -1459,16 +1636,18 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   if (M.n_c > 1) {
     if (mixed) {
       size_t sm = (size_t)((14 * M.Nq + 1) / 2 + 32 * 10) * sizeof(double);
-      k_core_core_mx<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+      k_core_core_mx<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S, S.cc);
     } else {
       size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
       k_core_coreX<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
     }
     L++;
   }
-  if (M.n_dna > 0 && M.n_c > 0) { k_dna_coreX<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.dc); L++; }
+  if (M.n_dna > 0 && M.n_c > 0) { k_dna_coreX<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S, S.dc); L++; }
   if (M.n_lhcore > 0) { k_ghead_coreX<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc); L++; }
   if (mixed) {
+    if (M.n_tail > 0) { k_tail_bonded_mx<<<cdiv(M.n_tail, 32), 32, 0, st>>>(M, X, S); L++; }
+    if (M.n_LH > 0) { k_lh_bonded_mx<<<cdiv(M.n_LH, 32), 32, 0, st>>>(M, X, S); L++; }
     if (M.n_tail > 0) { k_tail_gather_mx<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, S, out, Et); L++; }
     if (M.n_LH > 0) { k_lh_gather_mx<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, S, out, El); L++; }
     k_chain_gather_mx<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
