@@ -144,7 +144,8 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   L += mixed ? 2 : 1;
   bool rebuild = (c->step_count % c->freq_rp) == 0;
   if (rebuild) {
-    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed);
+    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed ? c->S.qh : nullptr,
+                      mixed ? c->S.ql : nullptr);
     L++;
   }
   record(c, 1);
@@ -596,9 +597,10 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
 }
 
 static void assemble_now(bd_ctx* c) {
-  bdk::gather_rall(c->M, c->X, c->r_all, nullptr, c->stream);
+  const bool mixed = c->precision == BD_PREC_MIXED;
+  bdk::gather_rall(c->M, c->X, c->r_all, mixed ? &c->S : nullptr, c->stream);
   bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream,
-                    c->precision == BD_PREC_MIXED);
+                    mixed ? c->S.qh : nullptr, mixed ? c->S.ql : nullptr);
 }
 
 extern "C" int bd_diffusion_tensor(bd_ctx* c, double* D) {

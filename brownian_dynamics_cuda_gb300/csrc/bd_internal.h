@@ -129,9 +129,10 @@ void gather_rall(const DevModel& M, const DevState& X, double* r_all, const DevS
 // returns the number of kernels launched
 int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& scr, int mixed, cudaStream_t st);
 // rpy_chol.cu
-// df: mixed path, FP32 RPY blocks stored as double-float pairs (value, 0)
+// qh, ql (mixed path): the positions as double-float pairs (gather_rall's
+// mirror); FP32 RPY blocks stored as double-float pairs (value, 0)
 void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
-                  cudaStream_t st, bool df = false);
+                  cudaStream_t st, const float4* qh = nullptr, const float4* ql = nullptr);
 int potrf_fp64(int m, double* A, int lda, double* rd_acc, const double* p, double s2dt, int* d_negpiv,
                cudaStream_t st);
 size_t trmv_scratch_doubles(int m);

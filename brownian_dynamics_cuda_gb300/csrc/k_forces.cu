@@ -1265,12 +1265,18 @@ __global__ void k_tail_bonded_mx(DevModel M, DevState X, DevScratch S) {
 }
 
 // Tail beads, one warp each (func.cpp:1809-1917, 2343-2476 for the LH side).
-__global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
+constexpr int kTailTile = 256;
+__global__ void __launch_bounds__(256) k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out,
+                                                        double* Eout) {
   __shared__ LHf P;
+  __shared__ float4 th[kTailTile], tl[kTailTile];
+  __shared__ float tq[kTailTile];
+  __shared__ int tg[kTailTile];
   load_lhf(M, P);
   const int lane = threadIdx.x & 31;
-  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (t >= M.n_tail) return;
+  const int t_raw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const bool active = t_raw < M.n_tail;  // the CTA's warps share the staged tiles: none leaves early
+  const int t = active ? t_raw : M.n_tail - 1;
   V3 rt = ld3(X.r_t + 3 * t);
   V3 F{0.0, 0.0, 0.0};
   double E = 0.0;
@@ -1287,14 +1293,25 @@ __global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces
   FAcc A;
   A.init();
   float dummy = 0.f;
-  for (int u = lane; u < nt; u += 32) {  // tail/tail (func.cpp:1863-1891); energy on the lower index
-    if (u == t) continue;
-    int lo = t < u ? t : u, hi = t < u ? u : t;
-    if (!(grp[lo] != grp[hi] || hi > lo + 2)) continue;
-    float e = 0.f;
-    A.force(pairf<true, false>(qt * M.t_qf[u], kap, 0.f, 0.f, sepf(pt, ldpf(S, S.ot + u)), e));
-    if (t < u) A.f[6] += e;
-    A.tick();
+  const int gt = grp[t];
+  for (int base = 0; base < nt; base += kTailTile) {  // tail/tail (func.cpp:1863-1891); energy on the lower index
+    __syncthreads();
+    for (int x = threadIdx.x; x < kTailTile && base + x < nt; x += blockDim.x) {
+      th[x] = S.ph[S.ot + base + x];
+      tl[x] = S.pl[S.ot + base + x];
+      tq[x] = M.t_qf[base + x];
+      tg[x] = grp[base + x];
+    }
+    __syncthreads();
+    const int ue = min(nt, base + kTailTile);
+    for (int u = base + lane; u < ue; u += 32) {
+      const int x = u - base;
+      if (u == t || (tg[x] == gt && abs(u - t) <= 2)) continue;  // bonded neighbours of one tail
+      float e = 0.f;
+      A.force(pairf<true, false>(qt * tq[x], kap, 0.f, 0.f, sepf(pt, PF{th[x], tl[x]}), e));
+      if (t < u) A.f[6] += e;
+      A.tick();
+    }
   }
   const float ql = (float)M.q_l, sTL = (float)M.sTL;
   for (int q = lane; q < M.n_dna; q += 32) {  // linker DNA (func.cpp:1898-1917); energy here
@@ -1316,7 +1333,7 @@ __global__ void k_tail_gather_mx(DevModel M, DevState X, DevScratch S, DevForces
   A.finish();
   F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
   F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
-  if (lane == 0) {
+  if (lane == 0 && active) {
     st3(out.tF + 3 * t, F);
     Eout[t] = E;
   }
@@ -1368,12 +1385,16 @@ __global__ void k_lh_bonded_mx(DevModel M, DevState X, DevScratch S) {
 }
 
 // Mobile LH beads, one warp each (func.cpp:2109-2398, 2588-2644, 2725-2777).
-__global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out, double* Eout) {
+__global__ void __launch_bounds__(256) k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces out,
+                                                      double* Eout) {
   __shared__ LHf P;
+  __shared__ float4 th[kTailTile], tl[kTailTile];
+  __shared__ float tq[kTailTile];
   load_lhf(M, P);
   const int lane = threadIdx.x & 31;
-  const int bI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (bI >= M.n_LH) return;
+  const int b_raw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const bool active = b_raw < M.n_LH;  // the CTA's warps share the staged tiles: none leaves early
+  const int bI = active ? b_raw : M.n_LH - 1;
   const int nL = M.n_LH, nlh = M.nlh;
   V3 rb = ld3(X.r_lh + 3 * bI);
   const int pb = M.lh_p[bI];
@@ -1412,9 +1433,20 @@ __global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces o
     A.force(pairf<true, true>(qb * ql, kap, kex, P.hl[pb], sepf(pp, ldpf(S, M.dna_bead[q])), A.f[6]));
     A.tick();
   }
-  for (int t = lane; t < M.n_tail; t += 32) {  // tails; energy here
-    A.force(pairf<true, true>(qb * M.t_qf[t], kap, kex, P.ht[pb], sepf(pp, ldpf(S, S.ot + t)), A.f[6]));
-    A.tick();
+  for (int base = 0; base < M.n_tail; base += kTailTile) {  // tails; energy here
+    __syncthreads();
+    for (int x = threadIdx.x; x < kTailTile && base + x < M.n_tail; x += blockDim.x) {
+      th[x] = S.ph[S.ot + base + x];
+      tl[x] = S.pl[S.ot + base + x];
+      tq[x] = M.t_qf[base + x];
+    }
+    __syncthreads();
+    const int te = min(M.n_tail, base + kTailTile);
+    for (int t = base + lane; t < te; t += 32) {
+      const int x = t - base;
+      A.force(pairf<true, true>(qb * tq[x], kap, kex, P.ht[pb], sepf(pp, PF{th[x], tl[x]}), A.f[6]));
+      A.tick();
+    }
   }
   const int own = bI / nlh;
   for (Idx2 x(lane, 32, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {  // other LHs' globular heads; energy on the core
@@ -1426,7 +1458,7 @@ __global__ void k_lh_gather_mx(DevModel M, DevState X, DevScratch S, DevForces o
   A.finish();
   F.x += A.s[0]; F.y += A.s[1]; F.z += A.s[2]; E += A.s[6];
   F.x = wsum(F.x); F.y = wsum(F.y); F.z = wsum(F.z); E = wsum(E);
-  if (lane == 0) {
+  if (lane == 0 && active) {
     st3(out.lF + 3 * bI, F);
     Eout[bI] = E;
   }

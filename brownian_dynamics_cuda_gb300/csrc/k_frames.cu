@@ -290,49 +290,72 @@ __global__ void k_translate(DevModel M, const double* __restrict__ r_all, const 
 // double-float positions (hi differences plus lo differences), RPY blocks in
 // FP32, each lane's terms summed in runs of 32 with the runs added under
 // Kahan compensation (no FP64 in the pair loop: an FP64 operation costs as
-// much as ~64 FP32 ones on GB300); the lane totals are reduced in FP64.
-__global__ void k_translate_mx(DevModel M, const float4* __restrict__ qh, const float4* __restrict__ ql,
-                               const float4* __restrict__ qf, const double* __restrict__ rd,
-                               const double* __restrict__ r0, const double* __restrict__ rt0,
-                               const double* __restrict__ rl0, double* r1, double* rt1, double* rl1) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= M.n_D) return;
-  int lo, hi;
+// much as ~64 FP32 ones on GB300); the lane totals are reduced in FP64.  One
+// warp per bead, 8 beads per CTA; the other beads' positions and forces are
+// staged through shared memory in tiles shared by the CTA's warps.
+constexpr int kTrTile = 256;
+__device__ __forceinline__ void species_range(const DevModel& M, int i, int& lo, int& hi) {
   if (i < M.n) { lo = 0; hi = M.n; }
   else if (i < M.n + M.n_tail) { lo = M.n; hi = M.n + M.n_tail; }
   else { lo = M.n + M.n_tail; hi = M.n_D; }
-  const float4 hi_i = qh[i], lo_i = ql[i];
+}
+__global__ void __launch_bounds__(256) k_translate_mx(DevModel M, const float4* __restrict__ qh,
+                                                      const float4* __restrict__ ql, const float4* __restrict__ qf,
+                                                      const double* __restrict__ rd, const double* __restrict__ r0,
+                                                      const double* __restrict__ rt0, const double* __restrict__ rl0,
+                                                      double* r1, double* rt1, double* rl1) {
+  __shared__ float4 sh[kTrTile], sl[kTrTile], sf[kTrTile];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i0 = blockIdx.x * 8, i = i0 + warp;
+  const bool active = i < M.n_D;
+  int lo = 0, hi = 0, clo, chi, tmp;
+  if (active) species_range(M, i, lo, hi);
+  species_range(M, i0, clo, tmp);                      // the CTA's beads span [clo, chi)
+  species_range(M, min(i0 + 7, M.n_D - 1), tmp, chi);
+  const float4 hi_i = active ? qh[i] : make_float4(0.f, 0.f, 0.f, 1.f), lo_i = active ? ql[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float a1f = (float)M.a1, a2f = (float)M.a2, delf = (float)M.del;
   float run[3] = {0.f, 0.f, 0.f}, ks[3] = {0.f, 0.f, 0.f}, kc[3] = {0.f, 0.f, 0.f};
   int cnt = 0;
-  for (int j = lo + lane; j < hi; j += 32) {
-    const float4 f = qf[j];
-    if (j == i) {
-      const float d = delf * (a1f / hi_i.w);
-      run[0] += d * f.x;
-      run[1] += d * f.y;
-      run[2] += d * f.z;
-    } else {
-      const float4 hj = qh[j], lj = ql[j];
-      float Db[3][3];
-      rpy_block_f((hi_i.x - hj.x) + (lo_i.x - lj.x), (hi_i.y - hj.y) + (lo_i.y - lj.y),
-                  (hi_i.z - hj.z) + (lo_i.z - lj.z), hi_i.w, hj.w, a1f, a2f, Db);
-      run[0] += delf * (Db[0][0] * f.x + Db[0][1] * f.y + Db[0][2] * f.z);
-      run[1] += delf * (Db[1][0] * f.x + Db[1][1] * f.y + Db[1][2] * f.z);
-      run[2] += delf * (Db[2][0] * f.x + Db[2][1] * f.y + Db[2][2] * f.z);
+  for (int base = clo; base < chi; base += kTrTile) {
+    __syncthreads();
+    for (int x = threadIdx.x; x < kTrTile && base + x < chi; x += blockDim.x) {
+      sh[x] = qh[base + x];
+      sl[x] = ql[base + x];
+      sf[x] = qf[base + x];
     }
-    if (++cnt == 32) {
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const float y = run[q] - kc[q], t = ks[q] + y;
-        kc[q] = (t - ks[q]) - y;
-        ks[q] = t;
-        run[q] = 0.f;
+    __syncthreads();
+    if (!active) continue;
+    const int je = min(hi, base + kTrTile);
+    for (int j = max(lo, base) + lane; j < je; j += 32) {
+      const int x = j - base;
+      const float4 f = sf[x];
+      if (j == i) {
+        const float d = delf * (a1f / hi_i.w);
+        run[0] += d * f.x;
+        run[1] += d * f.y;
+        run[2] += d * f.z;
+      } else {
+        const float4 hj = sh[x], lj = sl[x];
+        float Db[3][3];
+        rpy_block_f((hi_i.x - hj.x) + (lo_i.x - lj.x), (hi_i.y - hj.y) + (lo_i.y - lj.y),
+                    (hi_i.z - hj.z) + (lo_i.z - lj.z), hi_i.w, hj.w, a1f, a2f, Db);
+        run[0] += delf * (Db[0][0] * f.x + Db[0][1] * f.y + Db[0][2] * f.z);
+        run[1] += delf * (Db[1][0] * f.x + Db[1][1] * f.y + Db[1][2] * f.z);
+        run[2] += delf * (Db[2][0] * f.x + Db[2][1] * f.y + Db[2][2] * f.z);
       }
-      cnt = 0;
+      if (++cnt == 32) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const float y = run[q] - kc[q], t = ks[q] + y;
+          kc[q] = (t - ks[q]) - y;
+          ks[q] = t;
+          run[q] = 0.f;
+        }
+        cnt = 0;
+      }
     }
   }
+  if (!active) return;
   double s[3];
 #pragma unroll
   for (int q = 0; q < 3; q++) {

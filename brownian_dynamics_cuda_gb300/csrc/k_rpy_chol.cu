@@ -58,26 +58,29 @@ __global__ void __launch_bounds__(256) k_rpy(int nD, const double* __restrict__ 
 // Mixed path: the same lower triangle from the FP32 form of the RPY block
 // (separations formed in FP64, then FP32), stored as the double-float pair
 // (value, 0).  No FP64 arithmetic beyond the separation.
-__global__ void __launch_bounds__(256) k_rpy_mx(int nD, const double* __restrict__ r, const double* __restrict__ rad,
-                                                double a1, double a2, float2* __restrict__ A, int lda) {
+// Mixed path: FP32 blocks from the double-float positions (hi differences
+// plus lo differences; radius in qh.w), no FP64 per pair; stored as (D, 0)
+// pairs.  The same separations and block formula as the mixed drift.
+__global__ void __launch_bounds__(256) k_rpy_mx(int nD, const float4* __restrict__ qh, const float4* __restrict__ ql,
+                                                float a1f, float a2f, float2* __restrict__ A, int lda) {
   int bi = blockIdx.y, bj = blockIdx.x;
   if (bj > bi) return;
   int i = bi * kRpyTile + threadIdx.x;
   if (i >= nD) return;
-  const V3 ri = ld3(r + 3 * i);
-  const float radi = (float)rad[i], a1f = (float)a1, a2f = (float)a2;
+  const float4 hi = qh[i], lo = ql[i];
   for (int jj = threadIdx.y; jj < kRpyTile; jj += blockDim.y) {
     int j = bj * kRpyTile + jj;
     if (j >= nD || j > i) continue;
     if (j == i) {
       for (int l = 0; l < 3; l++)
         for (int k = l; k < 3; k++)
-          A[(size_t)(3 * j + l) * lda + 3 * i + k] = make_float2((k == l) ? a1f / radi : 0.f, 0.f);
+          A[(size_t)(3 * j + l) * lda + 3 * i + k] = make_float2((k == l) ? a1f / hi.w : 0.f, 0.f);
       continue;
     }
-    const V3 rj = ld3(r + 3 * j);
+    const float4 hj = qh[j], lj = ql[j];
     float Db[3][3];
-    rpy_block_f((float)(ri.x - rj.x), (float)(ri.y - rj.y), (float)(ri.z - rj.z), radi, (float)rad[j], a1f, a2f, Db);
+    rpy_block_f((hi.x - hj.x) + (lo.x - lj.x), (hi.y - hj.y) + (lo.y - lj.y), (hi.z - hj.z) + (lo.z - lj.z), hi.w, hj.w,
+                a1f, a2f, Db);
     for (int l = 0; l < 3; l++) {
       float2* col = A + (size_t)(3 * j + l) * lda + 3 * i;
       for (int k = 0; k < 3; k++) col[k] = make_float2(Db[k][l], 0.f);
@@ -275,10 +278,11 @@ __global__ void k_trmv_sum(int m, int nchunk, const double* __restrict__ part, d
 namespace bdk {
 
 void rpy_assemble(int nD, const double* r_all, const double* rad, double a1, double a2, double* A, int lda,
-                  cudaStream_t st, bool df) {
+                  cudaStream_t st, const float4* qh, const float4* ql) {
   int nt = cdiv(nD, kRpyTile);
-  if (df)
-    k_rpy_mx<<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, reinterpret_cast<float2*>(A), lda);
+  if (qh)
+    k_rpy_mx<<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, qh, ql, (float)a1, (float)a2,
+                                                         reinterpret_cast<float2*>(A), lda);
   else
     k_rpy<<<dim3(nt, nt), dim3(kRpyTile, 8), 0, st>>>(nD, r_all, rad, a1, a2, A, lda);
 }
