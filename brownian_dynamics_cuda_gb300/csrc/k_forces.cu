@@ -799,6 +799,12 @@ __device__ void chain_finish_mx(const DevModel& M, const DevScratch& S, const do
 }
 
 constexpr int kGatherThreads = 256;
+// FP64 thread-per-bead kernels: few beads per CTA, so that the CTAs spread
+// over many SMs (FP64 throughput is per SM)
+#ifndef BD_FP64_BEAD_THREADS
+#define BD_FP64_BEAD_THREADS 32
+#endif
+constexpr int kBeadThreads = BD_FP64_BEAD_THREADS;
 
 template <bool MX>
 __global__ void __launch_bounds__(kGatherThreads) k_chain_gather(DevModel M, DevState X, const double* Fm,
@@ -1465,13 +1471,18 @@ __global__ void __launch_bounds__(256) k_lh_gather_mx(DevModel M, DevState X, De
 }
 
 // Chain beads, one CTA each.
-__global__ void __launch_bounds__(kGatherThreads) k_chain_gather_mx(DevModel M, DevState X, const double* Fm,
-                                                                   const double* Tm, const double* Ech, DevScratch S,
-                                                                   DevForces out, double* Eout) {
+// One CTA per chain bead, beads[blockIdx.x]: launched once over the linker
+// DNA beads (kGatherThreads threads) and once over the cores, whose pair
+// lists (globular heads, anchored tails) are ~20x longer (kGatherCoreThreads).
+constexpr int kGatherCoreThreads = 512;
+__global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel M, DevState X, const double* Fm,
+                                                                       const double* Tm, const double* Ech,
+                                                                       DevScratch S, DevForces out, double* Eout,
+                                                                       const int* __restrict__ beads) {
   __shared__ double red[32 * 7];
   __shared__ LHf P;
   load_lhf(M, P);
-  const int j = blockIdx.x;
+  const int j = beads[blockIdx.x];
   const int tid = threadIdx.x, nt = blockDim.x;
   V3 rj = ld3(X.r + 3 * j), aj = ld3(X.a + 3 * j), bj = ld3(X.b + 3 * j), cj = ld3(X.c + 3 * j);
   V3 F{0.0, 0.0, 0.0}, T{0.0, 0.0, 0.0};
@@ -1663,7 +1674,7 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
 #undef KSEL
   if (M.n_lhcore > 0) { k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X); L++; }
   if (mixed) { k_mirror<<<cdiv(S.npos, 128), 128, 0, st>>>(M, X, S.ph, S.pl, S.npos); L++; }
-  k_chain_bonded<<<cdiv(M.n, 32), 32, 0, st>>>(M, X, Fm, Tm, Ebond);  // FP64: one warp per SM
+  k_chain_bonded<<<cdiv(M.n, kBeadThreads), kBeadThreads, 0, st>>>(M, X, Fm, Tm, Ebond);
   L++;
   if (M.n_c > 1) {
     if (mixed) {
@@ -1678,11 +1689,13 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   if (M.n_dna > 0 && M.n_c > 0) { k_dna_coreX<<<cdiv(M.n_dna * M.n_c * 32, 256), 256, 0, st>>>(M, X, S, S.dc); L++; }
   if (M.n_lhcore > 0) { k_ghead_coreX<<<cdiv(M.n_lhcore * M.n_c * 32, 256), 256, 0, st>>>(M, X, S.gc); L++; }
   if (mixed) {
-    if (M.n_tail > 0) { k_tail_bonded_mx<<<cdiv(M.n_tail, 32), 32, 0, st>>>(M, X, S); L++; }
-    if (M.n_LH > 0) { k_lh_bonded_mx<<<cdiv(M.n_LH, 32), 32, 0, st>>>(M, X, S); L++; }
+    if (M.n_tail > 0) { k_tail_bonded_mx<<<cdiv(M.n_tail, kBeadThreads), kBeadThreads, 0, st>>>(M, X, S); L++; }
+    if (M.n_LH > 0) { k_lh_bonded_mx<<<cdiv(M.n_LH, kBeadThreads), kBeadThreads, 0, st>>>(M, X, S); L++; }
     if (M.n_tail > 0) { k_tail_gather_mx<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, S, out, Et); L++; }
     if (M.n_LH > 0) { k_lh_gather_mx<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, S, out, El); L++; }
-    k_chain_gather_mx<<<M.n, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech);
+    if (M.n_dna > 0) k_chain_gather_mx<<<M.n_dna, kGatherThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech, M.dna_bead);
+    if (M.n_c > 0) k_chain_gather_mx<<<M.n_c, kGatherCoreThreads, 0, st>>>(M, X, Fm, Tm, Ebond, S, out, Ech, M.core_bead);
+    L += (M.n_dna > 0) + (M.n_c > 0) - 1;  // one chain launch is counted below
   } else {
     if (M.n_tail > 0) { k_tail_gatherX<<<cdiv(M.n_tail * 32, 256), 256, 0, st>>>(M, X, out, Et); L++; }
     if (M.n_LH > 0) { k_lh_gatherX<<<cdiv(M.n_LH * 32, 256), 256, 0, st>>>(M, X, out, El); L++; }

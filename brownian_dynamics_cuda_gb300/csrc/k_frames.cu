@@ -23,7 +23,10 @@ namespace {
 
 // FP64 throughout (GB300 runs ~2 FP64 operations per clock per SM), so the
 // beads are spread over many small CTAs: one warp per CTA, 32 beads each.
-constexpr int kFrameThreads = 32;
+#ifndef BD_FP64_BEAD_THREADS
+#define BD_FP64_BEAD_THREADS 32
+#endif
+constexpr int kFrameThreads = BD_FP64_BEAD_THREADS;
 
 // pass 1: DNA frames follow their bond; lengths (func.cpp:448-505)
 __global__ void __launch_bounds__(kFrameThreads) k_frames_dna(DevModel M, DevState S) {
@@ -440,7 +443,7 @@ void gather_rall(const DevModel& M, const DevState& X, double* r_all, const DevS
 // hold X's positions (the tensor is evaluated at the start configuration).
 void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const DevForces& Fo, const double* rr,
                       const double* rd, const double* r_all, int mixed, const DevScratch& S, cudaStream_t st) {
-  k_rotate<<<cdiv(M.n, 32), 32, 0, st>>>(M, Fo.T, rr, X.a, X.b, X.c, Y.a, Y.b, Y.c);  // FP64: one warp per SM
+  k_rotate<<<cdiv(M.n, kFrameThreads), kFrameThreads, 0, st>>>(M, Fo.T, rr, X.a, X.b, X.c, Y.a, Y.b, Y.c);
   if (mixed) {
     k_forces_f32<<<cdiv(M.n_D, 256), 256, 0, st>>>(M.n, M.n_tail, M.n_LH, Fo.F, Fo.tF, Fo.lF, S.qf);
     k_translate_mx<<<cdiv(M.n_D * 32, 256), 256, 0, st>>>(M, S.qh, S.ql, S.qf, rd, X.r, X.r_t, X.r_lh, Y.r, Y.r_t,
