@@ -33,8 +33,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "BD steps/s vs plain FP64 on 1 GB300 at <=1e-6 rel. error; replica-steps/s"
 # dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one
-# k_chol_step launch (panel 0's bulk update, 3N = 11,700) under ncu
-NCU_TRAFFIC_PER_ALG_BYTE = 1052.7 / 1047.9
+# k_chol_step launch under ncu (the fifth of a factorisation: panel 2 beside
+# the K = 256 bulk update by panels 0 and 1, 3N = 11,700: 1,057.9 MB of DRAM
+# traffic for 1,047.9 MB algorithmic)
+NCU_TRAFFIC_PER_ALG_BYTE = 1057.9 / 1047.9
 
 
 def peaks():
@@ -313,7 +315,8 @@ def run_ours(args):
                 "traffic": byt * NCU_TRAFFIC_PER_ALG_BYTE,
                 "traffic_source": "DRAM read+write per algorithmic byte of one ncu capture "
                                   "(profiles/k_chol_step_cfg1_mixed.md), times this step's algorithmic bytes",
-                "kernel": "k_chol_step (bulk tcgen05 trailing update of one or two panels, next panel in extra CTAs, double-float tile "
+                "kernel": "k_chol_step (every launch of the mixed factorisation: next panel in its own CTAs beside "
+                          "tcgen05 column and bulk trailing updates of one or two panels, double-float tile "
                           "read-modify-write), %d launches/step, avg %.3f ms" % (nk, ms_k / max(nk, 1)),
                 "algorithmic_bytes_per_step": byt,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
