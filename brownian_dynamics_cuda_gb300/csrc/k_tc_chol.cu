@@ -417,6 +417,9 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
 #ifndef BD_REST_PREFETCH
 #define BD_REST_PREFETCH 0  // L2 prefetch of the FP64 tile ahead of the epilogue (measured slower)
 #endif
+#ifndef BD_EPI_EVICT_FIRST
+#define BD_EPI_EVICT_FIRST 1  // L2 evict-first hint on the epilogue's tile loads and stores
+#endif
 #ifndef BD_EPI_AHEAD
 #define BD_EPI_AHEAD 8  // chunks of 8 columns whose old values are in flight per epilogue thread (4: 8 % slower bulk)
 #endif
@@ -695,6 +698,15 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
     constexpr int kEpC = 8, kEpN = 64 / kEpC, kEpS = BD_EPI_AHEAD;
     static_assert(kEpN % kEpS == 0, "slots must divide the chunks");
     const int q = warp & 3, ch = (warp - 2) >> 2;
+    // the tiles stream through L2 once per launch: marked first for eviction
+    // (BD_EPI_EVICT_FIRST), so the panel slices and the next launch's column
+    // stay resident
+    const uint64_t pol = sm100::policy_evict_first();
+    auto ld_tile = [&](const float2* a) { return BD_EPI_EVICT_FIRST ? sm100::ld_f2_hint(a, pol) : *a; };
+    auto st_tile = [&](float2* a, float2 v) {
+      if (BD_EPI_EVICT_FIRST) sm100::st_f2_hint(a, v, pol);
+      else *a = v;
+    };
     // columns [0, jcnt) of this thread's row of tile t are inside the matrix
     // and the lower triangle, at colp + j lda
     auto row_of = [&](int t, float2*& colp, int& jcnt) {
@@ -710,7 +722,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
     auto load_chunk = [&](float2 (&o)[kEpC], const float2* colp, int jcnt, int c) {
 #pragma unroll
       for (int j = 0; j < kEpC; j++)
-        o[j] = (kEpC * c + j < jcnt) ? colp[(size_t)(kEpC * c + j) * lda] : make_float2(0.f, 0.f);
+        o[j] = (kEpC * c + j < jcnt) ? ld_tile(colp + (size_t)(kEpC * c + j) * lda) : make_float2(0.f, 0.f);
     };
     float2* colp = A;
     int jcnt = 0;
@@ -748,7 +760,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
         }
 #pragma unroll
         for (int j = 0; j < kEpC; j++)
-          if (kEpC * c + j < jcnt) colp[(size_t)(kEpC * c + j) * lda] = df_sub(old[s2][j], v[j]);
+          if (kEpC * c + j < jcnt) st_tile(colp + (size_t)(kEpC * c + j) * lda, df_sub(old[s2][j], v[j]));
         if (c + kEpS < kEpN) load_chunk(old[s2], colp, jcnt, c + kEpS);
         else if (more) load_chunk(old[s2], ncolp, njcnt, c + kEpS - kEpN);
       }
