@@ -91,6 +91,9 @@ constexpr int kLt = 36;              // row stride of the transposed 32 x 32 fac
 constexpr int kDpThreads = 256;
 constexpr size_t kDpSmem = (2 * (size_t)kT * kLd + 32 * kLt) * sizeof(float);
 
+#ifndef BD_DP_EVICT_FIRST
+#define BD_DP_EVICT_FIRST 1  // L2 evict-first hint on the panel's tile loads and (L, 0) stores
+#endif
 #ifndef DP_MARK
 #define DP_MARK(i)  // phase boundary of the panel CTAs (a timestamp hook for profiling builds)
 #endif
@@ -254,10 +257,14 @@ __device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, flo
 // exactly, 8 + 8 + 8 significant bits) for every row of the tile.
 __device__ __forceinline__ void dp_emit(const float (&x)[32], int r, int nrows, int c0, int w, float2* g, int lda,
                                         unsigned char* ps) {
-  if (r < nrows) {
+  if (r < nrows) {  // read again only by the noise product after the factorisation (BD_DP_EVICT_FIRST)
+    const uint64_t pol = sm100::policy_evict_first();
 #pragma unroll
     for (int j = 0; j < 32; j++)
-      if (j < w) g[(size_t)j * lda + r] = make_float2(x[j], 0.f);
+      if (j < w) {
+        if (BD_DP_EVICT_FIRST) sm100::st_f2_hint(g + (size_t)j * lda + r, make_float2(x[j], 0.f), pol);
+        else g[(size_t)j * lda + r] = make_float2(x[j], 0.f);
+      }
   }
 #pragma unroll
   for (int q8 = 0; q8 < 4; q8++) {
@@ -311,6 +318,8 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
     const float4* ga = reinterpret_cast<const float4*>(A + (size_t)k0 * lda + k0);
     const float4* gx = reinterpret_cast<const float4*>(A + (size_t)k0 * lda + row0);
     const size_t ld4 = (size_t)lda / 2;
+    const uint64_t pol = sm100::policy_evict_first();  // read once (BD_DP_EVICT_FIRST)
+    auto ld_panel = [&](const float4* a) { return BD_DP_EVICT_FIRST ? sm100::ld_f4_hint(a, pol) : *a; };
 #pragma unroll 1
     for (int cb = warp; cb < kT / 8; cb += kDpThreads / 32) {
       const int c = 8 * cb + cc;
@@ -318,8 +327,8 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
 #pragma unroll
       for (int i = 0; i < 16; i++) {
         const int r = 8 * i + rr;
-        va[i] = (r + 1 >= c && r < kb && c < kb) ? ga[c * ld4 + r / 2] : make_float4(0.f, 0.f, 0.f, 0.f);
-        vx[i] = (r < nrows && c < kb) ? gx[c * ld4 + r / 2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        va[i] = (r + 1 >= c && r < kb && c < kb) ? ld_panel(ga + c * ld4 + r / 2) : make_float4(0.f, 0.f, 0.f, 0.f);
+        vx[i] = (r < nrows && c < kb) ? ld_panel(gx + c * ld4 + r / 2) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
       for (int i = 0; i < 16; i++) {
@@ -470,6 +479,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int t0 = tlo + cta * group, t1 = min(t0 + group, thi);
   const int nt = cdiv_d(m, kT);
+
   if (threadIdx.x == 0) {
     sm100::mbar_init(&bars->fullA, 1);
     sm100::mbar_init(&bars->emptyA, 1);
