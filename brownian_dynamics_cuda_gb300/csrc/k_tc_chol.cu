@@ -132,7 +132,7 @@ __device__ __forceinline__ void dp_block_update_n(float (*S)[kLd], int t, int c0
   for (int j = 0; j < 4; j++) lv[j] = *reinterpret_cast<const float4*>(lr[j] + qlo);
 #pragma unroll
   for (int i = 0; i < NI; i++) xv[i] = *reinterpret_cast<const float4*>(xr[i] + qlo);
-#pragma unroll 1
+#pragma unroll 2
   for (int q = qlo; q < qhi; q += 4) {
     const int qn = (q + 4 < qhi) ? q + 4 : q;
     float4 ln[4], xn[NI];
@@ -463,13 +463,14 @@ __device__ __forceinline__ void rest_tile(int t, int jlo, int mode, int nt, int&
 
 // `cta` is the CTA's index among the update CTAs.
 // NPAN = 1: one panel's update, the A operand resident per row of tiles.
-// NPAN = 2: two consecutive panels' updates (PS, PS2) in one read-modify-write
-// of the tile (K = 256): both operands streamed in four 96 KB chunks per
-// tile (panel, K-half) through the two stages.
+// NPAN = 2, 3: two or three consecutive panels' updates (PS, PS2, PS3) in one
+// read-modify-write of the tile (K = 256, 384): both operands streamed in
+// 2 NPAN chunks of 96 KB per tile (panel, K-half) through the two stages.
 template <int NPAN>
 __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int lda, int m, int jlo, int mode,
                                           int tlo, int thi, int group, int cta, const unsigned char* __restrict__ PS,
-                                          const unsigned char* __restrict__ PS2, int* err) {
+                                          const unsigned char* __restrict__ PS2, const unsigned char* __restrict__ PS3,
+                                          int* err) {
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   unsigned char* sA = sm;                 // 3 slices x 32 KB
   unsigned char* sB = sm + kTileBytes;    // 2 stages x (3 slices x 16 KB)
@@ -552,7 +553,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
         if (nfill[h] > 0) (void)sm100::mbar_wait(&bars->fullB[h], (nfill[h] - 1) & 1, kWaitLimit);
       if (nA > 0) (void)sm100::mbar_wait(&bars->fullA, (nA - 1) & 1, kWaitLimit);
       } else {
-        // two panels: chunk q = (panel q >> 1, K-half q & 1) of both operands
+        // NPAN panels: chunk q = (panel q >> 1, K-half q & 1) of both operands
         uint32_t nfill[2] = {0, 0};
         int ctot = 0;
         bool ok = true;
@@ -560,14 +561,14 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
           int I, J;
           rest_tile(t, jlo, mode, nt, I, J);
           const bool dg = I == J;
-          for (int q = 0; q < 4; q++) {
+          for (int q = 0; q < 2 * NPAN; q++) {
             const int st = ctot & 1;
             if (nfill[st] > 0) ok = sm100::mbar_wait(&bars->emptyB[st], (nfill[st] - 1) & 1, kWaitLimit);
             if (!ok || *abort_flag) {
               ok = false;
               break;
             }
-            const unsigned char* src = (q >> 1) ? PS2 : PS;
+            const unsigned char* src = (q >> 1) == 0 ? PS : ((q >> 1) == 1 ? PS2 : PS3);
             const int h = q & 1;
             unsigned char* sa = sm + st * (2 * kStageBytes);
             sm100::mbar_arrive_expect_tx(&bars->fullB[st], dg ? kStageBytes : 2 * kStageBytes);
@@ -665,7 +666,7 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
           }
           sm100::tc_fence_after();
           const uint32_t d = tmem + (uint32_t)(acc * kAccCols);
-          for (int q = 0; q < 4 && ok; q++) {
+          for (int q = 0; q < 2 * NPAN && ok; q++) {
             const int st = ctot & 1;
             ok = sm100::mbar_wait(&bars->fullB[st], nuse[st] & 1, kWaitLimit);
             if (!ok) break;
@@ -787,7 +788,8 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
 // jlo, panel slices ps (and ps2: two panels, K = 256), `group` tiles per CTA.
 struct UpdJob {
   const unsigned char* ps;
-  const unsigned char* ps2;
+  const unsigned char* ps2;  // second panel (K = 256) or null
+  const unsigned char* ps3;  // third panel (K = 384) or null
   int jlo, mode, tlo, thi, group, nctas;
 };
 struct StepArgs {
@@ -815,12 +817,15 @@ __global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_cons
   const int jn = b < a.job[0].nctas ? 0 : 1;
   if (jn) b -= a.job[0].nctas;
   const UpdJob& j = a.job[jn];
-  if (j.ps2)
+  if (j.ps3)
+    rest_body<3>(reinterpret_cast<unsigned char*>(smem4), a.A, a.lda, a.m, j.jlo, j.mode, j.tlo, j.thi, j.group, b,
+                 j.ps, j.ps2, j.ps3, a.err);
+  else if (j.ps2)
     rest_body<2>(reinterpret_cast<unsigned char*>(smem4), a.A, a.lda, a.m, j.jlo, j.mode, j.tlo, j.thi, j.group, b,
-                 j.ps, j.ps2, a.err);
+                 j.ps, j.ps2, nullptr, a.err);
   else
     rest_body<1>(reinterpret_cast<unsigned char*>(smem4), a.A, a.lda, a.m, j.jlo, j.mode, j.tlo, j.thi, j.group, b,
-                 j.ps, nullptr, a.err);
+                 j.ps, nullptr, nullptr, a.err);
 }
 
 // After the last panel: the diagonal factors L_kk from the side buffer into
@@ -838,9 +843,9 @@ __global__ void __launch_bounds__(256) k_diag_scatter(float2* A, int lda, int m,
 
 namespace bdk {
 
-// kBufs panel-slice buffers, panel p in buffer p % kBufs: a pair's bulk
-// update reads panels k and k + 1 while panel k + 2 is written
-constexpr int kBufs = 3;
+// kBufs panel-slice buffers, panel p in buffer p % kBufs: a triple's bulk
+// update reads panels k .. k + 2 while panel k + 3 is written
+constexpr int kBufs = 4;
 size_t mixed_panel_bytes(int m) {  // the slice buffers, then the diagonal factors
   return kBufs * (size_t)cdiv(m, kT) * kTileBytes + (size_t)cdiv(m, kT) * kT * kT * sizeof(float);
 }
@@ -891,10 +896,14 @@ static int rest_group(int tiles) {
 #ifndef BD_PAIR_MIN
 #define BD_PAIR_MIN 24  // pair while at least this many tile rows remain right of column k+2
 #endif
+#ifndef BD_TRIPLE_MIN
+#define BD_TRIPLE_MIN 40  // three panels per bulk pass while this many tile rows remain right of column k+3
+#endif
 namespace {
 struct Job {
   const unsigned char* ps = nullptr;
   const unsigned char* ps2 = nullptr;
+  const unsigned char* ps3 = nullptr;
   int jlo = 0, mode = kCol, tiles = 0, group = 1;
 };
 }  // namespace
@@ -922,10 +931,11 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     j.ps = psb(p), j.jlo = J, j.mode = kCol, j.tiles = nt - J, j.group = 1;
     return j;
   };
-  auto tri_job = [&](int p, bool two, int jlo) {
+  auto tri_job = [&](int p, int npan, int jlo) {  // panels p .. p + npan - 1 on the triangle from column jlo
     Job j;
     const int n = nt - jlo;
-    j.ps = psb(p), j.ps2 = two ? psb(p + 1) : nullptr, j.jlo = jlo, j.mode = kRowTri;
+    j.ps = psb(p), j.ps2 = npan > 1 ? psb(p + 1) : nullptr, j.ps3 = npan > 2 ? psb(p + 2) : nullptr;
+    j.jlo = jlo, j.mode = kRowTri;
     j.tiles = n > 0 ? n * (n + 1) / 2 : 0;
     j.group = rest_group(j.tiles);
     return j;
@@ -943,7 +953,8 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     for (int q = 0; q < 2; q++) {
       const Job& j = *js[q];
       UpdJob& u = a.job[q];
-      u.ps = j.ps, u.ps2 = j.ps2, u.jlo = j.jlo, u.mode = j.mode, u.tlo = 0, u.thi = j.tiles, u.group = j.group;
+      u.ps = j.ps, u.ps2 = j.ps2, u.ps3 = j.ps3, u.jlo = j.jlo, u.mode = j.mode, u.tlo = 0, u.thi = j.tiles,
+      u.group = j.group;
       u.nctas = j.tiles > 0 ? cdiv(j.tiles, j.group) : 0;
       grid += u.nctas;
     }
@@ -962,7 +973,7 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
         const Job& j = *js[q];
         if (j.tiles <= 0) continue;
         by += 16.0 * elems(j.jlo, j.mode == kCol ? j.jlo + 1 : nt);  // double-float tile read + write
-        fl += 6.0 * 2.0 * kT * kT * kT * j.tiles * (j.ps2 ? 2 : 1);  // BF16 tensor work issued
+        fl += 6.0 * 2.0 * kT * kT * kT * j.tiles * (j.ps3 ? 3 : (j.ps2 ? 2 : 1));  // BF16 tensor work issued
       }
       if (kbytes) *kbytes += by;
       if (kflop) *kflop += fl;
@@ -972,15 +983,23 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
   launch(0, none, none);  // panel 0 alone
   int k = 0;
   while (k + 1 < nt) {
-    if (nt - (k + 3) >= BD_PAIR_MIN) {
+    if (nt - (k + 4) >= BD_TRIPLE_MIN) {
+      launch(-1, col_job(k, k + 1), none);
+      launch(k + 1, col_job(k, k + 2), col_job(k, k + 3));
+      launch(-1, col_job(k + 1, k + 2), none);
+      launch(k + 2, col_job(k + 1, k + 3), none);
+      launch(-1, col_job(k + 2, k + 3), none);
+      launch(k + 3, tri_job(k, 3, k + 4), none);
+      k += 3;
+    } else if (nt - (k + 3) >= BD_PAIR_MIN) {
       launch(-1, col_job(k, k + 1), none);
       launch(k + 1, col_job(k, k + 2), none);
       launch(-1, col_job(k + 1, k + 2), none);
-      launch(k + 2, tri_job(k, true, k + 3), none);
+      launch(k + 2, tri_job(k, 2, k + 3), none);
       k += 2;
     } else {
       launch(-1, col_job(k, k + 1), none);
-      launch(k + 1, tri_job(k, false, k + 2), none);
+      launch(k + 1, tri_job(k, 1, k + 2), none);
       k += 1;
     }
   }
