@@ -296,8 +296,23 @@ __device__ __forceinline__ void dp_emit(const float (&x)[32], int r, int nrows, 
 // Runs in a CTA of kRestThreads (320) threads: 256 load, update and solve;
 // while warp 0 factors a diagonal block, warps 2..9 update the next block
 // column.  `b` is the CTA's index among the panel CTAs.
+// The previous panel's update of this panel's column, applied in the panel
+// CTA itself (so no separate launch precedes the panel): with panel p's
+// slices PSpre, D0 = L_kp L_kp^T for the diagonal tile and (tile CTAs)
+// D1 = L_ip L_kp^T for the CTA's tile, six BF16 products per K step on
+// tcgen05 into two 128-column TMEM accumulators.  The operands are streamed
+// in two K-halves into the memory the panel later uses for S, so the
+// products are complete before S is loaded; they are subtracted from S
+// after the load.  Every wait is bounded; a timeout records an error code.
+struct PreBars {
+  uint64_t full[2], done;
+  uint32_t slot;
+};
+constexpr int kPreStage = 2 * kTileSlices * kHalfBytes;  // one K-half of the A and B slices (96 KB)
+
 __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, int lda, int m, int k0, int kb, int tile0,
-                                            int b, unsigned char* PS, int* negpiv) {
+                                            int b, unsigned char* PS, int* negpiv, const unsigned char* PSpre,
+                                            int* err) {
   float (*S)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);  // rows 0..127 diagonal block, 128..255 tile
   float* T = reinterpret_cast<float*>(sm4) + 2 * kT * kLd;  // the current 32 x 32 factor, transposed
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -307,6 +322,73 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
   const int row0 = tile * kT;
   const int nrows = is_diag ? 0 : min(kT, m - row0);
   DP_MARK(0);
+  unsigned char* smA = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sm4) + 1023) & ~uintptr_t(1023));
+  PreBars* pbar = reinterpret_cast<PreBars*>(smA + 2 * kPreStage);
+  uint32_t tmem = 0;
+  bool pre_ok = true;
+  if (PSpre) {
+    if (tid == 0) {
+      sm100::mbar_init(&pbar->full[0], 1);
+      sm100::mbar_init(&pbar->full[1], 1);
+      sm100::mbar_init(&pbar->done, 1);
+      sm100::fence_mbar_init();
+    }
+    if (warp == 1) sm100::tmem_alloc(&pbar->slot, 2 * kT);
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    tmem = pbar->slot;
+    if (tid == 0) {
+      const unsigned char* gB = PSpre + (size_t)(tile0 - 1) * kTileBytes;  // this panel's tile row
+      const unsigned char* gA = PSpre + (size_t)tile * kTileBytes;
+      for (int h = 0; h < 2; h++) {  // stage h: [A: three 16 KB slice halves][B: three]
+        unsigned char* st = smA + h * kPreStage;
+        sm100::mbar_arrive_expect_tx(&pbar->full[h], (is_diag ? 1 : 2) * kTileSlices * kHalfBytes);
+        for (int s2 = 0; s2 < kTileSlices; s2++)
+          sm100::bulk_g2s(st + kTileSlices * kHalfBytes + s2 * kHalfBytes, gB + s2 * kSliceBytes + h * kHalfBytes,
+                          kHalfBytes, &pbar->full[h]);
+        if (!is_diag)
+          for (int s2 = 0; s2 < kTileSlices; s2++)
+            sm100::bulk_g2s(st + s2 * kHalfBytes, gA + s2 * kSliceBytes + h * kHalfBytes, kHalfBytes, &pbar->full[h]);
+      }
+      const uint32_t idesc = sm100::idesc_bf16_f32(128, 128);
+      const int pa[6] = {2, 1, 0, 1, 0, 0};  // (A slice, B slice) products, smallest first
+      const int pb[6] = {0, 1, 2, 0, 1, 0};
+      bool ok = true;
+      for (int h = 0; h < 2 && ok; h++) {
+        ok = sm100::mbar_wait(&pbar->full[h], 0, kWaitLimit);
+        if (!ok) break;
+        sm100::tc_fence_after();
+        const unsigned char* sa = smA + h * kPreStage;
+        const unsigned char* sb = sa + kTileSlices * kHalfBytes;
+#pragma unroll
+        for (int p = 0; p < 6; p++) {
+          const uint32_t b0 = sm100::smem_u32(sb + pa[p] * kHalfBytes), b1 = sm100::smem_u32(sb + pb[p] * kHalfBytes);
+          const uint32_t a0 = sm100::smem_u32(sa + pa[p] * kHalfBytes);
+#pragma unroll
+          for (int kk = 0; kk < 4; kk++) {
+            const uint32_t acc = (h | p | kk) != 0;
+            sm100::mma_bf16(tmem, sm100::desc_kmajor_sw128(b0 + kk * 32), sm100::desc_kmajor_sw128(b1 + kk * 32), idesc,
+                            acc);
+            if (!is_diag)
+              sm100::mma_bf16(tmem + kT, sm100::desc_kmajor_sw128(a0 + kk * 32), sm100::desc_kmajor_sw128(b1 + kk * 32),
+                              idesc, acc);
+          }
+        }
+      }
+      sm100::mma_commit(&pbar->done);
+      if (!ok) {
+        atomicExch(err, 6);
+        // copies still in flight land before their memory is reused
+        (void)sm100::mbar_wait(&pbar->full[0], 0, kWaitLimit);
+        (void)sm100::mbar_wait(&pbar->full[1], 0, kWaitLimit);
+      }
+    }
+    // the products read the stage memory: complete before S overwrites it
+    pre_ok = sm100::mbar_wait(&pbar->done, 0, kWaitLimit);
+    sm100::tc_fence_after();
+    if (!pre_ok && tid == 0) atomicExch(err, 7);
+  }
   if (work) {
     // two rows per 16-byte load; lane l takes rows 2 (l & 3) + {0, 1} of an
     // 8-row block and column l >> 2 of an 8-column block, so a warp reads
@@ -342,6 +424,29 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
     }
   }
   __syncthreads();
+  if (PSpre) {
+    if (pre_ok && warp < 8 && (warp < 4 || !is_diag)) {
+      // warp w reads TMEM lanes 32 (w % 4) ..: rows of D0 (w < 4) or D1
+      const int q = warp & 3, r = 32 * q + lane;
+      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (warp < 4 ? 0u : (uint32_t)kT);
+      float* row = warp < 4 ? S[r] : S[kT + r];
+#pragma unroll 1
+      for (int cc = 0; cc < kT; cc += 32) {
+        float v[32];
+        sm100::tmem_ld32(ta + cc, v);
+#pragma unroll
+        for (int k4 = 0; k4 < 8; k4++) {
+          float4* p4 = reinterpret_cast<float4*>(row + cc + 4 * k4);
+          float4 x = *p4;
+          x.x -= v[4 * k4], x.y -= v[4 * k4 + 1], x.z -= v[4 * k4 + 2], x.w -= v[4 * k4 + 3];
+          *p4 = x;
+        }
+      }
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) sm100::tmem_dealloc(tmem, 2 * kT);
+  }
   DP_MARK(1);
   const int nb = (kb + 31) >> 5;
   const int nrt = is_diag ? 0 : kT;  // tile rows solved (rows past the matrix are zero and stay zero)
@@ -796,6 +901,7 @@ struct StepArgs {
   float2* A;
   float* Ldg;           // this panel's diagonal factor
   unsigned char* PSp;   // this panel's slice buffer
+  const unsigned char* PSpre;  // the previous panel's slices: its update of this panel's column, or null
   int* negpiv;
   int* err;
   int lda, m, ndp, pk0, pkb;
@@ -810,7 +916,7 @@ __global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_cons
   extern __shared__ float4 smem4[];
   int b = (int)blockIdx.x;
   if (b < a.ndp) {
-    dpanel_body(smem4, a.A, a.Ldg, a.lda, a.m, a.pk0, a.pkb, a.pk0 / kT + 1, b, a.PSp, a.negpiv);
+    dpanel_body(smem4, a.A, a.Ldg, a.lda, a.m, a.pk0, a.pkb, a.pk0 / kT + 1, b, a.PSp, a.negpiv, a.PSpre, a.err);
     return;
   }
   b -= a.ndp;
@@ -879,22 +985,24 @@ static int rest_group(int tiles) {
 }
 
 // Right-looking with a lookahead of one panel, on one stream, no two kernels
-// at a time; every launch is one k_chol_step (panel CTAs and up to two
-// update jobs).  Panel p's slices live in buffer p % kBufs, L_kk in a side
-// buffer.
-// Single step k (panel k factored; columns > k hold the updates of panels
-// < k):
-//   1: panel k's update of column k+1;
-//   2: panel k+1 + panel k's update of the tiles right of column k+1.
-// Pair (k, k+1), while the trailing matrix is large: the bulk tiles get both
-// panels in one read-modify-write (K = 256), half the HBM traffic:
-//   1: panel k's update of column k+1;
-//   2: panel k+1 + panel k's update of column k+2;
-//   3: panel k+1's update of column k+2;
-//   4: panel k+2 + panels k and k+1 on the tiles right of column k+2.
+// at a time; every launch is one k_chol_step: panel pn in its own CTAs (which
+// first apply panel pn-1's update to column pn themselves) beside up to two
+// update jobs.  Panel p's slices live in buffer p % kBufs, L_kk in a side
+// buffer.  Invariant before the launch of panel k+1: panels <= k are
+// factored and column k+1 holds the updates of panels < k.
+// Single step: panel k+1 beside panel k's update of the tiles right of
+// column k+1 (K = 128).
+// Pair (k+1, k+2), while the trailing matrix is large: the bulk tiles get
+// both panels in one read-modify-write (K = 256), half the HBM traffic:
+//   1: panel k+1 beside panel k's update of column k+2;
+//   2: panel k+2 beside panels k and k+1 on the tiles right of column k+2.
+// Triple (k+1 .. k+3), while it is larger still (K = 384):
+//   1: panel k+1 beside panel k's updates of columns k+2 and k+3;
+//   2: panel k+2 beside panel k+1's update of column k+3;
+//   3: panel k+3 beside panels k .. k+2 on the tiles right of column k+3.
 // Returns the number of kernel launches.
 #ifndef BD_PAIR_MIN
-#define BD_PAIR_MIN 24  // pair while at least this many tile rows remain right of column k+2
+#define BD_PAIR_MIN 24  // pair while at least this many tile rows remain right of column k+2 (k: last factored)
 #endif
 #ifndef BD_TRIPLE_MIN
 #define BD_TRIPLE_MIN 40  // three panels per bulk pass while this many tile rows remain right of column k+3
@@ -940,13 +1048,16 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     j.group = rest_group(j.tiles);
     return j;
   };
-  auto launch = [&](int pn, const Job& j0, const Job& j1) {
+  // pn: the panel factored by this launch (-1: none); pre: panel pn - 1's
+  // update of column pn is applied by the panel CTAs themselves
+  auto launch = [&](int pn, const Job& j0, const Job& j1, bool pre) {
     StepArgs a{};
     a.A = A, a.negpiv = negpiv, a.err = err, a.lda = lda, a.m = m;
-    a.Ldg = Ld, a.PSp = PS;
+    a.Ldg = Ld, a.PSp = PS, a.PSpre = nullptr;
     if (pn >= 0) {
       a.ndp = nt - pn, a.pk0 = pn * kT, a.pkb = kb_of(pn);
       a.Ldg = Ld + (size_t)pn * kT * kT, a.PSp = psb(pn);
+      if (pre && pn > 0) a.PSpre = psb(pn - 1);
     }
     const Job* js[2] = {&j0, &j1};
     int grid = a.ndp;
@@ -968,7 +1079,7 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     L++;
     if (kbytes || kflop) {
       double by = pn >= 0 ? 16.0 * (double)(m - pn * kT) * kb_of(pn) : 0.0;  // panel read and written back
-      double fl = 0.0;
+      double fl = a.PSpre ? 6.0 * 2.0 * kT * kT * kT * (2 * (nt - pn) - 1) : 0.0;  // the panel CTAs' own products
       for (int q = 0; q < 2; q++) {
         const Job& j = *js[q];
         if (j.tiles <= 0) continue;
@@ -980,26 +1091,20 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     }
   };
   const Job none;
-  launch(0, none, none);  // panel 0 alone
+  launch(0, none, none, false);  // panel 0 alone
   int k = 0;
   while (k + 1 < nt) {
     if (nt - (k + 4) >= BD_TRIPLE_MIN) {
-      launch(-1, col_job(k, k + 1), none);
-      launch(k + 1, col_job(k, k + 2), col_job(k, k + 3));
-      launch(-1, col_job(k + 1, k + 2), none);
-      launch(k + 2, col_job(k + 1, k + 3), none);
-      launch(-1, col_job(k + 2, k + 3), none);
-      launch(k + 3, tri_job(k, 3, k + 4), none);
+      launch(k + 1, col_job(k, k + 2), col_job(k, k + 3), true);
+      launch(k + 2, col_job(k + 1, k + 3), none, true);
+      launch(k + 3, tri_job(k, 3, k + 4), none, true);
       k += 3;
     } else if (nt - (k + 3) >= BD_PAIR_MIN) {
-      launch(-1, col_job(k, k + 1), none);
-      launch(k + 1, col_job(k, k + 2), none);
-      launch(-1, col_job(k + 1, k + 2), none);
-      launch(k + 2, tri_job(k, 2, k + 3), none);
+      launch(k + 1, col_job(k, k + 2), none, true);
+      launch(k + 2, tri_job(k, 2, k + 3), none, true);
       k += 2;
     } else {
-      launch(-1, col_job(k, k + 1), none);
-      launch(k + 1, tri_job(k, 1, k + 2), none);
+      launch(k + 1, tri_job(k, 1, k + 2), none, true);
       k += 1;
     }
   }
