@@ -997,8 +997,8 @@ static int rest_group(int tiles) {
 //   1: panel k+1 beside panel k's update of column k+2;
 //   2: panel k+2 beside panels k and k+1 on the tiles right of column k+2.
 // Triple (k+1 .. k+3), while it is larger still (K = 384):
-//   1: panel k+1 beside panel k's updates of columns k+2 and k+3;
-//   2: panel k+2 beside panel k+1's update of column k+3;
+//   1: panel k+1 beside panel k's update of column k+2;
+//   2: panel k+2 beside panels k and k+1 on column k+3 (K = 256);
 //   3: panel k+3 beside panels k .. k+2 on the tiles right of column k+3.
 // Returns the number of kernel launches.
 #ifndef BD_PAIR_MIN
@@ -1034,9 +1034,9 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     }
     return e;
   };
-  auto col_job = [&](int p, int J) {
+  auto col_job = [&](int p, int J, int npan = 1) {  // panels p .. p + npan - 1 on column J
     Job j;
-    j.ps = psb(p), j.jlo = J, j.mode = kCol, j.tiles = nt - J, j.group = 1;
+    j.ps = psb(p), j.ps2 = npan > 1 ? psb(p + 1) : nullptr, j.jlo = J, j.mode = kCol, j.tiles = nt - J, j.group = 1;
     return j;
   };
   auto tri_job = [&](int p, int npan, int jlo) {  // panels p .. p + npan - 1 on the triangle from column jlo
@@ -1095,8 +1095,8 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
   int k = 0;
   while (k + 1 < nt) {
     if (nt - (k + 4) >= BD_TRIPLE_MIN) {
-      launch(k + 1, col_job(k, k + 2), col_job(k, k + 3), true);
-      launch(k + 2, col_job(k + 1, k + 3), none, true);
+      launch(k + 1, col_job(k, k + 2), none, true);
+      launch(k + 2, col_job(k, k + 3, 2), none, true);
       launch(k + 3, tri_job(k, 3, k + 4), none, true);
       k += 3;
     } else if (nt - (k + 3) >= BD_PAIR_MIN) {
