@@ -251,12 +251,13 @@ __device__ __forceinline__ void warp_chol32(float (&a)[32], int w, int lane, flo
   __syncwarp();
 }
 
-// Row r of L_ik, columns c0 .. c0 + 31 (x[j] = 0 past column w): (L, 0)
-// pairs into A (`g` = A at column c0 of the tile's row 0) for rows inside the
-// matrix, and the 16-byte chunks of the three BF16 slices (x = hi + mid + lo
-// exactly, 8 + 8 + 8 significant bits) for every row of the tile.
-__device__ __forceinline__ void dp_emit(const float (&x)[32], int r, int nrows, int c0, int w, float2* g, int lda,
-                                        unsigned char* ps) {
+// Row r of the CTA's rows of L_ik (row rs of the 128-row tile), columns
+// c0 .. c0 + 31 (x[j] = 0 past column w): (L, 0) pairs into A (`g` = A at
+// column c0 of the CTA's first row) for rows inside the matrix, and the
+// 16-byte chunks of the three BF16 slices (x = hi + mid + lo exactly,
+// 8 + 8 + 8 significant bits) for every row of the tile.
+__device__ __forceinline__ void dp_emit(const float (&x)[32], int r, int rs, int nrows, int c0, int w, float2* g,
+                                        int lda, unsigned char* ps) {
   if (r < nrows) {  // read again only by the noise product after the factorisation (BD_DP_EVICT_FIRST)
     const uint64_t pol = sm100::policy_evict_first();
 #pragma unroll
@@ -286,7 +287,7 @@ __device__ __forceinline__ void dp_emit(const float (&x)[32], int r, int nrows, 
       }
       hw[j2] = h2, mw[j2] = m2, lw[j2] = l2;
     }
-    const uint32_t off = swz_off(r, c0 + 8 * q8);
+    const uint32_t off = swz_off(rs, c0 + 8 * q8);
     *reinterpret_cast<uint4*>(ps + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *reinterpret_cast<uint4*>(ps + kSliceBytes + off) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
     *reinterpret_cast<uint4*>(ps + 2 * kSliceBytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
@@ -312,15 +313,17 @@ constexpr int kPreStage = 2 * kTileSlices * kHalfBytes;  // one K-half of the A 
 
 __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, int lda, int m, int k0, int kb, int tile0,
                                             int b, unsigned char* PS, int* negpiv, const unsigned char* PSpre,
-                                            int* err) {
+                                            int* err, int rpc) {
   float (*S)[kLd] = reinterpret_cast<float (*)[kLd]>(sm4);  // rows 0..127 diagonal block, 128..255 tile
   float* T = reinterpret_cast<float*>(sm4) + 2 * kT * kLd;  // the current 32 x 32 factor, transposed
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool work = tid < kDpThreads;
   const bool is_diag = b == 0;
-  const int tile = tile0 + b - 1;
-  const int row0 = tile * kT;
-  const int nrows = is_diag ? 0 : min(kT, m - row0);
+  // tile CTAs take rpc (128 or 64) rows of a tile: b - 1 = (tile - tile0) (128 / rpc) + part
+  const int parts = kT / rpc, part = is_diag ? 0 : (b - 1) % parts;
+  const int tile = tile0 + (is_diag ? 0 : (b - 1) / parts);
+  const int row0 = tile * kT + part * rpc;
+  const int nrows = is_diag ? 0 : max(0, min(rpc, m - row0));
   DP_MARK(0);
   unsigned char* smA = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sm4) + 1023) & ~uintptr_t(1023));
   PreBars* pbar = reinterpret_cast<PreBars*>(smA + 2 * kPreStage);
@@ -425,11 +428,13 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
   }
   __syncthreads();
   if (PSpre) {
-    if (pre_ok && warp < 8 && (warp < 4 || !is_diag)) {
-      // warp w reads TMEM lanes 32 (w % 4) ..: rows of D0 (w < 4) or D1
-      const int q = warp & 3, r = 32 * q + lane;
+    // warp w reads TMEM lanes 32 (w % 4) ..: rows of D0 (w < 4) or of D1
+    // (the CTA's part of the tile)
+    const int q = warp & 3;
+    if (pre_ok && warp < 8 && (warp < 4 || (!is_diag && (32 * q) / rpc == part))) {
+      const int r = 32 * q + lane;
       const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (warp < 4 ? 0u : (uint32_t)kT);
-      float* row = warp < 4 ? S[r] : S[kT + r];
+      float* row = warp < 4 ? S[r] : S[kT + r - part * rpc];
 #pragma unroll 1
       for (int cc = 0; cc < kT; cc += 32) {
         float v[32];
@@ -449,7 +454,7 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
   }
   DP_MARK(1);
   const int nb = (kb + 31) >> 5;
-  const int nrt = is_diag ? 0 : kT;  // tile rows solved (rows past the matrix are zero and stay zero)
+  const int nrt = is_diag ? 0 : rpc;  // tile rows solved (rows past the matrix are zero and stay zero)
   for (int jb = 0; jb < nb; jb++) {
     const int c0 = 32 * jb, w = min(32, kb - c0);
     const int c1 = c0 + 32, w1 = kb - c1;  // the next block column (w1 <= 0: none)
@@ -488,7 +493,7 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
     if (tid < nd + nrt) {
       float x[32];
       dp_row_solve(&S[tid < nd ? c1 + tid : kT + tid - nd][c0], T, x);
-      if (tid >= nd) dp_emit(x, tid - nd, nrows, c0, w, A + (size_t)(k0 + c0) * lda + row0, lda,
+      if (tid >= nd) dp_emit(x, tid - nd, part * rpc + tid - nd, nrows, c0, w, A + (size_t)(k0 + c0) * lda + row0, lda,
                              PS + (size_t)tile * kTileBytes);
     }
     __syncthreads();
@@ -905,6 +910,7 @@ struct StepArgs {
   int* negpiv;
   int* err;
   int lda, m, ndp, pk0, pkb;
+  int prows;  // tile rows per panel CTA (128, or 64 when the panel is split over twice the CTAs)
   UpdJob job[2];
 };
 
@@ -916,7 +922,8 @@ __global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_cons
   extern __shared__ float4 smem4[];
   int b = (int)blockIdx.x;
   if (b < a.ndp) {
-    dpanel_body(smem4, a.A, a.Ldg, a.lda, a.m, a.pk0, a.pkb, a.pk0 / kT + 1, b, a.PSp, a.negpiv, a.PSpre, a.err);
+    dpanel_body(smem4, a.A, a.Ldg, a.lda, a.m, a.pk0, a.pkb, a.pk0 / kT + 1, b, a.PSp, a.negpiv, a.PSpre, a.err,
+                a.prows);
     return;
   }
   b -= a.ndp;
@@ -1004,6 +1011,12 @@ static int rest_group(int tiles) {
 #ifndef BD_PAIR_MIN
 #define BD_PAIR_MIN 24  // pair while at least this many tile rows remain right of column k+2 (k: last factored)
 #endif
+#ifndef BD_SPLIT_CTAS
+#define BD_SPLIT_CTAS 151  // panel CTAs allowed when the panel is split in 64-row parts
+#endif
+#ifndef BD_SPLIT_JOB_TILES
+#define BD_SPLIT_JOB_TILES 400  // ... and at most this many update tiles in the launch
+#endif
 #ifndef BD_TRIPLE_MIN
 #define BD_TRIPLE_MIN 40  // three panels per bulk pass while this many tile rows remain right of column k+3
 #endif
@@ -1053,9 +1066,14 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
   auto launch = [&](int pn, const Job& j0, const Job& j1, bool pre) {
     StepArgs a{};
     a.A = A, a.negpiv = negpiv, a.err = err, a.lda = lda, a.m = m;
-    a.Ldg = Ld, a.PSp = PS, a.PSpre = nullptr;
+    a.Ldg = Ld, a.PSp = PS, a.PSpre = nullptr, a.prows = kT;
     if (pn >= 0) {
-      a.ndp = nt - pn, a.pk0 = pn * kT, a.pkb = kb_of(pn);
+      // the panel over twice the CTAs (64 tile rows each) when they fit on
+      // the GPU beside small update jobs: the diagonal work is repeated,
+      // the tile work halved
+      const int jt = (j0.tiles > 0 ? j0.tiles : 0) + (j1.tiles > 0 ? j1.tiles : 0);
+      if (2 * (nt - pn - 1) + 1 <= BD_SPLIT_CTAS && jt <= BD_SPLIT_JOB_TILES) a.prows = kT / 2;
+      a.ndp = 1 + (nt - pn - 1) * (kT / a.prows), a.pk0 = pn * kT, a.pkb = kb_of(pn);
       a.Ldg = Ld + (size_t)pn * kT * kT, a.PSp = psb(pn);
       if (pre && pn > 0) a.PSpre = psb(pn - 1);
     }
@@ -1079,7 +1097,7 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
     L++;
     if (kbytes || kflop) {
       double by = pn >= 0 ? 16.0 * (double)(m - pn * kT) * kb_of(pn) : 0.0;  // panel read and written back
-      double fl = a.PSpre ? 6.0 * 2.0 * kT * kT * kT * (2 * (nt - pn) - 1) : 0.0;  // the panel CTAs' own products
+      double fl = a.PSpre ? 6.0 * 2.0 * kT * kT * kT * (2 * a.ndp - 1) : 0.0;  // the panel CTAs' own products
       for (int q = 0; q < 2; q++) {
         const Job& j = *js[q];
         if (j.tiles <= 0) continue;
