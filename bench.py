@@ -33,10 +33,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "BD steps/s vs plain FP64 on 1 GB300 at <=1e-6 rel. error; replica-steps/s"
 # dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one
-# k_chol_step launch under ncu (the fifth of a factorisation: panel 2 beside
-# the K = 256 bulk update by panels 0 and 1, 3N = 11,700: 1,057.9 MB of DRAM
-# traffic for 1,047.9 MB algorithmic)
-NCU_TRAFFIC_PER_ALG_BYTE = 1057.9 / 1047.9
+# k_chol_step launch under ncu (the fourth of a factorisation: panel 3 beside
+# the K = 384 bulk update by panels 0-2, 3N = 11,700: 1,015.5 MB of DRAM
+# traffic for 1,024.6 MB algorithmic)
+NCU_TRAFFIC_PER_ALG_BYTE = 1015.5 / 1024.6
 
 
 def peaks():
