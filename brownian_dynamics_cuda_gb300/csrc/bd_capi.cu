@@ -304,6 +304,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   for (int q = 0; q < 3; q++) addD(2 * (size_t)M.n_D);
   addD(4 * ((size_t)nt + nL));
   addI(nL);
+  addD(37 * (size_t)n);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
   if (c->precision != BD_PREC_MIXED && c->precision != BD_PREC_FP64)
@@ -364,6 +365,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   c->S.qf = ar.take<float4>(M.n_D);
   c->S.bond = ar.take<double>(4 * ((size_t)nt + nL));
   int* d_lhp_idx = ar.take<int>(nL);
+  c->S.bonds = ar.take<double>(37 * (size_t)n);
   c->S.ot = n; c->S.ol = n + nt; c->S.og = n + nt + nL; c->S.npos = npos;
   c->negpiv = ar.take<int>(1);
   cudaStream_t st = c->stream;

@@ -114,6 +114,7 @@ struct DevScratch {
   // qh.w) and the move's forces in FP32, per bead of the tensor
   float4 *qh, *ql, *qf;
   double* bond;  // [4 (n_tail + n_LH)] mixed path: per-bead bonded force and energy of tails, LH beads
+  double* bonds; // [37 n] per chain bond: forces and torques on both beads, energy
 };
 
 namespace bdk {

@@ -276,21 +276,42 @@ __device__ V3 mech_torque(const DevModel& M, const DevState& X, int i, V3 T) {
 
 // Thread per chain bead: bonded forces and torques in the reference's
 // accumulation order; energy of bond j on thread j.
-__global__ void k_chain_bonded(DevModel M, DevState X, double* Fm, double* Tm, double* Ech) {
+// Bonded terms of each chain bond i (beads i, i+1), one thread per bond: the
+// FP64 work of every bond done once (each bead used to evaluate both of its
+// bonds).  Stored per bond: f1, f2, t1, t2 (3 V3 each), E.
+constexpr int kBondDoubles = 37;
+__global__ void k_chain_bonds(DevModel M, DevState X, double* B) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M.n - 1) return;
+  BondOut o;
+  bond_terms(M, X, i, o);
+  double* b = B + (size_t)kBondDoubles * i;
+  for (int q = 0; q < 3; q++) {
+    st3(b + 3 * q, o.f1[q]);
+    st3(b + 9 + 3 * q, o.f2[q]);
+    st3(b + 18 + 3 * q, o.t1[q]);
+    st3(b + 27 + 3 * q, o.t2[q]);
+  }
+  b[36] = o.E;
+}
+
+// Per chain bead j: the terms of bonds j-1 and j summed in the order of the
+// reference's loop, then the mechanical torque.
+__global__ void k_chain_bonded(DevModel M, DevState X, const double* __restrict__ B, double* Fm, double* Tm,
+                               double* Ech) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= M.n) return;
   V3 F{0.0, 0.0, 0.0}, T{0.0, 0.0, 0.0};
-  BondOut lo, hi;
-  bool has_lo = j >= 1, has_hi = j <= M.n - 2;
-  if (has_lo) bond_terms(M, X, j - 1, lo);
-  if (has_hi) bond_terms(M, X, j, hi);
+  const bool has_lo = j >= 1, has_hi = j <= M.n - 2;
+  const double* lo = B + (size_t)kBondDoubles * (j - 1);  // bond j-1: f2, t2 act on bead j
+  const double* hi = B + (size_t)kBondDoubles * j;        // bond j: f1, t1
   for (int q = 0; q < 3; q++) {
-    if (has_lo) { acc(F, lo.f2[q]); }
-    if (has_hi) { acc(F, hi.f1[q]); }
+    if (has_lo) { acc(F, ld3(lo + 9 + 3 * q)); }
+    if (has_hi) { acc(F, ld3(hi + 3 * q)); }
   }
   for (int q = 0; q < 3; q++) {
-    if (has_lo) acc(T, lo.t2[q]);
-    if (has_hi) acc(T, hi.t1[q]);
+    if (has_lo) acc(T, ld3(lo + 27 + 3 * q));
+    if (has_hi) acc(T, ld3(hi + 18 + 3 * q));
   }
   if (j <= M.n - 2) {
     T = mech_torque(M, X, j, T);
@@ -300,7 +321,7 @@ __global__ void k_chain_bonded(DevModel M, DevState X, double* Fm, double* Tm, d
   }
   st3(Fm + 3 * j, F);
   st3(Tm + 3 * j, T);
-  Ech[j] = has_hi ? hi.E : 0.0;
+  Ech[j] = has_hi ? hi[36] : 0.0;
 }
 
 // ------------------------------------------------------------ charge sets
@@ -1674,7 +1695,11 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
 #undef KSEL
   if (M.n_lhcore > 0) { k_gpos<<<cdiv(M.n_lhcore * M.n_lh_g, 128), 128, 0, st>>>(M, X); L++; }
   if (mixed) { k_mirror<<<cdiv(S.npos, 128), 128, 0, st>>>(M, X, S.ph, S.pl, S.npos); L++; }
-  k_chain_bonded<<<cdiv(M.n, kBeadThreads), kBeadThreads, 0, st>>>(M, X, Fm, Tm, Ebond);
+  if (M.n > 1) {
+    k_chain_bonds<<<cdiv(M.n - 1, kBeadThreads), kBeadThreads, 0, st>>>(M, X, S.bonds);
+    L++;
+  }
+  k_chain_bonded<<<cdiv(M.n, kBeadThreads), kBeadThreads, 0, st>>>(M, X, S.bonds, Fm, Tm, Ebond);
   L++;
   if (M.n_c > 1) {
     if (mixed) {
