@@ -219,17 +219,19 @@ __device__ __forceinline__ void rpy_block(const V3& sij, double ssq, double s, d
   out[2][1] = out[1][2] = o21;
 }
 
-// FP32 form of rpy_block for the mixed-precision drift (separation given in
-// FP32, already formed in FP64).
+// FP32 form of rpy_block for the mixed path (drift and tensor; separation
+// given in FP32, formed from double-float positions).
 __device__ __forceinline__ void rpy_block_f(float sx, float sy, float sz, float radi, float radj, float a1, float a2,
                                             float (&out)[3][3]) {
   const float sv[3] = {sx, sy, sz};
   const float ssq = sx * sx + sy * sy + sz * sz;
-  const float s = sqrtf(ssq);
+  const float inv_s = rsqrtf(ssq);  // one reciprocal square root instead of a root and three divisions
+  const float s = ssq * inv_s;
   if (s >= radi + radj) {
-    const float f = (radi * radi + radj * radj) / ssq;
-    const float f1 = 1.f + f / 3.f, f2 = 1.f - f;
-    const float as = a2 / s, w = as * f2 / ssq;
+    const float inv_ssq = inv_s * inv_s;
+    const float f = (radi * radi + radj * radj) * inv_ssq;
+    const float f1 = 1.f + f * (1.f / 3.f), f2 = 1.f - f;
+    const float as = a2 * inv_s, w = as * f2 * inv_ssq;
 #pragma unroll
     for (int k = 0; k < 3; k++)
 #pragma unroll

@@ -1168,19 +1168,20 @@ __global__ void k_mirror(DevModel M, DevState X, float4* ph, float4* pl, int npo
 template <bool DH, bool LJ>
 __device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float sig, float3 d, float& E) {
   const float d2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-  const float dd = sqrtf(d2);
+  const float rinv = rsqrtf(d2);  // 1/d: one reciprocal square root instead of a root and divisions
+  const float dd = d2 * rinv;
   float t = 0.f;
   if (DH && dd < 7.f) {
-    const float ex = expf(-kap * dd);
-    t = qq * fmaf(kap, dd, 1.f) * ex / d2;
-    E += qq * ex / dd;
+    const float qe = qq * expf(-kap * dd) * rinv;  // k_e q1 q2 e^{-kappa d} / d
+    t = qe * fmaf(kap, dd, 1.f) * rinv;
+    E += qe;
   }
   if (LJ && dd < 4.f) {
-    const float sr = sig / dd, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-    t = t - kev * (6.f * sr6 - 12.f * sr12) / dd;
+    const float sr = sig * rinv, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+    t = t - kev * (6.f * sr6 - 12.f * sr12) * rinv;
     E += kev * (sr12 - sr6);
   }
-  const float w = t / dd;
+  const float w = t * rinv;
   return make_float3(clamp09f(w * d.x), clamp09f(w * d.y), clamp09f(w * d.z));
 }
 
@@ -1519,13 +1520,14 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
       for (int i = tid; i < M.n; i += nt) {
         if (i == j || M.type[i] != 0 || abs(i - j) <= 1 || !chain_ok(M, i)) continue;
         const float3 z = sepf(pj, ldpf(S, i));
-        const float df = sqrtf(fmaf(z.x, z.x, fmaf(z.y, z.y, z.z * z.z)));
+        const float d2 = fmaf(z.x, z.x, fmaf(z.y, z.y, z.z * z.z));
+        const float mi = rsqrtf(d2), df = d2 * mi;  // 1/d and d
         if (df > 25.f) continue;
-        const float mi = 1.f / df, ex = expf(-kll * df);
-        float g = qq * ex * fmaf(kll, df, 1.f) / (df * df), e = qq * ex / df;
+        const float ex = expf(-kll * df);
+        float e = qq * ex * mi, g = e * fmaf(kll, df, 1.f) * mi;
         if (df <= 8.f) {
-          const float sr = sDD / df, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-          g += kex * (12.f * sr12 - 6.f * sr6) / df;
+          const float sr = sDD * mi, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+          g += kex * (12.f * sr12 - 6.f * sr6) * mi;
           e += kex * (sr12 - sr6);
         }
         if (j < i) A.f[6] += e;
