@@ -390,68 +390,66 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
     // the products read the stage memory: complete before S overwrites it
     pre_ok = sm100::mbar_wait(&pbar->done, 0, kWaitLimit);
     sm100::tc_fence_after();
+    pre_ok = __syncthreads_and(pre_ok);  // one verdict for the CTA (it gates a named barrier below)
     if (!pre_ok && tid == 0) atomicExch(err, 7);
   }
-  if (work) {
-    // two rows per 16-byte load; lane l takes rows 2 (l & 3) + {0, 1} of an
-    // 8-row block and column l >> 2 of an 8-column block, so a warp reads
-    // 64-byte runs of 8 columns and its shared stores hit 32 distinct banks.
-    // Row pairs start even and lda is a multiple of 32: every load is
-    // aligned and stays inside its column.  16 blocks per batch, so that 32
-    // loads per thread are in flight.
+  // Rows [0, nr) of a 128-row part of the panel (columns k0 .. k0 + kb) into
+  // S[roff ..], FP32 (the nearest of each stored double-float; entries past
+  // the part are zero), by 8 warps (w8 = 0 .. 7).  Two rows per 16-byte
+  // load; lane l takes rows 2 (l & 3) + {0, 1} of an 8-row block and column
+  // l >> 2 of an 8-column block, so a warp reads 64-byte runs of 8 columns
+  // and its shared stores hit 32 distinct banks.  Row pairs start even and
+  // lda is a multiple of 32: every load is aligned and stays inside its
+  // column.  16 loads per thread in flight.
+  const size_t ld4 = (size_t)lda / 2;
+  const uint64_t pol = sm100::policy_evict_first();  // read once (BD_DP_EVICT_FIRST)
+  auto load_part = [&](const float2* gbase, int roff, int nr, bool lower, int w8) {
     const int rr = 2 * (lane & 3), cc = lane >> 2;
-    const float4* ga = reinterpret_cast<const float4*>(A + (size_t)k0 * lda + k0);
-    const float4* gx = reinterpret_cast<const float4*>(A + (size_t)k0 * lda + row0);
-    const size_t ld4 = (size_t)lda / 2;
-    const uint64_t pol = sm100::policy_evict_first();  // read once (BD_DP_EVICT_FIRST)
-    auto ld_panel = [&](const float4* a) { return BD_DP_EVICT_FIRST ? sm100::ld_f4_hint(a, pol) : *a; };
+    const float4* g4 = reinterpret_cast<const float4*>(gbase);
 #pragma unroll 1
-    for (int cb = warp; cb < kT / 8; cb += kDpThreads / 32) {
+    for (int cb = w8; cb < kT / 8; cb += 8) {
       const int c = 8 * cb + cc;
-      float4 va[16], vx[16];
+      float4 v[16];
 #pragma unroll
       for (int i = 0; i < 16; i++) {
         const int r = 8 * i + rr;
-        va[i] = (r + 1 >= c && r < kb && c < kb) ? ld_panel(ga + c * ld4 + r / 2) : make_float4(0.f, 0.f, 0.f, 0.f);
-        vx[i] = (r < nrows && c < kb) ? ld_panel(gx + c * ld4 + r / 2) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool in = (!lower || r + 1 >= c) && r < nr && c < kb;
+        v[i] = in ? (BD_DP_EVICT_FIRST ? sm100::ld_f4_hint(g4 + c * ld4 + r / 2, pol) : g4[c * ld4 + r / 2])
+                  : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
       for (int i = 0; i < 16; i++) {
         const int r = 8 * i + rr;
-        // nearest FP32 of the stored double-float; entries past the block are zero
-        S[r][c] = (r < kb && c < kb) ? va[i].x + va[i].y : 0.f;
-        S[r + 1][c] = (r + 1 < kb && c < kb) ? va[i].z + va[i].w : 0.f;
-        S[kT + r][c] = (r < nrows) ? vx[i].x + vx[i].y : 0.f;
-        S[kT + r + 1][c] = (r + 1 < nrows) ? vx[i].z + vx[i].w : 0.f;
+        S[roff + r][c] = (r < nr && c < kb) ? v[i].x + v[i].y : 0.f;
+        S[roff + r + 1][c] = (r + 1 < nr && c < kb) ? v[i].z + v[i].w : 0.f;
       }
     }
-  }
-  __syncthreads();
-  if (PSpre) {
-    // warp w reads TMEM lanes 32 (w % 4) ..: rows of D0 (w < 4) or of D1
-    // (the CTA's part of the tile)
-    const int q = warp & 3;
-    if (pre_ok && warp < 8 && (warp < 4 || (!is_diag && (32 * q) / rpc == part))) {
-      const int r = 32 * q + lane;
-      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (warp < 4 ? 0u : (uint32_t)kT);
-      float* row = warp < 4 ? S[r] : S[kT + r - part * rpc];
+  };
+  // the CTA's D accumulator rows into S: warp w reads TMEM lanes 32 (w % 4) ..
+  auto subtract = [&](bool tile_part) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (tile_part ? (uint32_t)kT : 0u);
+    float* row = tile_part ? S[kT + r - part * rpc] : S[r];
 #pragma unroll 1
-      for (int cc = 0; cc < kT; cc += 32) {
-        float v[32];
-        sm100::tmem_ld32(ta + cc, v);
+    for (int cc = 0; cc < kT; cc += 32) {
+      float v[32];
+      sm100::tmem_ld32(ta + cc, v);
 #pragma unroll
-        for (int k4 = 0; k4 < 8; k4++) {
-          float4* p4 = reinterpret_cast<float4*>(row + cc + 4 * k4);
-          float4 x = *p4;
-          x.x -= v[4 * k4], x.y -= v[4 * k4 + 1], x.z -= v[4 * k4 + 2], x.w -= v[4 * k4 + 3];
-          *p4 = x;
-        }
+      for (int k4 = 0; k4 < 8; k4++) {
+        float4* p4 = reinterpret_cast<float4*>(row + cc + 4 * k4);
+        float4 x = *p4;
+        x.x -= v[4 * k4], x.y -= v[4 * k4 + 1], x.z -= v[4 * k4 + 2], x.w -= v[4 * k4 + 3];
+        *p4 = x;
       }
     }
-    sm100::tc_fence_before();
-    __syncthreads();
-    if (warp == 1) sm100::tmem_dealloc(tmem, 2 * kT);
-  }
+  };
+  // the diagonal block first (and D0 off it); the tile rows load while the
+  // first 32 x 32 block is factored (below)
+  if (work) load_part(A + (size_t)k0 * lda + k0, 0, kb, true, warp);
+  __syncthreads();
+  if (PSpre && pre_ok && warp < 4) subtract(false);
+  if (PSpre) sm100::tc_fence_before();
+  __syncthreads();
   DP_MARK(1);
   const int nb = (kb + 31) >> 5;
   const int nrt = is_diag ? 0 : rpc;  // tile rows solved (rows past the matrix are zero and stay zero)
@@ -480,10 +478,22 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
         for (int j = 0; j < 32; j++)
           if (lane < w && j <= lane) S[c0 + lane][c0 + j] = a[j];
       }
+    } else if (warp >= 2 && jb == 0) {
+      // the tile rows (and the previous panel's update of them)
+      if (!is_diag) {
+        sm100::tc_fence_after();
+        load_part(A + (size_t)k0 * lda + row0, kT, nrows, false, warp - 2);
+        if (PSpre && pre_ok) {
+          asm volatile("bar.sync 1, 256;" ::: "memory");  // warps 2..9: the tile rows loaded
+          if (warp >= 4 && warp < 8 && (32 * (warp & 3)) / rpc == part) subtract(true);
+        }
+      }
     } else if (warp >= 2 && w1 > 0 && c0 > 0) {
       dp_block_update(S, tid - 64, c1, min(32, w1), nd, nd + nrows, 0, c0);
     }
+    if (jb == 0 && PSpre) sm100::tc_fence_before();
     __syncthreads();
+    if (jb == 0 && PSpre && warp == 1) sm100::tmem_dealloc(tmem, 2 * kT);
     DP_MARK(2 + 3 * jb);
     // B: the rows below the block, the rest of the diagonal block, then the
     // 128 tile rows; a tile row's 32 new entries of L_ik go out at once:
