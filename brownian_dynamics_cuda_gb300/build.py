@@ -32,6 +32,7 @@ UNITS = [
     ("k_rpy_chol.cu", ["-fmad=false"]),
     ("k_tc_chol.cu", []),
     ("k_noalloc.cu", ["-fmad=false"]),
+    ("k_adjoint.cu", []),
 ]
 
 

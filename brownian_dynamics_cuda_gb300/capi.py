@@ -114,6 +114,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, _ip]
     L.bd_kernel_bytes.argtypes = [C.c_void_p, _dp]
     L.bd_negative_pivots.argtypes = [C.c_void_p, _ip]
+    L.bd_adjoint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
+    L.bd_rollout_loss.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp]
+    L.bd_set_moduli.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.bd_adjoint_launches.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
     _lib = L
     return L
 
@@ -403,6 +407,31 @@ class Context:
     def negative_pivots(self) -> int:
         v = C.c_int()
         _check(self._L.bd_negative_pivots(self._h, C.byref(v)))
+        return v.value
+
+    def adjoint(self, rr: np.ndarray, p: np.ndarray, window: int, checkpoint_every: int = 20) -> tuple:
+        """(loss, d loss / d (h, g, s, Debye length)) of the rollout driven by the
+        noise rows rr [steps, 3n], p [steps, 3 n_D] (bd_adjoint)."""
+        rr = np.ascontiguousarray(rr, dtype=np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        loss, g = C.c_double(), np.zeros(4)
+        _check(self._L.bd_adjoint(self._h, rr.shape[0], checkpoint_every, window, _pd(rr), _pd(p), C.byref(loss),
+                                  _pd(g)))
+        return loss.value, g
+
+    def rollout_loss(self, rr: np.ndarray, p: np.ndarray, window: int) -> float:
+        rr = np.ascontiguousarray(rr, dtype=np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        loss = C.c_double()
+        _check(self._L.bd_rollout_loss(self._h, rr.shape[0], window, _pd(rr), _pd(p), C.byref(loss)))
+        return loss.value
+
+    def set_moduli(self, h: float, g: float, s: float, debye_length: float) -> None:
+        _check(self._L.bd_set_moduli(self._h, h, g, s, debye_length))
+
+    def adjoint_launches(self) -> int:
+        v = C.c_long()
+        _check(self._L.bd_adjoint_launches(self._h, C.byref(v)))
         return v.value
 
 

@@ -68,38 +68,6 @@ size_t slab(size_t count) {
 
 }  // namespace
 
-struct bd_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  int precision = BD_PREC_FP64;
-  int freq_rp = 1;
-  int use_graph = 0;
-  long step_count = 0;
-  DevModel M{};
-  DevState X{}, Y{};
-  DevForces F0{}, F1{}, Fa{};
-  DevScratch S{};
-  void* arena_base = nullptr;
-  double* A = nullptr;   // m x lda, column-major; holds D then L (FP64 path)
-  unsigned char* PS = nullptr;  // mixed path: BF16 panel slices
-  int* d_err = nullptr;         // device error code of the tensor-core kernels
-  int m = 0, lda = 0;
-  double *r_all = nullptr, *rd = nullptr, *p = nullptr, *rr = nullptr, *rd_part = nullptr, *energy = nullptr;
-  int* negpiv = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  int last_launches = 0;
-  int host_negpiv = 0;
-  cudaEvent_t ev[10] = {};
-  bool timing = false;
-  std::vector<cudaEvent_t> kev;   // events around every k_chol_step launch (timing steps only)
-  int kev_pairs = 0;
-  double kflop = 0.0;
-  double kbytes = 0.0;
-  // host copies for the drop-in paths
-  std::vector<int> h_type;
-  std::vector<double> h_rvar;  // rotational noise scale (bd_batch_run draws noise on the host)
-};
 
 namespace {
 
@@ -134,10 +102,25 @@ int record(bd_ctx* c, int k) {
 }
 
 // The device part of one step (stream-ordered, capturable).
-int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
+}  // namespace
+
+// [r a b c r_t] of a state into one buffer (12n + 3 n_tail doubles)
+static int pack_ns(bd_ctx* c, const DevState& Y, double* dst) {
+  const size_t n3 = 3 * (size_t)c->M.n, b = n3 * sizeof(double);
+  CK(cudaMemcpyAsync(dst, Y.r, b, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(dst + n3, Y.a, b, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(dst + 2 * n3, Y.b, b, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(dst + 3 * n3, Y.c, b, cudaMemcpyDeviceToDevice, c->stream));
+  if (c->M.n_tail)
+    CK(cudaMemcpyAsync(dst + 4 * n3, Y.r_t, 3 * (size_t)c->M.n_tail * sizeof(double), cudaMemcpyDeviceToDevice,
+                       c->stream));
+  return BD_OK;
+}
+
+int bdh::step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* const* saves) {
   DevModel& M = c->M;
   cudaStream_t st = c->stream;
-  int L = 0;
+  int L = 0, rc = 0;
   record(c, 0);
   const bool mixed = c->precision == BD_PREC_MIXED;
   bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
@@ -170,15 +153,18 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   record(c, 4);
   bdk::rotate_translate(M, c->X, c->Y, c->F0, d_rr, c->rd, c->r_all, c->precision, c->S, st);
   L += mixed ? 3 : 2;
+  if (saves && (rc = pack_ns(c, c->Y, saves[0]))) return rc;
   record(c, 5);
   bdk::frames(M, c->Y, st);
   L += 2;
+  if (saves && (rc = pack_ns(c, c->Y, saves[1]))) return rc;
   record(c, 6);
   L += bdk::forces(M, c->Y, c->F1, c->S, c->precision, st);
   record(c, 7);
   bdk::average_forces(M, c->F0, c->F1, c->Fa, st);
   bdk::rotate_translate(M, c->X, c->Y, c->Fa, d_rr, c->rd, c->r_all, c->precision, c->S, st);
   L += mixed ? 4 : 3;
+  if (saves && (rc = pack_ns(c, c->Y, saves[2]))) return rc;
   // X <- Y (final_updates, func_cuda.cu:2643-2662), then refresh frames
   size_t n3 = 3 * (size_t)M.n;
   CK(cudaMemcpyAsync(c->X.r, c->Y.r, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -195,7 +181,8 @@ int step_device(bd_ctx* c, const double* d_rr, const double* d_p) {
   return BD_OK;
 }
 
-}  // namespace
+using bdh::step_device;
+
 
 extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options* opt, bd_ctx** out) {
   if (!out || !s) return set_error(BD_ERR_ARG, "bd_create: null argument");
@@ -468,6 +455,7 @@ extern "C" int bd_destroy(bd_ctx* c) {
   if (!c) return BD_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  bdh::adj_free(c->adj);
   for (int k = 0; k < 10; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (auto ev : c->kev) cudaEventDestroy(ev);
@@ -938,6 +926,24 @@ extern "C" int bd_batch_run(bd_batch* b, int nsteps, unsigned long seed_base, do
     }
     int rc = bd_batch_step(b, prr.data(), pp.data(), s + 1 == nsteps ? energies : nullptr);
     if (rc) return rc;
+  }
+  return BD_OK;
+}
+
+extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double debye_length) {
+  if (!c || !(debye_length > 0.0)) return set_error(BD_ERR_ARG, "bd_set_moduli: bad argument");
+  DevModel& M = c->M;
+  const double kap = 1.0 / debye_length;
+  M.debyell = M.debyell * (kap / M.debye);
+  M.debye = kap;
+  M.h = h;
+  M.g = g;
+  M.s = s;
+  // a captured graph holds the old constants in its kernel parameters
+  if (c->graph) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
   }
   return BD_OK;
 }

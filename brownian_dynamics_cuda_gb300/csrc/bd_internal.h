@@ -153,3 +153,50 @@ int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
                    cudaStream_t st, bool df = false);
 }  // namespace bdk
+
+namespace bdh {
+struct AdjWork;                 // k_adjoint.cu: buffers of the rollout gradient
+void adj_free(AdjWork* w);
+}  // namespace bdh
+
+// One fiber on one device: every buffer is allocated at bd_create.
+struct bd_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int precision = BD_PREC_FP64;
+  int freq_rp = 1;
+  int use_graph = 0;
+  long step_count = 0;
+  DevModel M{};
+  DevState X{}, Y{};
+  DevForces F0{}, F1{}, Fa{};
+  DevScratch S{};
+  void* arena_base = nullptr;
+  double* A = nullptr;   // m x lda, column-major; holds D then L (FP64 path)
+  unsigned char* PS = nullptr;  // mixed path: BF16 panel slices
+  int* d_err = nullptr;         // device error code of the tensor-core kernels
+  int m = 0, lda = 0;
+  double *r_all = nullptr, *rd = nullptr, *p = nullptr, *rr = nullptr, *rd_part = nullptr, *energy = nullptr;
+  int* negpiv = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int last_launches = 0;
+  int host_negpiv = 0;
+  cudaEvent_t ev[10] = {};
+  bool timing = false;
+  std::vector<cudaEvent_t> kev;   // events around every k_chol_step launch (timing steps only)
+  int kev_pairs = 0;
+  double kflop = 0.0;
+  double kbytes = 0.0;
+  // host copies for the drop-in paths
+  std::vector<int> h_type;
+  std::vector<double> h_rvar;  // rotational noise scale (bd_batch_run draws noise on the host)
+  bdh::AdjWork* adj = nullptr;  // allocated by the first bd_adjoint / bd_rollout_loss
+};
+
+namespace bdh {
+// The device part of one step (bd_capi.cu).  With saves != nullptr the
+// predictor state before and after its frame refresh and the corrector state
+// before its refresh are copied to saves[0..2] ([r a b c r_t], 12n + 3 n_tail).
+int step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* const* saves = nullptr);
+}  // namespace bdh

@@ -248,6 +248,34 @@ int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
 int bd_negative_pivots(bd_ctx* ctx, int* out);
 
+/* ---------------------------------------------------------------- gradients
+ * No counterpart in the reference (main.cpp runs the dynamics forward only).
+ *
+ * Rollout observable: starting from the context's state, n_steps steps of
+ * bd_step with the caller's noise (rr: n_steps rows of 3n, p: n_steps rows
+ * of 3 n_D, the bd_noise_step stream), then
+ *   loss = mean over the final `window` states of |r_{n-1} - r_0|^2 + Rg,
+ * r the chain beads (cores and linker DNA), Rg their radius of gyration.
+ * The context's state and step counter are left as they were.  Requires
+ * n_LH == 0 and frequency_RP == 1.
+ *
+ * bd_adjoint: loss and its gradient grad4 = d loss / d (h, g, s, lambda_D)
+ * (stretch, bend, twist moduli; Debye length lambda_D = 1 / debye, with
+ * debyell scaled alongside), by the reverse-mode pass of the step with
+ * recomputation checkpointing: the state is kept every checkpoint_every
+ * steps and each segment is recomputed during the backward sweep.  The
+ * forward arithmetic is the context's (FP32-class on a BD_PREC_MIXED
+ * context, FP64 otherwise); the adjoint runs in FP32 or FP64 accordingly. */
+int bd_adjoint(bd_ctx* ctx, int n_steps, int checkpoint_every, int window, const double* rr, const double* p,
+               double* loss, double* grad4);
+/* The loss alone (the forward sweep of bd_adjoint). */
+int bd_rollout_loss(bd_ctx* ctx, int n_steps, int window, const double* rr, const double* p, double* loss);
+/* Set h, g, s and the Debye length (debye = 1 / lambda_D, debyell scaled by
+ * the same factor) of a context, e.g. for finite differences. */
+int bd_set_moduli(bd_ctx* ctx, double h, double g, double s, double debye_length);
+/* Kernel launches issued by the last bd_adjoint (forward sweep excluded). */
+int bd_adjoint_launches(bd_ctx* ctx, long* out);
+
 #ifdef __cplusplus
 }
 #endif

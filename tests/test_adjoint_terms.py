@@ -1,0 +1,77 @@
+"""The adjoint kernels' force-field terms on the CPU.
+
+The terms (brownian_dynamics_cuda_gb300/csrc/adj_terms.cuh) are compiled for
+the host into a test harness (tests/adj_terms_check.cpp):
+  * summed the way the adjoint kernels split them, they must give the CPU
+    oracle's forces and torques (a restatement check; different summation
+    order, so 1e-10 relative);
+  * each term's dual-number vector-Jacobian product must match central
+    finite differences of the same term (derivative check).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden_names, load_golden, rel_err
+
+CSRC = os.path.join(ROOT, "brownian_dynamics_cuda_gb300", "csrc")
+SRC = os.path.join(ROOT, "tests", "adj_terms_check.cpp")
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("adjh") / "libadjh.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I" + CSRC, SRC, "-o", so], check=True)
+    L = C.CDLL(so)
+    L.adjh_vjp_check.argtypes = [C.c_int, C.c_uint, C.POINTER(C.c_double)]
+    return L
+
+
+def test_term_vjps_match_finite_differences(harness):
+    out = (C.c_double * 20)()
+    harness.adjh_vjp_check(60, 7, out)
+    names = ["bond DNA", "bond core", "bond DNA->core", "frame refresh", "rotation", "RPY block", "DNA pair",
+             "clamped pair", "tail bend", "anchor"]
+    errs = dict(zip(names, list(out)[:10]))
+    used = dict(zip(names, list(out)[10:]))
+    assert all(v >= 20 for v in used.values()), used
+    assert all(v < 1e-6 for v in errs.values()), errs
+
+
+def _fibers():
+    import tempfile
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, make_fiber
+    out = []
+    for name in golden_names():
+        fib, _ = load_golden(name)
+        if fib.sizes["n_LH"] == 0:
+            out.append((name, fib))
+    out.append(("syn_4nuc_30bp", make_fiber(FiberSpec(4, [30] * 4, lh=False, seed=3), tempfile.mkdtemp())))
+    return out
+
+
+@pytest.mark.parametrize("name,fib", _fibers(), ids=lambda v: v if isinstance(v, str) else "")
+def test_terms_sum_to_oracle_forces(harness, name, fib):
+    from oracle.pyoracle import Oracle
+    o = Oracle(fib)
+    ref = o.forces()
+    sz, ar, sc = fib.sizes, fib.arrays, fib.scalars
+    x = np.concatenate([o.get(k) for k in ("r", "a", "b", "c", "r_t")])
+    ints = [np.ascontiguousarray(ar[k], dtype=np.int32) for k in ("type", "tail_fix", "nc_t_flag", "t_grp")]
+    dbls = [np.ascontiguousarray(ar[k], dtype=np.float64) for k in
+            ("phi_o", "core_pos", "core_q", "tail_pos", "h_t", "g_t", "lo_t", "beta_o_t", "t_q")]
+    par = np.array([sc[k] for k in ("h", "g", "s", "debyell", "debye", "q_l", "k_e", "k_ex", "sigma_DNA_DNA",
+                                    "sigma_DNA_Core", "sigma_Core_Core", "sigma_Tail_Linker")])
+    isz = np.array([sz["n"], sz["n_c"], sz["Nq"], sz["n_t"], sz["n_tail"]], dtype=np.int32)
+    n, nt = sz["n"], sz["n_tail"]
+    F, T, tF = np.zeros(3 * n), np.zeros(3 * n), np.zeros(3 * nt)
+    ip = (C.POINTER(C.c_int) * 4)(*[a.ctypes.data_as(C.POINTER(C.c_int)) for a in ints])
+    dp = (C.POINTER(C.c_double) * 9)(*[a.ctypes.data_as(C.POINTER(C.c_double)) for a in dbls])
+    d = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    harness.adjh_forces(isz.ctypes.data_as(C.POINTER(C.c_int)), ip, dp, d(par), d(x), d(F), d(T), d(tF))
+    assert rel_err(F, ref["force"]) < 1e-10
+    assert rel_err(T, ref["torque"]) < 1e-10
+    assert rel_err(tF, ref["t_force"]) < 1e-10
