@@ -414,6 +414,79 @@ def run_batch(args):
     b.close()
 
 
+def run_adjoint(args):
+    """Config 3: gradient of the 200-step rollout observable (mean over the
+    final 50 states of the squared end-to-end distance plus the radius of
+    gyration) with respect to the stretch, bend and twist moduli and the
+    Debye length, by bd_adjoint (reverse mode, checkpoints every 20 steps,
+    FP32-class forward on a mixed-precision context).  One "step" of this
+    workload is one gradient evaluation (forward sweep + checkpointed
+    reverse sweep); metric: gradient evaluations/s.  With --fd the FP64
+    central-difference gradient (steps of 1e-4 relative) is computed too and
+    the relative error reported."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber as mk
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    spec = config(3, seed=1 + rank)
+    fib = mk(spec, tempfile.mkdtemp(prefix="bdadj_"))
+    nsteps, window, ck = 200, 50, 20
+    gen = Noise(1)
+    rows = [gen.step(s, fib.arrays["r_var"], fib.m) for s in range(nsteps)]
+    rr = np.array([r[0] for r in rows])
+    p = np.array([r[1] for r in rows])
+    ctx = Context(fib, precision=PREC_MIXED if args.precision == "mixed" else PREC_FP64, device=local)
+    for _ in range(args.warmup):
+        ctx.adjoint(rr, p, window, ck)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss, grad = ctx.adjoint(rr, p, window, ck)
+    dt = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    clocks = clk.stop()
+    launches = ctx.adjoint_launches()
+    t0 = time.perf_counter()
+    ctx.rollout_loss(rr, p, window)
+    fwd = time.perf_counter() - t0
+    fd = None
+    if args.fd and rank == 0:
+        c64 = Context(fib, precision=PREC_FP64, device=local)
+        sc = fib.scalars
+        th = np.array([sc["h"], sc["g"], sc["s"], 1.0 / sc["debye"]])
+        g = np.zeros(4)
+        for k in range(4):
+            d = 1e-4 * th[k]
+            tp, tm = th.copy(), th.copy()
+            tp[k] += d
+            tm[k] -= d
+            c64.set_moduli(*tp)
+            lp = c64.rollout_loss(rr, p, window)
+            c64.set_moduli(*tm)
+            lm = c64.rollout_loss(rr, p, window)
+            g[k] = (lp - lm) / (2 * d)
+        fd = {"grad_fd64": g.tolist(), "rel_err": float(np.max(np.abs(grad - g)) / np.max(np.abs(g)))}
+        c64.close()
+    if rank == 0:
+        h2d = (rr.size + p.size) * 8
+        line = {"metric": "adjoint gradient evaluations/s (200-step rollout, 4 parameters)",
+                "value": world / dt, "unit": "gradients/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt * 1000.0, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 (adjoint pair sums, RPY, Cholesky backward) + f64 (angle terms)",
+                "data": "synthetic (seeded fiber generator, reference file formats)",
+                "config": {"workload": spec.name, "n_D": fib.n_D, "3N": fib.m, "rollout_steps": nsteps,
+                           "window": window, "checkpoint_every": ck, "precision": args.precision,
+                           "forward_rollout_ms": fwd * 1000.0, "l2": "inputs larger than L2 (D: 60 MB FP32 x4)"},
+                "e2e": {"value": world / dt, "unit": "gradients/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": 5 * 8},
+                "gpu_launches": launches, "clocks": clocks, "roofline": None, "cpu_baseline": None,
+                "loss": loss, "grad": grad.tolist(), "fd_check": fd}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -427,6 +500,7 @@ def main():
     ap.add_argument("--frequency-rp", type=int, default=None,
                     help="rebuild and refactor D every k steps (default 1; 10 for config 4)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg of the mixed run")
+    ap.add_argument("--fd", action="store_true", help="config 3: also the FP64 central-difference gradient")
     args = ap.parse_args()
     big = args.config == 4
     args.frequency_rp = args.frequency_rp or (10 if big else 1)
@@ -436,6 +510,8 @@ def main():
         run_reference(args)
     elif args.config == 2:
         run_batch(args)
+    elif args.config == 3:
+        run_adjoint(args)
     else:
         run_ours(args)
 

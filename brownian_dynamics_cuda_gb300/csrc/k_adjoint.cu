@@ -8,10 +8,10 @@
 // state is kept every `checkpoint` steps.  Observable: the mean over the
 // final `window` states of |r_{n-1} - r_0|^2 + Rg (chain beads).
 //
-// Reverse: per segment (last first) the segment's states are recomputed
-// from its checkpoint; per step (last first) the forward step is recomputed
-// once more with its predictor and corrector states saved, and the adjoint
-// of the state is carried back through
+// Reverse: per segment (last first) the segment's steps are recomputed from
+// its checkpoint, each keeping its intermediates (the factor L, the forces,
+// the predictor and corrector states); per step (last first) the adjoint of
+// the state is carried back through
 //   corrector frame refresh -> rotation + translation (drift del D F and
 //   noise rd) -> averaged forces -> forces at the refreshed predictor ->
 //   predictor refresh -> rotation + translation -> forces at the state ->
@@ -75,9 +75,10 @@ __device__ __forceinline__ bool pair_ok(const DevModel& M, int i, int j) {
 }
 
 // ------------------------------------------------------------ chain bonds
-constexpr int kBW = 8;
+constexpr int kBW = 8;         // inputs seeded per thread (frame refresh, anchors)
+constexpr int kBondW = 2;      // inputs seeded per thread of the bond term (FP64; many short threads)
 constexpr int kBondIn = 39;
-constexpr int kBondChunks = (kBondIn + kBW - 1) / kBW;
+constexpr int kBondChunks = (kBondIn + kBondW - 1) / kBondW;
 
 template <class R>
 __global__ void __launch_bounds__(64) k_adj_bonds(DevModel M, const double* __restrict__ x,
@@ -108,12 +109,12 @@ __global__ void __launch_bounds__(64) k_adj_bonds(DevModel M, const double* __re
     yb[6 + q] = R(fb[n3 + 3 * i + q]);
     yb[9 + q] = R(fb[n3 + 3 * (i + 1) + q]);
   }
-  R xb[kBW];
-  vjp_chunk<kBW, kBondIn, 12>(
+  R xb[kBondW];
+  vjp_chunk<kBondW, kBondIn, 12>(
       [&](const auto* xd, auto* yd) { bond_term(k, xd, xd + 12, xd + 24, xd[36], xd[37], xd[38], yd); }, xin, yb,
       ch, xb);
-  for (int j = 0; j < kBW; j++) {
-    const int q = ch * kBW + j;
+  for (int j = 0; j < kBondW; j++) {
+    const int q = ch * kBondW + j;
     if (q >= kBondIn) break;
     const double v = (double)xb[j];
     if (q < 12) {
@@ -715,15 +716,20 @@ __global__ void __launch_bounds__(64) k_inv_leaf(int mp, const R* __restrict__ U
   for (int e = c; e < 64 * 64; e += 64) V[(size_t)(b0 + e / 64) * mp + b0 + e % 64] = Vs[e / 64][e % 64];
 }
 
-// C = alpha A op(B) (row-major; op(B) = B or B^T), M, N, K multiples of 64.
+// C = alpha A op(B) (row-major; op(B) = B or B^T), M, N, K multiples of 64;
+// gridDim.z independent products with operands zstride elements apart.
 // kmode restricts the k range of each 64 x 64 output tile (r0, c0) to
 // the nonzero band of triangular operands: 1: k >= r0, 2: k >= c0,
 // 4: k < c0 + 64.
 constexpr int kGT = 64, kGK = 16;
 template <class R, bool TB>
 __global__ void __launch_bounds__(256) k_gemm(int K, R alpha, const R* __restrict__ A, int lda,
-                                              const R* __restrict__ B, int ldb, R* C, int ldc, int kmode) {
+                                              const R* __restrict__ B, int ldb, R* C, int ldc, int kmode,
+                                              long zstride) {
   const int r0 = blockIdx.y * kGT, c0 = blockIdx.x * kGT;
+  A += blockIdx.z * zstride;  // batch item z: every operand shifted by z * zstride elements
+  B += blockIdx.z * zstride;
+  C += blockIdx.z * zstride;
   int kb = 0, ke = K;
   if (kmode & 1) kb = max(kb, r0);
   if (kmode & 2) kb = max(kb, c0);
@@ -798,26 +804,27 @@ __global__ void __launch_bounds__(256) k_build_xt(int m, int mp, const R* __rest
 // ------------------------------------------------------------ host side
 template <class R>
 int gemm(cudaStream_t st, int M_, int N_, int K_, R alpha, const R* A, int lda, const R* B, int ldb, R* C, int ldc,
-         bool tb, int kmode) {
-  dim3 grid(N_ / kGT, M_ / kGT);
-  if (tb) k_gemm<R, true><<<grid, 256, 0, st>>>(K_, alpha, A, lda, B, ldb, C, ldc, kmode);
-  else k_gemm<R, false><<<grid, 256, 0, st>>>(K_, alpha, A, lda, B, ldb, C, ldc, kmode);
+         bool tb, int kmode, int batch = 1, long zstride = 0) {
+  dim3 grid(N_ / kGT, M_ / kGT, batch);
+  if (tb) k_gemm<R, true><<<grid, 256, 0, st>>>(K_, alpha, A, lda, B, ldb, C, ldc, kmode, zstride);
+  else k_gemm<R, false><<<grid, 256, 0, st>>>(K_, alpha, A, lda, B, ldb, C, ldc, kmode, zstride);
   return 0;
 }
 
-// V = U^-1 for the upper-triangular U (diagonal 64-blocks already inverted)
+// V = U^-1 for the upper-triangular U of order mp = 64 * 2^k (diagonal
+// 64-blocks already inverted), by doubling: at block size b every diagonal
+// 2b-block [[V11, V12], [0, V22]] gets V12 = -V11 (U12 V22), all blocks of a
+// level in one batched launch per product (2 launches per level).
 template <class R>
-void inv_upper(cudaStream_t st, int mp, const R* U, R* V, R* tmp, int off, int nn, int& launches) {
-  if (nn <= 64) return;
-  const int n1 = ((nn / 64 + 1) / 2) * 64, n2 = nn - n1;
-  inv_upper(st, mp, U, V, tmp, off, n1, launches);
-  inv_upper(st, mp, U, V, tmp, off + n1, n2, launches);
-  // T = U12 V22 (V22 upper: k < c0 + 64), then V12 = -V11 T (V11 upper: k >= r0)
-  gemm<R>(st, n1, n2, n2, R(1), U + (size_t)off * mp + off + n1, mp, V + (size_t)(off + n1) * mp + off + n1, mp, tmp,
-          mp, false, 4);
-  gemm<R>(st, n1, n2, n1, R(-1), V + (size_t)off * mp + off, mp, tmp, mp, V + (size_t)off * mp + off + n1, mp, false,
-          1);
-  launches += 2;
+void inv_upper(cudaStream_t st, int mp, const R* U, R* V, R* tmp, int& launches) {
+  for (int b = 64; b < mp; b *= 2) {
+    const int nodes = mp / (2 * b);
+    const long zs = 2L * b * (mp + 1);
+    // T = U12 V22 (V22 upper: k < c0 + 64), then V12 = -V11 T (V11 upper: k >= r0)
+    gemm<R>(st, b, b, b, R(1), U + b, mp, V + (size_t)b * mp + b, mp, tmp + b, mp, false, 4, nodes, zs);
+    gemm<R>(st, b, b, b, R(-1), V, mp, tmp + b, mp, V + b, mp, false, 1, nodes, zs);
+    launches += 2;
+  }
 }
 
 }  // namespace
@@ -827,8 +834,11 @@ struct bdh::AdjWork {
   int nsteps = 0, K = 0, mp = 0, rsize = 0;
   size_t ns = 0, nfull = 0, nf = 0;
   double *ckpt = nullptr, *seg = nullptr, *x0 = nullptr;
+  // per step of the segment being reversed: the factor L (the context's A),
+  // r_all, the forces F0 and Fa ([F | T | tF] each) and the predictor /
+  // corrector states of the step
+  double *segA = nullptr, *segR = nullptr, *segF = nullptr, *segS = nullptr;
   double *lam = nullptr, *lamX = nullptr, *lamZ = nullptr, *lamY = nullptr, *lamYr = nullptr;
-  double* sv[3] = {nullptr, nullptr, nullptr};
   double *fbA = nullptr, *fb0 = nullptr, *fb1 = nullptr;
   double *lz = nullptr, *ly = nullptr, *fa = nullptr, *f0 = nullptr, *rdb = nullptr;
   double *th = nullptr, *loss = nullptr, *scratch = nullptr, *rr = nullptr, *p = nullptr;
@@ -882,7 +892,10 @@ int ensure_work(bd_ctx* c, int N, int K, bool grad) {
   size_t nfull = 0;
   for (auto& f : full_fields(c, c->X)) nfull += f.second;
   w->nfull = nfull;
-  w->mp = ((int)m + 63) / 64 * 64;
+  // the triangular inverse doubles 64-blocks: the matrices of the Cholesky
+  // backward are padded (identity) to 64 * 2^k >= m
+  w->mp = 64;
+  while (w->mp < (int)m) w->mp *= 2;
   auto take = [&](void** p, size_t bytes) -> int {
     CK(cudaMalloc(p, bytes ? bytes : 256));
     w->allocs.push_back(*p);
@@ -900,13 +913,14 @@ int ensure_work(bd_ctx* c, int N, int K, bool grad) {
     if ((rc = take((void**)&w->ckpt, nck * nfull * d)) || (rc = take((void**)&w->seg, (size_t)K * nfull * d)) ||
         (rc = take((void**)&w->lam, ns * d)) || (rc = take((void**)&w->lamX, ns * d)) ||
         (rc = take((void**)&w->lamZ, ns * d)) || (rc = take((void**)&w->lamY, ns * d)) ||
-        (rc = take((void**)&w->lamYr, ns * d)) || (rc = take((void**)&w->sv[0], ns * d)) ||
-        (rc = take((void**)&w->sv[1], ns * d)) || (rc = take((void**)&w->sv[2], ns * d)) ||
+        (rc = take((void**)&w->lamYr, ns * d)) ||
         (rc = take((void**)&w->fbA, nf * d)) || (rc = take((void**)&w->fb0, nf * d)) ||
         (rc = take((void**)&w->fb1, nf * d)) || (rc = take((void**)&w->lz, m * d)) ||
         (rc = take((void**)&w->ly, m * d)) || (rc = take((void**)&w->fa, m * d)) ||
         (rc = take((void**)&w->f0, m * d)) || (rc = take((void**)&w->rdb, mp * d)) ||
-        (rc = take((void**)&w->th, 8 * d)) || (rc = take(&w->U, mp * mp * rsize)) ||
+        (rc = take((void**)&w->th, 8 * d)) || (rc = take((void**)&w->segA, (size_t)K * m * c->lda * d)) ||
+        (rc = take((void**)&w->segR, (size_t)K * m * d)) || (rc = take((void**)&w->segF, (size_t)K * 2 * nf * d)) ||
+        (rc = take((void**)&w->segS, (size_t)K * 3 * ns * d)) || (rc = take(&w->U, mp * mp * rsize)) ||
         (rc = take(&w->V, mp * mp * rsize)) || (rc = take(&w->Xt, mp * mp * rsize)) ||
         (rc = take(&w->Db, mp * mp * rsize)) || (rc = take(&w->u, mp * rsize)))
       return rc;
@@ -938,18 +952,46 @@ int forces_vjp(bd_ctx* c, const double* x, const double* fbar, double* lamOut, d
   return BD_OK;
 }
 
-// one reverse step: lam holds the adjoint of x_{n+1}; on return, of x_n
+// run step `step` forward from the context's state, keeping its
+// intermediates in slot `slot` of the segment buffers
+int forward_saved(bd_ctx* c, bdh::AdjWork& w, int step, int slot) {
+  cudaStream_t st = c->stream;
+  const int n3 = 3 * c->M.n, nt3 = 3 * c->M.n_tail, m = c->m;
+  const size_t ns = w.ns, nf = w.nf;
+  double* S = w.segS + (size_t)slot * 3 * ns;
+  double* sv[3] = {S, S + ns, S + 2 * ns};
+  int rc = bdh::step_device(c, w.rr + (size_t)step * n3, w.p + (size_t)step * m, sv);
+  if (rc) return rc;
+  const size_t d = sizeof(double);
+  CK(cudaMemcpyAsync(w.segA + (size_t)slot * m * c->lda, c->A, (size_t)m * c->lda * d, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(w.segR + (size_t)slot * m, c->r_all, (size_t)m * d, cudaMemcpyDeviceToDevice, st));
+  double* F = w.segF + (size_t)slot * 2 * nf;
+  const DevForces* fs[2] = {&c->F0, &c->Fa};
+  for (int k = 0; k < 2; k++) {
+    CK(cudaMemcpyAsync(F + k * nf, fs[k]->F, n3 * d, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(F + k * nf + n3, fs[k]->T, n3 * d, cudaMemcpyDeviceToDevice, st));
+    if (nt3) CK(cudaMemcpyAsync(F + k * nf + 2 * n3, fs[k]->tF, nt3 * d, cudaMemcpyDeviceToDevice, st));
+  }
+  return BD_OK;
+}
+
+// one reverse step from the intermediates forward_saved kept in `slot`: lam
+// holds the adjoint of x_{n+1}; on return, of x_n
 template <class R>
-int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs) {
+int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs, int slot) {
   const DevModel& M = c->M;
   cudaStream_t st = c->stream;
   const int n = M.n, nt = M.n_tail, n3 = 3 * n, m = c->m, mp = w.mp;
   const double* rr = w.rr + (size_t)step * n3;
   const double* p = w.p + (size_t)step * m;
-  int rc = bdh::step_device(c, rr, p, w.sv);
-  if (rc) return rc;
-  const double *Yraw = w.sv[0], *Yref = w.sv[1], *Zraw = w.sv[2];
+  int rc = 0;
   const int ns = (int)w.ns, nf = (int)w.nf;
+  const double* S = w.segS + (size_t)slot * 3 * ns;
+  const double *Yraw = S, *Yref = S + ns, *Zraw = S + 2 * ns;
+  const double* Lf = w.segA + (size_t)slot * m * c->lda;
+  const double* r_all = w.segR + (size_t)slot * m;
+  const double* F0 = w.segF + (size_t)slot * 2 * nf;  // [F | T | tF]
+  const double* Fa = F0 + nf;
   long& L = w.launches;
   // corrector: refresh, rotation, translation
   k_pass1_init<<<cdiv(ns, 256), 256, 0, st>>>(M, w.lam, w.lamZ, ns);
@@ -957,9 +999,9 @@ int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs) {
   CK(cudaMemsetAsync(w.lamX, 0, ns * sizeof(double), st));
   CK(cudaMemsetAsync(w.fbA, 0, nf * sizeof(double), st));
   CK(cudaMemsetAsync(w.rdb, 0, mp * sizeof(double), st));
-  k_adj_rotate<double><<<cdiv(n, 64), 64, 0, st>>>(M, xs, c->Fa.T, rr, w.lamZ, w.lamX, w.fbA + n3);
+  k_adj_rotate<double><<<cdiv(n, 64), 64, 0, st>>>(M, xs, Fa + n3, rr, w.lamZ, w.lamX, w.fbA + n3);
   k_pos_through<<<cdiv(m, 256), 256, 0, st>>>(n, nt, w.lamZ, w.lamX, w.lz, w.rdb);
-  k_dblk<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, c->r_all, w.lz, M.del, w.fbA);
+  k_dblk<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, r_all, w.lz, M.del, w.fbA);
   k_half<<<cdiv(nf, 256), 256, 0, st>>>(nf, w.fbA, w.fb0, w.fb1);
   // forces at the refreshed predictor
   CK(cudaMemsetAsync(w.lamYr, 0, ns * sizeof(double), st));
@@ -967,28 +1009,30 @@ int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs) {
   // predictor: refresh, rotation, translation
   k_pass1_init<<<cdiv(ns, 256), 256, 0, st>>>(M, w.lamYr, w.lamY, ns);
   k_adj_pass1<double><<<cdiv((long)(n - 1) * kP1Chunks, 64), 64, 0, st>>>(M, Yraw, w.lamYr, w.lamY);
-  k_adj_rotate<double><<<cdiv(n, 64), 64, 0, st>>>(M, xs, c->F0.T, rr, w.lamY, w.lamX, w.fb0 + n3);
+  k_adj_rotate<double><<<cdiv(n, 64), 64, 0, st>>>(M, xs, F0 + n3, rr, w.lamY, w.lamX, w.fb0 + n3);
   k_pos_through<<<cdiv(m, 256), 256, 0, st>>>(n, nt, w.lamY, w.lamX, w.ly, w.rdb);
-  k_dblk<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, c->r_all, w.ly, M.del, w.fb0);
+  k_dblk<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, r_all, w.ly, M.del, w.fb0);
   // forces at the state
   if ((rc = forces_vjp<R>(c, xs, w.fb0, w.lamX, w.th, L))) return rc;
   // Cholesky backward: D_bar = V (Phi V^T), V = U^-1, U = L^T
   R *U = (R*)w.U, *V = (R*)w.V, *Xt = (R*)w.Xt, *Db = (R*)w.Db, *u = (R*)w.u;
   if (c->precision == BD_PREC_MIXED)
-    k_extract_u<R, true><<<dim3(cdiv(mp, 256), mp), 256, 0, st>>>(m, mp, c->A, c->lda, U);
+    k_extract_u<R, true><<<dim3(cdiv(mp, 256), mp), 256, 0, st>>>(m, mp, Lf, c->lda, U);
   else
-    k_extract_u<R, false><<<dim3(cdiv(mp, 256), mp), 256, 0, st>>>(m, mp, c->A, c->lda, U);
+    k_extract_u<R, false><<<dim3(cdiv(mp, 256), mp), 256, 0, st>>>(m, mp, Lf, c->lda, U);
   k_trmv_u<R><<<cdiv((long)mp * 32, 256), 256, 0, st>>>(mp, U, w.rdb, u);
   k_inv_leaf<R><<<mp / 64, 64, 2 * 64 * 65 * sizeof(R), st>>>(mp, U, V);
   int gl = 0;
-  inv_upper<R>(st, mp, U, V, Xt, 0, mp, gl);
+  inv_upper<R>(st, mp, U, V, Xt, gl);
   k_build_xt<R><<<mp, 256, 0, st>>>(m, mp, V, p, u, R(M.s2dt), Xt);
-  gemm<R>(st, mp, mp, mp, R(1), V, mp, Xt, mp, Db, mp, true, 3);
+  // D_bar tiles that k_adj_rpy reads (rows, columns < m); beyond m both
+  // factors vanish along k (p and u are zero on the padding)
+  const int m64 = (m + 63) / 64 * 64;
+  gemm<R>(st, m64, m64, m64, R(1), V, mp, Xt, mp, Db, mp, true, 3);
   // the RPY tensor
-  k_stack<<<cdiv(m, 256), 256, 0, st>>>(n, nt, c->Fa.F, c->Fa.tF, w.fa);
-  k_stack<<<cdiv(m, 256), 256, 0, st>>>(n, nt, c->F0.F, c->F0.tF, w.f0);
-  k_adj_rpy<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, c->r_all, Db, mp, w.lz, w.ly, w.fa, w.f0,
-                                                               w.lamX);
+  k_stack<<<cdiv(m, 256), 256, 0, st>>>(n, nt, Fa, Fa + 2 * n3, w.fa);
+  k_stack<<<cdiv(m, 256), 256, 0, st>>>(n, nt, F0, F0 + 2 * n3, w.f0);
+  k_adj_rpy<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, r_all, Db, mp, w.lz, w.ly, w.fa, w.f0, w.lamX);
   L += 24 + gl;
   CK(cudaGetLastError());
   std::swap(w.lam, w.lamX);
@@ -1033,12 +1077,11 @@ int run(bd_ctx* c, int N, int K, int Wn, const double* rr, const double* p, doub
       if ((rc = pack_full(c, w.ckpt + (size_t)sg * w.nfull, false))) return rc;
       for (int s = s0; s < e; s++) {
         if ((rc = pack_full(c, w.seg + (size_t)(s - s0) * w.nfull, true))) return rc;
-        if (s < e - 1 && (rc = bdh::step_device(c, w.rr + (size_t)s * n3, w.p + (size_t)s * m))) return rc;
+        if ((rc = forward_saved(c, w, s, s - s0))) return rc;
       }
       for (int s = e - 1; s >= s0; s--) {
         double* xs = w.seg + (size_t)(s - s0) * w.nfull;
-        if ((rc = pack_full(c, xs, false))) return rc;
-        if ((rc = reverse_step<R>(c, w, s, xs))) return rc;
+        if ((rc = reverse_step<R>(c, w, s, xs, s - s0))) return rc;
         if (s >= N - Wn + 1) k_loss<<<1, 256, 0, st>>>(M.n, xs, scale, w.scratch, w.lam);
       }
     }
