@@ -33,6 +33,7 @@ UNITS = [
     ("k_tc_chol.cu", []),
     ("k_noalloc.cu", ["-fmad=false"]),
     ("k_adjoint.cu", []),
+    ("k_noise.cu", []),
 ]
 
 

@@ -114,6 +114,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, _ip]
     L.bd_kernel_bytes.argtypes = [C.c_void_p, _dp]
     L.bd_negative_pivots.argtypes = [C.c_void_p, _ip]
+    L.bd_dev_noise_create.argtypes = [C.c_ulong, C.POINTER(C.c_void_p)]
+    L.bd_dev_noise_step.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]
+    L.bd_dev_noise_free.argtypes = [C.c_void_p]
     L.bd_adjoint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.bd_rollout_loss.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp]
     L.bd_set_moduli.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -287,6 +291,28 @@ class Noise:
         if getattr(self, "_h", None):
             self._L.bd_noise_free(self._h)
             self._h = None
+
+
+class DevNoise:
+    """The reference's MT19937 noise stream generated on the device (bd_dev_noise_*)."""
+
+    def __init__(self, seed: int):
+        self._L = load_library()
+        self._h = C.c_void_p()
+        _check(self._L.bd_dev_noise_create(seed, C.byref(self._h)))
+
+    def step(self, step: int, d_r_var: int, n3: int, n_D3: int, d_rr: int, d_p: int, stream: int = 0) -> None:
+        """Step `step`'s draws into device buffers (addresses)."""
+        _check(self._L.bd_dev_noise_step(self._h, step, n3, C.c_void_p(d_r_var), n_D3, C.c_void_p(d_rr),
+                                         C.c_void_p(d_p), C.c_void_p(stream) if stream else None))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.bd_dev_noise_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 class Context:

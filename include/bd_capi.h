@@ -135,6 +135,18 @@ int bd_noise_create(unsigned long seed, bd_noise** out);
 int bd_noise_step(bd_noise* g, int step, int n3, const double* r_var, int n_D3, double* rr, double* p);
 int bd_noise_u32(bd_noise* g, int count, uint32_t* out);
 void bd_noise_free(bd_noise* g);
+/* The same stream generated on the device (one CTA per generator; state in
+ * device memory): bd_dev_noise_step writes step `step`'s draws into device
+ * arrays d_rr [n3] (scaled by d_r_var) and d_p [n_D3], stream-ordered on
+ * `stream` (a cudaStream_t, NULL for the legacy stream).  The 32-bit words
+ * and the polar method's accept / reject decisions are those of
+ * bd_noise_step bit for bit; the deviates agree with the host's to the last
+ * bit or two (the device log). */
+typedef struct bd_dev_noise bd_dev_noise;
+int bd_dev_noise_create(unsigned long seed, bd_dev_noise** out);
+int bd_dev_noise_step(bd_dev_noise* g, int step, int n3, const double* d_r_var, int n_D3, double* d_rr, double* d_p,
+                      void* stream);
+int bd_dev_noise_free(bd_dev_noise* g);
 
 /* ------------------------------------------------------------ device step */
 typedef struct bd_ctx bd_ctx;
