@@ -117,23 +117,30 @@ static int pack_ns(bd_ctx* c, const DevState& Y, double* dst) {
   return BD_OK;
 }
 
-int bdh::step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* const* saves) {
+// The phases of one step: kPre (positions, RPY tensor), kChol (its
+// factorisation), kPost (noise displacement, forces, moves, frames).  A
+// batch runs kPre of every replica, one batched factorisation, then kPost.
+enum { kPre = 1, kChol = 2, kPost = 4 };
+
+static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double* const* saves, int phases) {
   DevModel& M = c->M;
   cudaStream_t st = c->stream;
   int L = 0, rc = 0;
-  record(c, 0);
   const bool mixed = c->precision == BD_PREC_MIXED;
-  bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
-  L += mixed ? 2 : 1;
   bool rebuild = (c->step_count % c->freq_rp) == 0;
-  if (rebuild) {
-    bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed ? c->S.qh : nullptr,
-                      mixed ? c->S.ql : nullptr);
-    L++;
+  if (phases & kPre) {
+    record(c, 0);
+    bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
+    L += mixed ? 2 : 1;
+    if (rebuild) {
+      bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed ? c->S.qh : nullptr,
+                        mixed ? c->S.ql : nullptr);
+      L++;
+      CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
+    }
+    record(c, 1);
   }
-  record(c, 1);
-  if (rebuild) {
-    CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
+  if ((phases & kChol) && rebuild) {
     if (mixed) {
       const bool kt = c->timing && !c->kev.empty();
       c->kflop = 0.0;
@@ -144,6 +151,10 @@ int bdh::step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* c
                             kt ? &c->kbytes : nullptr);
     }
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
+  }
+  if (!(phases & kPost)) {
+    c->last_launches = L;
+    return BD_OK;
   }
   record(c, 2);
   bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st, mixed);
@@ -179,6 +190,10 @@ int bdh::step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* c
   CK(cudaGetLastError());
   c->last_launches = L;
   return BD_OK;
+}
+
+int bdh::step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* const* saves) {
+  return step_phases(c, d_rr, d_p, saves, kPre | kChol | kPost);
 }
 
 using bdh::step_device;
@@ -767,18 +782,66 @@ struct bd_batch {
   cudaGraphExec_t graph = nullptr;
   std::vector<bd_noise*> noise;
   std::vector<std::vector<double>> h_rr, h_p;
+  bdk::MixedBatch* chol = nullptr;  // the replicas' factorisations as one launch per schedule step
 };
 
+// One step of every replica.  Mixed precision, D rebuilt every step: the
+// positions and tensors of all replicas, then one batched factorisation
+// (bdk::mixed_batch_run: launch i carries step i of every replica's
+// schedule), then the rest of every replica's step.  Otherwise the replicas'
+// steps run one after another.
+static bool batch_together(const bd_batch* b) {
+  bool together = true;
+  for (bd_ctx* c : b->ctx) together = together && c->precision == BD_PREC_MIXED && c->freq_rp == 1;
+  return together;
+}
+
+// the batched factorisation's plan (allocates and copies: never inside a
+// stream capture)
+static int batch_prepare(bd_batch* b) {
+  if (batch_together(b) && !b->chol) {
+    const size_t nr = b->ctx.size();
+    std::vector<int> m(nr), lda(nr);
+    std::vector<double*> A(nr);
+    std::vector<unsigned char*> PS(nr);
+    std::vector<int*> np(nr), er(nr);
+    for (size_t i = 0; i < nr; i++) {
+      bd_ctx* c = b->ctx[i];
+      m[i] = c->m, lda[i] = c->lda, A[i] = c->A, PS[i] = c->PS, np[i] = c->negpiv, er[i] = c->d_err;
+    }
+    b->chol = bdk::mixed_batch_create((int)nr, m.data(), A.data(), lda.data(), PS.data(), np.data(), er.data());
+    if (!b->chol) return set_error(BD_ERR_NOMEM, "bd_batch: batched factorisation plan");
+  }
+  return BD_OK;
+}
+
+static int batch_enqueue(bd_batch* b) {
+  int rc = BD_OK;
+  if (!b->chol) {
+    for (bd_ctx* c : b->ctx)
+      if (!rc) rc = step_device(c, c->rr, c->p);
+    return rc;
+  }
+  for (bd_ctx* c : b->ctx)
+    if (!rc) rc = step_phases(c, c->rr, c->p, nullptr, kPre);
+  if (rc) return rc;
+  bdk::mixed_batch_run(b->chol, b->stream);
+  CK(cudaGetLastError());
+  for (bd_ctx* c : b->ctx)
+    if (!rc) rc = step_phases(c, c->rr, c->p, nullptr, kPost);
+  return rc;
+}
+
 static int batch_device_step(bd_batch* b) {
+  int prc = batch_prepare(b);
+  if (prc) return prc;
   bool graph_ok = b->use_graph;
   for (bd_ctx* c : b->ctx) graph_ok = graph_ok && c->freq_rp == 1;
   if (graph_ok) {
     if (!b->graph) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = BD_OK;
-      for (bd_ctx* c : b->ctx)
-        if (!rc) rc = step_device(c, c->rr, c->p);
+      int rc = batch_enqueue(b);
       cudaError_t e = cudaStreamEndCapture(b->stream, &g);
       if (rc) return rc;
       if (e != cudaSuccess) return set_error(BD_ERR_CUDA, "bd_batch: graph capture failed");
@@ -788,10 +851,8 @@ static int batch_device_step(bd_batch* b) {
     }
     CK(cudaGraphLaunch(b->graph, b->stream));
   } else {
-    for (bd_ctx* c : b->ctx) {
-      int rc = step_device(c, c->rr, c->p);
-      if (rc) return rc;
-    }
+    int rc = batch_enqueue(b);
+    if (rc) return rc;
   }
   for (bd_ctx* c : b->ctx) c->step_count++;
   return BD_OK;
@@ -836,6 +897,7 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
   if (!b) return BD_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  bdk::mixed_batch_free(b->chol);
   for (bd_ctx* c : b->ctx) bd_destroy(c);
   for (bd_noise* g : b->noise) bd_noise_free(g);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);

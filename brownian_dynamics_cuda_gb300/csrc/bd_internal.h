@@ -149,6 +149,14 @@ int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* 
                 double* kbytes = nullptr);
 int mixed_tiles(int m);
 int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at most
+// Many mixed factorisations (replicas) advanced together: launch i runs step
+// i of every factorisation's schedule (k_chol_step_multi), then one diagonal
+// scatter for all.  The plan holds the matrices' addresses.
+struct MixedBatch;
+MixedBatch* mixed_batch_create(int nrep, const int* m, double* const* A, const int* lda, unsigned char* const* PS,
+                               int* const* negpiv, int* const* err);
+int mixed_batch_run(const MixedBatch* b, cudaStream_t st);  // returns the launches issued
+void mixed_batch_free(MixedBatch* b);
 
 void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt, double* rd, double* part,
                    cudaStream_t st, bool df = false);

@@ -29,6 +29,8 @@
 // potrf_mixed).  Every mbarrier wait is bounded; on a timeout the kernel
 // records an error code, frees its tensor memory and returns.
 #include <algorithm>
+#include <utility>
+#include <vector>
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -928,9 +930,7 @@ struct StepArgs {
 // tiles below it, writing its slices to PSp); then the CTAs of update job 0,
 // then those of job 1.  The parts of one launch touch disjoint tiles and
 // slice buffers.
-__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_constant__ StepArgs a) {
-  extern __shared__ float4 smem4[];
-  int b = (int)blockIdx.x;
+__device__ __forceinline__ void chol_step_body(const StepArgs& a, int b, float4* smem4) {
   if (b < a.ndp) {
     dpanel_body(smem4, a.A, a.Ldg, a.lda, a.m, a.pk0, a.pkb, a.pk0 / kT + 1, b, a.PSp, a.negpiv, a.PSpre, a.err,
                 a.prows);
@@ -951,15 +951,50 @@ __global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_cons
                  j.ps, nullptr, nullptr, a.err);
 }
 
+__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step(const __grid_constant__ StepArgs a) {
+  extern __shared__ float4 smem4[];
+  chol_step_body(a, (int)blockIdx.x, smem4);
+}
+
+// The same step for many independent factorisations in one launch (replicas
+// of a batch): factorisation r owns CTAs [off[r], off[r + 1]) and runs its own
+// schedule's step with args[r]; the factorisations share no memory.
+__global__ void __launch_bounds__(kRestThreads, 1) k_chol_step_multi(const StepArgs* __restrict__ args,
+                                                                      const int* __restrict__ off, int nrep) {
+  extern __shared__ float4 smem4[];
+  const int bid = (int)blockIdx.x;
+  int lo = 0, hi = nrep;  // off[lo] <= bid < off[lo + 1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= bid) lo = mid;
+    else hi = mid;
+  }
+  chol_step_body(args[lo], bid - off[lo], smem4);
+}
+
 // After the last panel: the diagonal factors L_kk from the side buffer into
 // the lower triangles of A's diagonal blocks, as (L, 0) pairs.
-__global__ void __launch_bounds__(256) k_diag_scatter(float2* A, int lda, int m, const float* __restrict__ Ld) {
-  const int k = blockIdx.x, k0 = k * kT, kb = min(kT, m - k0);
+__device__ __forceinline__ void diag_scatter_body(float2* A, int lda, int m, const float* __restrict__ Ld, int k) {
+  const int k0 = k * kT, kb = min(kT, m - k0);
   const float* src = Ld + (size_t)k * kT * kT;
   for (int e = threadIdx.x; e < kT * kT; e += blockDim.x) {
     const int c = e >> 7, r = e & (kT - 1);
     if (r >= c && r < kb && c < kb) A[(size_t)(k0 + c) * lda + k0 + r] = make_float2(src[e], 0.f);
   }
+}
+__global__ void __launch_bounds__(256) k_diag_scatter(float2* A, int lda, int m, const float* __restrict__ Ld) {
+  diag_scatter_body(A, lda, m, Ld, blockIdx.x);
+}
+struct ScatterArgs {
+  float2* A;
+  int lda, m;
+  const float* Ld;
+};
+// every factorisation of a batch (blockIdx.y), diagonal block blockIdx.x
+__global__ void __launch_bounds__(256) k_diag_scatter_multi(const ScatterArgs* __restrict__ sc) {
+  const ScatterArgs a = sc[blockIdx.y];
+  if ((int)blockIdx.x * kT >= a.m) return;
+  diag_scatter_body(a.A, a.lda, a.m, a.Ld, blockIdx.x);
 }
 
 }  // namespace
@@ -981,6 +1016,8 @@ int set_mixed_attributes() {
   if (g_attr_done) return 0;
   static_assert(kDpSmem <= kRestSmem, "panel CTAs run inside the update kernel's shared memory");
   cudaError_t e = cudaFuncSetAttribute(k_chol_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRestSmem);
+  if (e != cudaSuccess) return 1;
+  e = cudaFuncSetAttribute(k_chol_step_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRestSmem);
   if (e != cudaSuccess) return 1;
   g_attr_done = true;
   return 0;
@@ -1039,8 +1076,11 @@ struct Job {
 };
 }  // namespace
 
-int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
-                cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes) {
+// The launches of one factorisation: issued on st, or (plan != nullptr)
+// only recorded with their grid sizes, without the final diagonal scatter.
+static int potrf_mixed_impl(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
+                            cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes,
+                            std::vector<std::pair<StepArgs, int>>* plan) {
   float2* A = reinterpret_cast<float2*>(A64);  // double-float storage, 8 bytes per element
   const int nt = cdiv(m, kT);
   const size_t buf = (size_t)nt * kTileBytes;
@@ -1098,6 +1138,10 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
       grid += u.nctas;
     }
     if (grid == 0) return;
+    if (plan) {
+      plan->emplace_back(a, grid);
+      return;
+    }
     if (kev) cudaEventRecord(kev[2 * timed], st);
     k_chol_step<<<grid, kRestThreads, kRestSmem, st>>>(a);
     if (kev) {
@@ -1136,10 +1180,96 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
       k += 1;
     }
   }
+  if (plan) return L;
   k_diag_scatter<<<nt, 256, 0, st>>>(A, lda, m, Ld);
   L++;
   if (kev_pairs) *kev_pairs = timed;
   return L;
+}
+
+int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
+                cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes) {
+  return potrf_mixed_impl(m, A64, lda, PS, negpiv, err, st, kev, kev_pairs, kflop, kbytes, nullptr);
+}
+
+// Factorisations of a batch advanced together: launch i of the batch runs
+// step i of every factorisation whose schedule has one, each in its own CTA
+// range; the step arguments and CTA offsets of every launch are uploaded
+// once (the matrices and buffers do not move).
+struct MixedBatch {
+  std::vector<int> nrep_at, grid_at;
+  std::vector<size_t> args_at, off_at;
+  StepArgs* d_args = nullptr;
+  int* d_off = nullptr;
+  ScatterArgs* d_sc = nullptr;
+  int nrep = 0, max_nt = 0;
+};
+
+MixedBatch* mixed_batch_create(int nrep, const int* m, double* const* A, const int* lda, unsigned char* const* PS,
+                               int* const* negpiv, int* const* err) {
+  std::vector<std::vector<std::pair<StepArgs, int>>> plans(nrep);
+  size_t steps = 0;
+  MixedBatch* b = new MixedBatch();
+  b->nrep = nrep;
+  std::vector<ScatterArgs> sc(nrep);
+  for (int r = 0; r < nrep; r++) {
+    potrf_mixed_impl(m[r], A[r], lda[r], PS[r], negpiv[r], err[r], nullptr, nullptr, nullptr, nullptr, nullptr,
+                     &plans[r]);
+    steps = std::max(steps, plans[r].size());
+    const int nt = cdiv(m[r], kT);
+    b->max_nt = std::max(b->max_nt, nt);
+    sc[r].A = reinterpret_cast<float2*>(A[r]);
+    sc[r].lda = lda[r];
+    sc[r].m = m[r];
+    sc[r].Ld = reinterpret_cast<const float*>(PS[r] + kBufs * (size_t)nt * kTileBytes);
+  }
+  std::vector<StepArgs> args;
+  std::vector<int> off;
+  for (size_t i = 0; i < steps; i++) {
+    b->args_at.push_back(args.size());
+    b->off_at.push_back(off.size());
+    int n = 0, total = 0;
+    for (int r = 0; r < nrep; r++) {
+      if (i >= plans[r].size()) continue;
+      args.push_back(plans[r][i].first);
+      off.push_back(total);
+      total += plans[r][i].second;
+      n++;
+    }
+    off.push_back(total);
+    b->nrep_at.push_back(n);
+    b->grid_at.push_back(total);
+  }
+  bool ok = cudaMalloc(&b->d_args, std::max<size_t>(1, args.size()) * sizeof(StepArgs)) == cudaSuccess &&
+            cudaMalloc(&b->d_off, std::max<size_t>(1, off.size()) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&b->d_sc, nrep * sizeof(ScatterArgs)) == cudaSuccess &&
+            cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(StepArgs), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(b->d_sc, sc.data(), nrep * sizeof(ScatterArgs), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    mixed_batch_free(b);
+    return nullptr;
+  }
+  return b;
+}
+
+int mixed_batch_run(const MixedBatch* b, cudaStream_t st) {
+  int L = 0;
+  for (size_t i = 0; i < b->grid_at.size(); i++) {
+    k_chol_step_multi<<<b->grid_at[i], kRestThreads, kRestSmem, st>>>(b->d_args + b->args_at[i],
+                                                                         b->d_off + b->off_at[i], b->nrep_at[i]);
+    L++;
+  }
+  k_diag_scatter_multi<<<dim3(b->max_nt, b->nrep), 256, 0, st>>>(b->d_sc);
+  return L + 1;
+}
+
+void mixed_batch_free(MixedBatch* b) {
+  if (!b) return;
+  if (b->d_args) cudaFree(b->d_args);
+  if (b->d_off) cudaFree(b->d_off);
+  if (b->d_sc) cudaFree(b->d_sc);
+  delete b;
 }
 
 }  // namespace bdk
