@@ -13,6 +13,7 @@
 //   Fa <- (F0 + F1)/2; Y <- move(X, Fa); X <- Y; frames(X).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -783,7 +784,13 @@ struct bd_batch {
   std::vector<bd_noise*> noise;
   std::vector<std::vector<double>> h_rr, h_p;
   bdk::MixedBatch* chol = nullptr;  // the replicas' factorisations as one launch per schedule step
+  // side streams: the replicas' position / tensor and move phases run on
+  // kBatchLanes streams side by side (no tensor-core kernel among them)
+  std::vector<cudaStream_t> lane;
+  std::vector<cudaEvent_t> ev;  // [0]: fork, [1 + k]: join of lane k
 };
+
+constexpr int kBatchLanes = 16;
 
 // One step of every replica.  Mixed precision, D rebuilt every step: the
 // positions and tensors of all replicas, then one batched factorisation
@@ -811,8 +818,33 @@ static int batch_prepare(bd_batch* b) {
     }
     b->chol = bdk::mixed_batch_create((int)nr, m.data(), A.data(), lda.data(), PS.data(), np.data(), er.data());
     if (!b->chol) return set_error(BD_ERR_NOMEM, "bd_batch: batched factorisation plan");
+    const int nl = (int)std::min<size_t>(nr, kBatchLanes);
+    b->lane.resize(nl, nullptr);
+    b->ev.resize(1 + nl, nullptr);
+    for (auto& s : b->lane) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    for (auto& e : b->ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   return BD_OK;
+}
+
+// run phase `ph` of every replica on the side streams, between a fork from
+// and a join back into the batch stream
+static int batch_lanes(bd_batch* b, int ph) {
+  const int nl = (int)b->lane.size();
+  CK(cudaEventRecord(b->ev[0], b->stream));
+  for (int k = 0; k < nl; k++) CK(cudaStreamWaitEvent(b->lane[k], b->ev[0], 0));
+  int rc = BD_OK;
+  for (size_t i = 0; i < b->ctx.size() && !rc; i++) {
+    bd_ctx* c = b->ctx[i];
+    c->stream = b->lane[i % nl];
+    rc = step_phases(c, c->rr, c->p, nullptr, ph);
+    c->stream = b->stream;
+  }
+  for (int k = 0; k < nl; k++) {
+    CK(cudaEventRecord(b->ev[1 + k], b->lane[k]));
+    CK(cudaStreamWaitEvent(b->stream, b->ev[1 + k], 0));
+  }
+  return rc;
 }
 
 static int batch_enqueue(bd_batch* b) {
@@ -822,14 +854,10 @@ static int batch_enqueue(bd_batch* b) {
       if (!rc) rc = step_device(c, c->rr, c->p);
     return rc;
   }
-  for (bd_ctx* c : b->ctx)
-    if (!rc) rc = step_phases(c, c->rr, c->p, nullptr, kPre);
-  if (rc) return rc;
-  bdk::mixed_batch_run(b->chol, b->stream);
+  if ((rc = batch_lanes(b, kPre))) return rc;
+  bdk::mixed_batch_run(b->chol, b->stream);  // alone on the GPU: the only tensor-core kernel of the step
   CK(cudaGetLastError());
-  for (bd_ctx* c : b->ctx)
-    if (!rc) rc = step_phases(c, c->rr, c->p, nullptr, kPost);
-  return rc;
+  return batch_lanes(b, kPost);
 }
 
 static int batch_device_step(bd_batch* b) {
@@ -898,6 +926,10 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   bdk::mixed_batch_free(b->chol);
+  for (auto s : b->lane)
+    if (s) cudaStreamDestroy(s);
+  for (auto e : b->ev)
+    if (e) cudaEventDestroy(e);
   for (bd_ctx* c : b->ctx) bd_destroy(c);
   for (bd_noise* g : b->noise) bd_noise_free(g);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
