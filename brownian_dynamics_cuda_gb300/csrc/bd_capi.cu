@@ -790,7 +790,7 @@ struct bd_batch {
   std::vector<cudaEvent_t> ev;  // [0]: fork, [1 + k]: join of lane k
 };
 
-constexpr int kBatchLanes = 16;
+constexpr int kBatchLanes = 64;
 
 // One step of every replica.  Mixed precision, D rebuilt every step: the
 // positions and tensors of all replicas, then one batched factorisation
