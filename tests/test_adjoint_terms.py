@@ -75,3 +75,32 @@ def test_terms_sum_to_oracle_forces(harness, name, fib):
     assert rel_err(F, ref["force"]) < 1e-10
     assert rel_err(T, ref["torque"]) < 1e-10
     assert rel_err(tF, ref["t_force"]) < 1e-10
+
+
+def _adjoint_fixture():
+    from brownian_dynamics_cuda_gb300 import Fiber
+    z = dict(np.load(os.path.join(ROOT, "tests", "golden", "adjoint", "ref_3nuc.npz")))
+    fib = Fiber.from_arrays({k[6:]: v for k, v in z.items() if k.startswith("fiber_")})
+    return fib, z
+
+
+def test_adjoint_reference_fixture_is_the_oracle():
+    """The oracle's FP64 reference gradient fixture (tests/golden/adjoint/,
+    made by make_adjoint_golden.py): its observable is the oracle's rollout
+    on the stored fiber and noise, and one of its central differences
+    reproduces."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mkadj", os.path.join(ROOT, "tests", "golden",
+                                                                        "make_adjoint_golden.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    fib, z = _adjoint_fixture()
+    assert mk.observable(fib, z["rr"], z["p"]) == float(z["loss"])
+    th = mk.theta_of(fib)
+    d = 5e-4 * th[3]
+    tp, tm = th.copy(), th.copy()
+    tp[3] += d
+    tm[3] -= d
+    g3 = (mk.observable(mk.with_theta(fib, tp), z["rr"], z["p"]) -
+          mk.observable(mk.with_theta(fib, tm), z["rr"], z["p"])) / (2 * d)
+    assert abs(g3 - z["grad"][3]) <= 1e-5 * abs(z["grad"][3])

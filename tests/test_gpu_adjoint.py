@@ -107,3 +107,22 @@ def test_adjoint_config3():
     loss, g = ctx.adjoint(rr, p, window=50, checkpoint_every=20)
     assert abs(loss - loss_fd) <= 1e-5 * abs(loss_fd)
     assert rel_vec(g, g_fd) <= 1e-4, (g, g_fd)
+
+
+def test_adjoint_matches_oracle_reference_gradient():
+    """bd_adjoint against the FP64 reference gradient that the CPU oracle
+    (bit for bit the reference's step) gives by Richardson-extrapolated
+    central differences (tests/golden/adjoint/ref_3nuc.npz)."""
+    import os
+    from brownian_dynamics_cuda_gb300 import Fiber
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    z = dict(np.load(os.path.join(root, "tests", "golden", "adjoint", "ref_3nuc.npz")))
+    fib = Fiber.from_arrays({k[6:]: v for k, v in z.items() if k.startswith("fiber_")})
+    w = int(z["window"])
+    c64 = Context(fib, precision=PREC_FP64)
+    loss, g = c64.adjoint(z["rr"], z["p"], window=w, checkpoint_every=4)
+    assert abs(loss - float(z["loss"])) <= 1e-12 * abs(float(z["loss"]))
+    assert rel_vec(g, z["grad"]) <= 1e-6, (g, z["grad"])
+    cmx = Context(fib, precision=PREC_MIXED)
+    _, gm = cmx.adjoint(z["rr"], z["p"], window=w, checkpoint_every=4)
+    assert rel_vec(gm, z["grad"]) <= 1e-4, (gm, z["grad"])
