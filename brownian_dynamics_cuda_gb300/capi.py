@@ -118,6 +118,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_dev_noise_step.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                     C.c_void_p]
     L.bd_dev_noise_free.argtypes = [C.c_void_p]
+    L.bd_set_lh_flags.argtypes = [C.c_void_p, _ip, _dp, _dp]
     L.bd_adjoint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.bd_rollout_loss.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp]
     L.bd_set_moduli.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -434,6 +435,16 @@ class Context:
         v = C.c_int()
         _check(self._L.bd_negative_pivots(self._h, C.byref(v)))
         return v.value
+
+    def set_lh_flags(self, nc_lh_flag: np.ndarray, r_lh: np.ndarray, lh_rad: np.ndarray | None = None) -> None:
+        """New linker-histone binding (bd_set_lh_flags); the sizes are re-read."""
+        f = np.ascontiguousarray(nc_lh_flag, dtype=np.int32)
+        r = np.ascontiguousarray(r_lh, dtype=np.float64)
+        rad = None if lh_rad is None else np.ascontiguousarray(lh_rad, dtype=np.float64)
+        _check(self._L.bd_set_lh_flags(self._h, _pi(f), _pd(r), _pd(rad)))
+        sz = (C.c_int * 8)()
+        _check(self._L.bd_sizes(self._h, sz))
+        self.n, self.n_c, self.n_tail, self.n_LH, self.n_D, self.m, self.lda, self.precision = list(sz)
 
     def adjoint(self, rr: np.ndarray, p: np.ndarray, window: int, checkpoint_every: int = 20) -> tuple:
         """(loss, d loss / d (h, g, s, Debye length)) of the rollout driven by the

@@ -200,6 +200,43 @@ int bdh::step_device(bd_ctx* c, const double* d_rr, const double* d_p, double* c
 using bdh::step_device;
 
 
+namespace {
+template <class T>
+std::vector<T> vec(const T* p, long n) {
+  return (p && n > 0) ? std::vector<T>(p, p + n) : std::vector<T>();
+}
+template <class T>
+const T* ptr(const std::vector<T>& v) {
+  return v.empty() ? nullptr : v.data();
+}
+}  // namespace
+
+void bdh::ModelCopy::take(const bd_model& s) {
+  m = s;
+  const long n = s.n, nc = s.n_c, Nq = s.Nq, nt0 = s.n_t, nt = s.n_tail, np = s.n_lh_n + s.n_lh_g + s.n_lh_c;
+  type = vec(s.type, n); rad = vec(s.rad, n); phi_o = vec(s.phi_o, n); r_var = vec(s.r_var, 3 * n);
+  core_pos = vec(s.core_pos, 3 * Nq); core_q = vec(s.core_q, Nq); tail_pos = vec(s.tail_pos, 3 * nt0);
+  tail_fix = vec(s.tail_fix, nt0); nc_t_flag = vec(s.nc_t_flag, nc);
+  h_t = vec(s.h_t, nt); g_t = vec(s.g_t, nt); lo_t = vec(s.lo_t, nt); beta_o_t = vec(s.beta_o_t, nt);
+  t_q = vec(s.t_q, nt); t_rad = vec(s.t_rad, nt); t_grp = vec(s.t_grp, nt); t_fix = vec(s.t_fix, nt);
+  LH_g_pos = vec(s.LH_g_pos, 3L * s.n_lh_g); LH_conn = vec(s.LH_conn, np); nc_lh_flag = vec(s.nc_lh_flag, nc);
+  LH_q = vec(s.LH_q, np); LH_vdw_hh = vec(s.LH_vdw_hh, np); LH_vdw_hc = vec(s.LH_vdw_hc, np);
+  LH_vdw_hl = vec(s.LH_vdw_hl, np); LH_vdw_ht = vec(s.LH_vdw_ht, np); LH_kstr = vec(s.LH_kstr, np);
+  LH_kben = vec(s.LH_kben, np); LH_streq = vec(s.LH_streq, np); LH_betaeq = vec(s.LH_betaeq, np);
+  lh_rad = vec(s.lh_rad, s.n_LH);
+  bind();
+}
+
+void bdh::ModelCopy::bind() {
+  m.type = ptr(type); m.rad = ptr(rad); m.phi_o = ptr(phi_o); m.r_var = ptr(r_var);
+  m.core_pos = ptr(core_pos); m.core_q = ptr(core_q); m.tail_pos = ptr(tail_pos); m.tail_fix = ptr(tail_fix);
+  m.nc_t_flag = ptr(nc_t_flag); m.h_t = ptr(h_t); m.g_t = ptr(g_t); m.lo_t = ptr(lo_t); m.beta_o_t = ptr(beta_o_t);
+  m.t_q = ptr(t_q); m.t_rad = ptr(t_rad); m.t_grp = ptr(t_grp); m.t_fix = ptr(t_fix); m.LH_g_pos = ptr(LH_g_pos);
+  m.LH_conn = ptr(LH_conn); m.nc_lh_flag = ptr(nc_lh_flag); m.LH_q = ptr(LH_q); m.LH_vdw_hh = ptr(LH_vdw_hh);
+  m.LH_vdw_hc = ptr(LH_vdw_hc); m.LH_vdw_hl = ptr(LH_vdw_hl); m.LH_vdw_ht = ptr(LH_vdw_ht); m.LH_kstr = ptr(LH_kstr);
+  m.LH_kben = ptr(LH_kben); m.LH_streq = ptr(LH_streq); m.LH_betaeq = ptr(LH_betaeq); m.lh_rad = ptr(lh_rad);
+}
+
 extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options* opt, bd_ctx** out) {
   if (!out || !s) return set_error(BD_ERR_ARG, "bd_create: null argument");
   int rc = validate(m);
@@ -210,6 +247,8 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
                              !s->alpha_p || !s->beta_p || !s->gamma_p))
     return set_error(BD_ERR_ARG, "bd_create: angles required when refresh_frames == 0");
   bd_ctx* c = new bd_ctx();
+  c->model = std::make_shared<bdh::ModelCopy>();
+  c->model->take(*m);
   if (opt) {
     c->precision = opt->precision;
     c->freq_rp = opt->frequency_RP > 0 ? opt->frequency_RP : 1;
@@ -1041,3 +1080,69 @@ extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double deb
   }
   return BD_OK;
 }
+
+// main.cpp:386-465 changes which cores carry a linker histone every 100
+// steps and with it n_LH and the size of D.  The context is rebuilt for the
+// new binding from its current device state (chain, tails, frames and
+// angles: the reference keeps them on the device, func_cuda.cu:3434-3490)
+// and the caller's LH positions (main.cpp rebuilds them on the host,
+// main.cpp:418-447), then takes the place of the old one.
+extern "C" int bd_set_lh_flags(bd_ctx* c, const int* nc_lh_flag, const double* r_lh, const double* lh_rad) {
+  if (!c || !nc_lh_flag || !c->model) return set_error(BD_ERR_ARG, "bd_set_lh_flags: null argument");
+  const bdh::ModelCopy& old = *c->model;
+  const int nc = old.m.n_c, n = old.m.n, nt = old.m.n_tail, nlh = old.m.n_lh_n + old.m.n_lh_c;
+  int bound = 0;
+  for (int k = 0; k < nc; k++) {
+    if (nc_lh_flag[k] != 0 && nc_lh_flag[k] != 1) return set_error(BD_ERR_ARG, "bd_set_lh_flags: flags are 0 or 1");
+    bound += nc_lh_flag[k];
+  }
+  const int nLH = bound * nlh;
+  if (nLH > 0 && !r_lh) return set_error(BD_ERR_ARG, "bd_set_lh_flags: LH positions required");
+  auto cp = std::make_shared<bdh::ModelCopy>(old);
+  cp->nc_lh_flag.assign(nc_lh_flag, nc_lh_flag + nc);
+  cp->m.n_LH = nLH;
+  if (lh_rad) {
+    cp->lh_rad.assign(lh_rad, lh_rad + nLH);
+  } else {  // every linker histone has the same beads: repeat the first one's radii
+    std::vector<double> one(nlh, 0.5);
+    if ((int)old.lh_rad.size() >= nlh) one.assign(old.lh_rad.begin(), old.lh_rad.begin() + nlh);
+    cp->lh_rad.clear();
+    for (int k = 0; k < bound; k++) cp->lh_rad.insert(cp->lh_rad.end(), one.begin(), one.end());
+  }
+  cp->bind();
+  cudaStream_t st = c->stream;
+  auto down = [&](const double* d, long cnt, std::vector<double>& h) -> int {
+    h.resize(cnt);
+    if (cnt) CK(cudaMemcpyAsync(h.data(), d, cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return BD_OK;
+  };
+  std::vector<double> r, a, b, cc, rt, al, be, ga, le, ad, bd, cd, ap, bp, gp;
+  const DevState& X = c->X;
+  int rc = 0;
+  if ((rc = down(X.r, 3L * n, r)) || (rc = down(X.a, 3L * n, a)) || (rc = down(X.b, 3L * n, b)) ||
+      (rc = down(X.c, 3L * n, cc)) || (rc = down(X.r_t, 3L * nt, rt)) || (rc = down(X.alpha, n, al)) ||
+      (rc = down(X.beta, n, be)) || (rc = down(X.gamma, n, ga)) || (rc = down(X.length, n, le)) ||
+      (rc = down(X.a_dna, 3L * nc, ad)) || (rc = down(X.b_dna, 3L * nc, bd)) || (rc = down(X.c_dna, 3L * nc, cd)) ||
+      (rc = down(X.alpha_p, nc, ap)) || (rc = down(X.beta_p, nc, bp)) || (rc = down(X.gamma_p, nc, gp)))
+    return rc;
+  CK(cudaStreamSynchronize(st));
+  bd_state s{};
+  s.r = r.data(); s.a = a.data(); s.b = b.data(); s.c = cc.data(); s.r_t = rt.data(); s.r_lh = r_lh;
+  s.refresh_frames = 0;
+  s.alpha = al.data(); s.beta = be.data(); s.gamma = ga.data(); s.length = le.data();
+  s.a_dna = ad.data(); s.b_dna = bd.data(); s.c_dna = cd.data();
+  s.alpha_p = ap.data(); s.beta_p = bp.data(); s.gamma_p = gp.data();
+  bd_options o{};
+  o.precision = c->precision;
+  o.frequency_RP = c->freq_rp;
+  o.use_graph = c->use_graph;
+  o.device = c->device;
+  o.stream = c->stream;
+  bd_ctx* fresh = nullptr;
+  if ((rc = bd_create(&cp->m, &s, &o, &fresh))) return rc;
+  fresh->step_count = c->step_count;
+  std::swap(*c, *fresh);
+  std::swap(c->own_stream, fresh->own_stream);  // the stream stays with the caller's handle
+  return bd_destroy(fresh);
+}
+

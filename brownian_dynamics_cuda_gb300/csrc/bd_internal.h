@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -165,6 +166,17 @@ void trmv_lower_ws(int m, const double* A, int lda, const double* p, double s2dt
 namespace bdh {
 struct AdjWork;                 // k_adjoint.cu: buffers of the rollout gradient
 void adj_free(AdjWork* w);
+
+// A deep copy of a bd_model (arrays owned here), kept by every context so
+// that it can be rebuilt for a new linker-histone binding (bd_set_lh_flags).
+struct ModelCopy {
+  bd_model m{};
+  std::vector<int> type, tail_fix, nc_t_flag, t_grp, t_fix, LH_conn, nc_lh_flag;
+  std::vector<double> rad, phi_o, r_var, core_pos, core_q, tail_pos, h_t, g_t, lo_t, beta_o_t, t_q, t_rad, LH_g_pos,
+      LH_q, LH_vdw_hh, LH_vdw_hc, LH_vdw_hl, LH_vdw_ht, LH_kstr, LH_kben, LH_streq, LH_betaeq, lh_rad;
+  void take(const bd_model& src);
+  void bind();  // m's array pointers into the vectors (null for empty ones)
+};
 }  // namespace bdh
 
 // One fiber on one device: every buffer is allocated at bd_create.
@@ -200,6 +212,7 @@ struct bd_ctx {
   std::vector<int> h_type;
   std::vector<double> h_rvar;  // rotational noise scale (bd_batch_run draws noise on the host)
   bdh::AdjWork* adj = nullptr;  // allocated by the first bd_adjoint / bd_rollout_loss
+  std::shared_ptr<bdh::ModelCopy> model;  // the model it was created from
 };
 
 namespace bdh {

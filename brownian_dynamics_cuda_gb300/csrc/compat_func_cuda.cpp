@@ -11,7 +11,8 @@
 //
 // Like the reference, the shim keeps one simulation per process.  The LH
 // binding Monte Carlo of main.cpp:386-465 may change n_LH; the shim then
-// rebuilds the context from the current host state.
+// resizes the context (bd_set_lh_flags) from its current device state and
+// the host's new LH beads.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -100,7 +101,7 @@ extern "C++" void main_cuda(int n_c, int nc3, int step, int number_of_steps, dou
   (void)nc3; (void)frequency_RP; (void)h; (void)g; (void)s; (void)debyell; (void)debye; (void)q_l; (void)k_e;
   (void)k_ex; (void)k_h1; (void)sigma_DNA_DNA; (void)sigma_DNA_Core; (void)sigma_Core_Core; (void)sigma_Tail_Tail;
   (void)sigma_Tail_Linker; (void)sigma_Tail_Core; (void)Nq; (void)Nq3; (void)n_t; (void)n_lh_n; (void)n_lh_g;
-  (void)n_lh_c; (void)n; (void)n3; (void)n_tail; (void)n_tail3; (void)n_LH3; (void)h_rad_all;
+  (void)n_lh_c; (void)n; (void)n3; (void)n_tail; (void)n_tail3; (void)n_LH3;
   Saved& S = g_sv;
   if (!S.have) {
     fprintf(stderr, "main_cuda: cuda_application_init_data was not called\n");
@@ -109,16 +110,13 @@ extern "C++" void main_cuda(int n_c, int nc3, int step, int number_of_steps, dou
   bool flags_changed = false;
   for (int i = 0; i < n_c; i++) flags_changed |= (S.nc_lh_flag[i] != nc_lh_flag[i]);
   if (g_ctx && (flags_changed || n_LH != S.n_LH)) {
-    // LH binding changed: rebuild from the current host state (main.cpp
-    // keeps r_lh current every step and r,a,b,c on sampling steps)
-    bd_destroy(g_ctx);
-    g_ctx = nullptr;
+    // LH binding changed: the chain, tails and frames stay as the device has
+    // them (the reference keeps them on the device); the LH beads and their
+    // radii come from the host, which main.cpp rebuilt (main.cpp:418-465)
     for (int i = 0; i < n_c; i++) S.nc_lh_flag[i] = nc_lh_flag[i];
     S.n_LH = n_LH;
-    S.r_lh = cp(h_r_lh, 3 * n_LH);
-    S.r = cp(h_r, 3 * S.n); S.a = cp(h_a, 3 * S.n); S.b = cp(h_b, 3 * S.n); S.c = cp(h_c, 3 * S.n);
-    S.r_t = cp(h_r_t, 3 * S.n_tail);
-    S.lh_rad.assign(n_LH, S.lh_rad.empty() ? 0.5 : S.lh_rad[0]);
+    int rc = bd_set_lh_flags(g_ctx, nc_lh_flag, h_r_lh, h_rad_all ? h_rad_all + S.n + S.n_tail : nullptr);
+    if (rc) die("main_cuda/bd_set_lh_flags", rc);
   }
   if (!g_ctx) {
     bd_model m{};

@@ -260,6 +260,15 @@ int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
 int bd_negative_pivots(bd_ctx* ctx, int* out);
 
+/* Linker-histone binding changed (main.cpp:386-465: every 100 steps one
+ * core may bind or release its linker histone, which changes n_LH and the
+ * size of D): the context is rebuilt in place for the new flags [n_c] from
+ * its current device state, with r_lh [3 n_LH] the new LH bead positions
+ * (bound cores in order, as main.cpp:418-447 builds them) and lh_rad [n_LH]
+ * their radii (NULL: the first linker histone's radii repeated).  The handle
+ * stays valid; sizes (bd_sizes) change.  Not for contexts inside a batch. */
+int bd_set_lh_flags(bd_ctx* ctx, const int* nc_lh_flag, const double* r_lh, const double* lh_rad);
+
 /* ---------------------------------------------------------------- gradients
  * No counterpart in the reference (main.cpp runs the dynamics forward only).
  *

@@ -1,0 +1,47 @@
+"""bd_set_lh_flags: a context resized in place for a new linker-histone
+binding (main.cpp:386-465 releases or binds one core's linker histone every
+100 steps) continues exactly as a context created from scratch with the same
+state and binding: same sizes, and bit-for-bit the same steps."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ANGLES = ("alpha", "beta", "gamma", "length", "a_dna", "b_dna", "c_dna", "alpha_p", "beta_p", "gamma_p")
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_release_one_linker_histone(tmp_path, prec):
+    from brownian_dynamics_cuda_gb300 import Context, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, make_fiber
+    fib = make_fiber(FiberSpec(4, [30] * 4, lh=True, seed=2), str(tmp_path))
+    nlh = fib.sizes["n_lh_n"] + fib.sizes["n_lh_c"]
+    a = Context(fib, precision=prec)
+    nz = Noise(5)
+    for s in range(2):
+        a.step(*nz.step(s, fib.arrays["r_var"], a.m))
+    flags = fib.arrays["nc_lh_flag"].copy()
+    assert flags.sum() == fib.sizes["n_c"]
+    flags[1] = 0  # core 1 releases its linker histone
+    keep = np.ones(fib.sizes["n_LH"], bool)
+    keep[nlh:2 * nlh] = False
+    r_lh = a.get("r_lh").reshape(-1, 3)[keep].ravel()
+    lh_rad = fib.arrays["lh_rad"][keep]
+    state = {k: a.get(k) for k in ("r", "a", "b", "c", "r_t")}
+    angles = {k: a.get(k) for k in ANGLES}
+    a.set_lh_flags(flags, r_lh, lh_rad)
+    n_lh = int(flags.sum()) * nlh
+    assert a.n_LH == n_lh and a.m == 3 * (fib.sizes["n"] + fib.sizes["n_tail"] + n_lh)
+    sizes = dict(fib.sizes, n_LH=n_lh)
+    arrays = dict(fib.arrays, nc_lh_flag=flags, lh_rad=lh_rad)
+    fib2 = dataclasses.replace(fib, sizes=sizes, arrays=arrays, state=dict(state, r_lh=r_lh))
+    b = Context(fib2, precision=prec, refresh=False, angles=angles)
+    for k in ("r", "a", "r_t", "r_lh", "beta"):
+        assert np.array_equal(a.get(k), b.get(k)), k
+    for s in range(2, 4):
+        rr, p = nz.step(s, fib.arrays["r_var"], a.m)
+        assert a.step(rr, p) == b.step(rr, p)
+        for k in ("r", "a", "r_t", "r_lh"):
+            assert np.array_equal(a.get(k), b.get(k)), (s, k)
