@@ -53,6 +53,53 @@ class bd_state(C.Structure):
                 ("c_dna", _dp), ("alpha_p", _dp), ("beta_p", _dp), ("gamma_p", _dp)]
 
 
+RESTART_ARRAYS = ("r", "a", "b", "c", "alpha", "beta", "gamma", "length", "a_dna", "b_dna", "c_dna", "alpha_p",
+                  "beta_p", "gamma_p", "r_t", "r_lh")
+
+
+class bd_restart(C.Structure):
+    _fields_ = [("step", C.c_long), ("n", C.c_int), ("n_c", C.c_int), ("n_tail", C.c_int), ("n_LH", C.c_int)] + \
+               [(k, _dp) for k in RESTART_ARRAYS] + [("nc_lh_flag", _ip)]
+
+
+def _restart_len(k: str, n: int, nc: int, nt: int, nl: int) -> int:
+    return {"r": 3 * n, "a": 3 * n, "b": 3 * n, "c": 3 * n, "alpha": n, "beta": n, "gamma": n, "length": n,
+            "a_dna": 3 * nc, "b_dna": 3 * nc, "c_dna": 3 * nc, "alpha_p": nc, "beta_p": nc, "gamma_p": nc,
+            "r_t": 3 * nt, "r_lh": 3 * nl}[k]
+
+
+def _restart_struct(step: int, n: int, nc: int, nt: int, nl: int, arrays: dict, flags: np.ndarray) -> bd_restart:
+    rs = bd_restart(step=step, n=n, n_c=nc, n_tail=nt, n_LH=nl)
+    for k in RESTART_ARRAYS:
+        setattr(rs, k, _pd(arrays[k]) if arrays[k].size else None)
+    rs.nc_lh_flag = _pi(flags)
+    return rs
+
+
+def restart_write(path: str, step: int, arrays: dict, nc_lh_flag: np.ndarray, noise: "Noise | None" = None) -> None:
+    """Binary restart (bd_restart_write): arrays as RESTART_ARRAYS (state, frames, angles)."""
+    L = load_library()
+    n, nc = arrays["alpha"].size, arrays["alpha_p"].size
+    nt, nl = arrays["r_t"].size // 3, arrays["r_lh"].size // 3
+    arrays = {k: np.ascontiguousarray(arrays[k], dtype=np.float64) for k in RESTART_ARRAYS}
+    flags = np.ascontiguousarray(nc_lh_flag, dtype=np.int32)
+    rs = _restart_struct(step, n, nc, nt, nl, arrays, flags)
+    _check(L.bd_restart_write(path.encode(), C.byref(rs), noise._h if noise is not None else None))
+
+
+def restart_read(path: str, noise: "Noise | None" = None) -> tuple:
+    """(step, arrays, nc_lh_flag, has_noise) of a restart; noise (if given) takes its generator state."""
+    L = load_library()
+    head, has = bd_restart(), C.c_int()
+    _check(L.bd_restart_info(path.encode(), C.byref(head), C.byref(has)))
+    n, nc, nt, nl = head.n, head.n_c, head.n_tail, head.n_LH
+    arrays = {k: np.zeros(_restart_len(k, n, nc, nt, nl)) for k in RESTART_ARRAYS}
+    flags = np.zeros(nc, dtype=np.int32)
+    rs = _restart_struct(0, n, nc, nt, nl, arrays, flags)
+    _check(L.bd_restart_read(path.encode(), C.byref(rs), noise._h if noise is not None else None))
+    return int(rs.step), arrays, flags, bool(has.value)
+
+
 class bd_options(C.Structure):
     _fields_ = [("precision", C.c_int), ("frequency_RP", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
                 ("stream", C.c_void_p)]
@@ -119,6 +166,12 @@ def load_library(path: str | None = None) -> C.CDLL:
                                     C.c_void_p]
     L.bd_dev_noise_free.argtypes = [C.c_void_p]
     L.bd_set_lh_flags.argtypes = [C.c_void_p, _ip, _dp, _dp]
+    L.bd_noise_get_state.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), _ip, _ip, _dp]
+    L.bd_noise_set_state.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int, C.c_int, C.c_double]
+    L.bd_restart_write.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
+    L.bd_restart_info.argtypes = [C.c_char_p, C.c_void_p, _ip]
+    L.bd_restart_read.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
+    L.bd_restart_from_context.argtypes = [C.c_void_p, C.c_void_p]
     L.bd_adjoint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.bd_rollout_loss.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp]
     L.bd_set_moduli.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -288,6 +341,19 @@ class Noise:
         _check(self._L.bd_noise_u32(self._h, count, out.ctypes.data_as(C.POINTER(C.c_uint32))))
         return out
 
+    def get_state(self) -> tuple:
+        """(words[624], index, have_cached, cached) of the generator."""
+        w = np.zeros(624, dtype=np.uint32)
+        idx, have, cached = C.c_int(), C.c_int(), C.c_double()
+        _check(self._L.bd_noise_get_state(self._h, w.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(idx),
+                                          C.byref(have), C.byref(cached)))
+        return w, idx.value, have.value, cached.value
+
+    def set_state(self, state: tuple) -> None:
+        w, idx, have, cached = state
+        w = np.ascontiguousarray(w, dtype=np.uint32)
+        _check(self._L.bd_noise_set_state(self._h, w.ctypes.data_as(C.POINTER(C.c_uint32)), idx, have, cached))
+
     def __del__(self):
         if getattr(self, "_h", None):
             self._L.bd_noise_free(self._h)
@@ -435,6 +501,14 @@ class Context:
         v = C.c_int()
         _check(self._L.bd_negative_pivots(self._h, C.byref(v)))
         return v.value
+
+    def restart_state(self) -> dict:
+        """The context's state, frames and angles (bd_restart_from_context), as RESTART_ARRAYS."""
+        nc = self.n_c
+        arrays = {k: np.zeros(_restart_len(k, self.n, nc, self.n_tail, self.n_LH)) for k in RESTART_ARRAYS}
+        rs = _restart_struct(0, self.n, nc, self.n_tail, self.n_LH, arrays, np.zeros(nc, dtype=np.int32))
+        _check(self._L.bd_restart_from_context(self._h, C.byref(rs)))
+        return arrays
 
     def set_lh_flags(self, nc_lh_flag: np.ndarray, r_lh: np.ndarray, lh_rad: np.ndarray | None = None) -> None:
         """New linker-histone binding (bd_set_lh_flags); the sizes are re-read."""

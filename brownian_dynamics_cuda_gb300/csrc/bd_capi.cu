@@ -1146,3 +1146,23 @@ extern "C" int bd_set_lh_flags(bd_ctx* c, const int* nc_lh_flag, const double* r
   return bd_destroy(fresh);
 }
 
+extern "C" int bd_restart_from_context(bd_ctx* c, bd_restart* rs) {
+  if (!c || !rs) return set_error(BD_ERR_ARG, "bd_restart_from_context: null argument");
+  const DevState& X = c->X;
+  const long n = c->M.n, nc = c->M.n_c, nt = c->M.n_tail, nl = c->M.n_LH;
+  rs->n = (int)n, rs->n_c = (int)nc, rs->n_tail = (int)nt, rs->n_LH = (int)nl;
+  const std::pair<double*, const double*> cp[] = {
+      {rs->r, X.r},         {rs->a, X.a},         {rs->b, X.b},         {rs->c, X.c},         {rs->alpha, X.alpha},
+      {rs->beta, X.beta},   {rs->gamma, X.gamma}, {rs->length, X.length}, {rs->a_dna, X.a_dna}, {rs->b_dna, X.b_dna},
+      {rs->c_dna, X.c_dna}, {rs->alpha_p, X.alpha_p}, {rs->beta_p, X.beta_p}, {rs->gamma_p, X.gamma_p},
+      {rs->r_t, X.r_t},     {rs->r_lh, X.r_lh}};
+  const long cnt[] = {3 * n, 3 * n, 3 * n, 3 * n, n, n, n, n, 3 * nc, 3 * nc, 3 * nc, nc, nc, nc, 3 * nt, 3 * nl};
+  for (int k = 0; k < 16; k++) {
+    if (!cnt[k]) continue;
+    if (!cp[k].first) return set_error(BD_ERR_ARG, "bd_restart_from_context: missing array");
+    CK(cudaMemcpyAsync(cp[k].first, cp[k].second, cnt[k] * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return BD_OK;
+}
+

@@ -498,3 +498,125 @@ extern "C" int bd_noise_u32(bd_noise* gp, int count, uint32_t* out) {
 }
 
 extern "C" void bd_noise_free(bd_noise* g) { delete reinterpret_cast<Mt19937*>(g); }
+
+extern "C" int bd_noise_get_state(const bd_noise* gp, uint32_t* words624, int* index, int* have_cached,
+                                  double* cached) {
+  if (!gp || !words624 || !index || !have_cached || !cached) return set_error(BD_ERR_ARG, "bd_noise_get_state: null argument");
+  const Mt19937& g = *reinterpret_cast<const Mt19937*>(gp);
+  std::memcpy(words624, g.st, sizeof g.st);
+  *index = g.idx;
+  *have_cached = g.have ? 1 : 0;
+  *cached = g.cached;
+  return BD_OK;
+}
+
+extern "C" int bd_noise_set_state(bd_noise* gp, const uint32_t* words624, int index, int have_cached, double cached) {
+  if (!gp || !words624 || index < 0 || index > 625) return set_error(BD_ERR_ARG, "bd_noise_set_state: bad argument");
+  Mt19937& g = *reinterpret_cast<Mt19937*>(gp);
+  std::memcpy(g.st, words624, sizeof g.st);
+  g.idx = index;
+  g.have = have_cached != 0;
+  g.cached = cached;
+  return BD_OK;
+}
+
+// ---------------------------------------------------------------- restart
+namespace {
+const char kRestartMagic[8] = {'B', 'D', 'R', 'S', 'T', '0', '0', '1'};
+
+struct RestartHead {
+  char magic[8];
+  int32_t n, n_c, n_tail, n_LH, has_noise, pad;
+  int64_t step;
+};
+
+// the arrays of a restart in file order, with their lengths
+std::vector<std::pair<double*, size_t>> restart_arrays(const bd_restart& r) {
+  const size_t n = r.n, nc = r.n_c, nt = r.n_tail, nl = r.n_LH;
+  return {{r.r, 3 * n},       {r.a, 3 * n},       {r.b, 3 * n},       {r.c, 3 * n},      {r.alpha, n},
+          {r.beta, n},        {r.gamma, n},       {r.length, n},      {r.a_dna, 3 * nc}, {r.b_dna, 3 * nc},
+          {r.c_dna, 3 * nc},  {r.alpha_p, nc},    {r.beta_p, nc},     {r.gamma_p, nc},   {r.r_t, 3 * nt},
+          {r.r_lh, 3 * nl}};
+}
+
+bool sizes_ok(const bd_restart& r) { return r.n > 0 && r.n_c > 0 && r.n_tail >= 0 && r.n_LH >= 0; }
+}  // namespace
+
+extern "C" int bd_restart_write(const char* path, const bd_restart* rs, const bd_noise* g) {
+  if (!path || !rs || !sizes_ok(*rs) || !rs->nc_lh_flag) return set_error(BD_ERR_ARG, "bd_restart_write: bad argument");
+  for (auto& a : restart_arrays(*rs))
+    if (a.second && !a.first) return set_error(BD_ERR_ARG, "bd_restart_write: missing array");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_error(BD_ERR_IO, "bd_restart_write: cannot open file");
+  RestartHead h{};
+  std::memcpy(h.magic, kRestartMagic, 8);
+  h.n = rs->n, h.n_c = rs->n_c, h.n_tail = rs->n_tail, h.n_LH = rs->n_LH, h.has_noise = g ? 1 : 0;
+  h.step = rs->step;
+  bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+  for (auto& a : restart_arrays(*rs))
+    if (a.second) ok = ok && std::fwrite(a.first, sizeof(double), a.second, f) == a.second;
+  ok = ok && std::fwrite(rs->nc_lh_flag, sizeof(int32_t), rs->n_c, f) == (size_t)rs->n_c;
+  if (g) {
+    const Mt19937& m = *reinterpret_cast<const Mt19937*>(g);
+    const int32_t idx = m.idx, have = m.have ? 1 : 0;
+    ok = ok && std::fwrite(m.st, sizeof m.st, 1, f) == 1 && std::fwrite(&idx, 4, 1, f) == 1 &&
+         std::fwrite(&have, 4, 1, f) == 1 && std::fwrite(&m.cached, 8, 1, f) == 1;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? BD_OK : set_error(BD_ERR_IO, "bd_restart_write: write failed");
+}
+
+static int read_head(FILE* f, RestartHead& h) {
+  if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kRestartMagic, 8) != 0)
+    return set_error(BD_ERR_IO, "bd_restart: not a restart file");
+  if (h.n <= 0 || h.n_c <= 0 || h.n_tail < 0 || h.n_LH < 0) return set_error(BD_ERR_IO, "bd_restart: bad sizes");
+  return BD_OK;
+}
+
+extern "C" int bd_restart_info(const char* path, bd_restart* rs, int* has_noise) {
+  if (!path || !rs) return set_error(BD_ERR_ARG, "bd_restart_info: null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(BD_ERR_IO, "bd_restart_info: cannot open file");
+  RestartHead h{};
+  int rc = read_head(f, h);
+  std::fclose(f);
+  if (rc) return rc;
+  rs->step = (long)h.step, rs->n = h.n, rs->n_c = h.n_c, rs->n_tail = h.n_tail, rs->n_LH = h.n_LH;
+  if (has_noise) *has_noise = h.has_noise;
+  return BD_OK;
+}
+
+extern "C" int bd_restart_read(const char* path, bd_restart* rs, bd_noise* g) {
+  if (!path || !rs || !rs->nc_lh_flag) return set_error(BD_ERR_ARG, "bd_restart_read: bad argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(BD_ERR_IO, "bd_restart_read: cannot open file");
+  RestartHead h{};
+  int rc = read_head(f, h);
+  if (!rc && (h.n != rs->n || h.n_c != rs->n_c || h.n_tail != rs->n_tail || h.n_LH != rs->n_LH))
+    rc = set_error(BD_ERR_ARG, "bd_restart_read: sizes differ from the file's");
+  bool ok = !rc;
+  for (auto& a : restart_arrays(*rs)) {
+    if (!ok) break;
+    if (a.second && !a.first) {
+      rc = set_error(BD_ERR_ARG, "bd_restart_read: missing array");
+      ok = false;
+      break;
+    }
+    if (a.second) ok = std::fread(a.first, sizeof(double), a.second, f) == a.second;
+  }
+  ok = ok && std::fread(rs->nc_lh_flag, sizeof(int32_t), rs->n_c, f) == (size_t)rs->n_c;
+  if (ok && g && h.has_noise) {
+    Mt19937& m = *reinterpret_cast<Mt19937*>(g);
+    int32_t idx = 0, have = 0;
+    double cached = 0.0;
+    ok = std::fread(m.st, sizeof m.st, 1, f) == 1 && std::fread(&idx, 4, 1, f) == 1 &&
+         std::fread(&have, 4, 1, f) == 1 && std::fread(&cached, 8, 1, f) == 1;
+    m.idx = idx, m.have = have != 0, m.cached = cached;
+  }
+  std::fclose(f);
+  if (rc) return rc;
+  if (!ok) return set_error(BD_ERR_IO, "bd_restart_read: truncated file");
+  rs->step = (long)h.step;
+  return BD_OK;
+}
+

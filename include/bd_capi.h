@@ -135,6 +135,37 @@ int bd_noise_create(unsigned long seed, bd_noise** out);
 int bd_noise_step(bd_noise* g, int step, int n3, const double* r_var, int n_D3, double* rr, double* p);
 int bd_noise_u32(bd_noise* g, int count, uint32_t* out);
 void bd_noise_free(bd_noise* g);
+/* The generator's full state: the 624 MT19937 words, the index of the next
+ * word, and the pending second deviate of the polar method. */
+int bd_noise_get_state(const bd_noise* g, uint32_t* words624, int* index, int* have_cached, double* cached);
+int bd_noise_set_state(bd_noise* g, const uint32_t* words624, int index, int have_cached, double cached);
+
+/* ---------------------------------------------------------------- restart
+ * Binary restart of one fiber: the step counter, positions, frames and the
+ * internal coordinates (so that a context created from it with
+ * refresh_frames = 0 continues bit for bit), the LH binding and, optionally,
+ * the noise generator's state.  The reference's restart (readfile.cpp:346-441)
+ * is text, positions only, and reseeds the generator.  Little-endian, file
+ * magic "BDRST001".  Array sizes are those of bd_state and bd_model. */
+typedef struct bd_restart {
+  long step;
+  int n, n_c, n_tail, n_LH;
+  double *r, *a, *b, *c;                                /* [3n]            */
+  double *alpha, *beta, *gamma, *length;                /* [n]             */
+  double *a_dna, *b_dna, *c_dna;                        /* [3 n_c]         */
+  double *alpha_p, *beta_p, *gamma_p;                   /* [n_c]           */
+  double *r_t, *r_lh;                                   /* [3 n_tail] [3 n_LH] */
+  int* nc_lh_flag;                                      /* [n_c]           */
+} bd_restart;
+/* Writes rs (all arrays given) and, if g is not NULL, g's state. */
+int bd_restart_write(const char* path, const bd_restart* rs, const bd_noise* g);
+/* Reads the header: step and sizes into rs (arrays untouched); *has_noise. */
+int bd_restart_info(const char* path, bd_restart* rs, int* has_noise);
+/* Reads everything into rs's arrays (sizes must match the file's) and, if g
+ * is not NULL and the file has it, the generator's state into g. */
+int bd_restart_read(const char* path, bd_restart* rs, bd_noise* g);
+/* bd_restart_from_context (below, with the context calls) fills one from a
+ * context. */
 /* The same stream generated on the device (one CTA per generator; state in
  * device memory): bd_dev_noise_step writes step `step`'s draws into device
  * arrays d_rr [n3] (scaled by d_r_var) and d_p [n_D3], stream-ordered on
@@ -259,6 +290,11 @@ int bd_kernel_bytes(bd_ctx* ctx, double* bytes);
 int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
 int bd_negative_pivots(bd_ctx* ctx, int* out);
+
+/* A context's current state (device) into rs's arrays, which must be
+ * allocated for the context's sizes (bd_sizes); rs's sizes are set from the
+ * context, rs->step and rs->nc_lh_flag are left to the caller. */
+int bd_restart_from_context(bd_ctx* ctx, bd_restart* rs);
 
 /* Linker-histone binding changed (main.cpp:386-465: every 100 steps one
  * core may bind or release its linker histone, which changes n_LH and the

@@ -1,0 +1,60 @@
+"""Binary restart files (bd_restart_*) and the noise generator's state
+(bd_noise_get_state / bd_noise_set_state) on the CPU: a generator restored
+from a saved state continues the stream bit for bit; a restart file returns
+exactly what was written, rejects foreign and truncated files and size
+mismatches."""
+import numpy as np
+import pytest
+
+from brownian_dynamics_cuda_gb300 import BDError, Noise
+from brownian_dynamics_cuda_gb300.capi import RESTART_ARRAYS, _restart_len, restart_read, restart_write
+
+
+def test_noise_state_round_trip():
+    r_var = np.linspace(0.1, 1.0, 33)
+    g = Noise(7)
+    for s in range(3):
+        g.step(s, r_var, 100)  # 133 draws per step: a cached deviate is pending after 3 steps
+    st = g.get_state()
+    assert st[2] == 1
+    h = Noise(1)
+    h.set_state(st)
+    for s in range(3, 6):
+        a, b = g.step(s, r_var, 100), h.step(s, r_var, 100)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def _arrays(n=7, nc=2, nt=5, nl=3, seed=0):
+    rng = np.random.default_rng(seed)
+    return {k: rng.normal(size=_restart_len(k, n, nc, nt, nl)) for k in RESTART_ARRAYS}
+
+
+def test_restart_round_trip(tmp_path):
+    arrays = _arrays()
+    flags = np.array([1, 0], dtype=np.int32)
+    g = Noise(11)
+    g.step(0, np.ones(21), 45)
+    path = str(tmp_path / "run.rst")
+    restart_write(path, 1234, arrays, flags, g)
+    h = Noise(3)
+    step, back, fl, has = restart_read(path, h)
+    assert step == 1234 and has and np.array_equal(fl, flags)
+    for k in RESTART_ARRAYS:
+        assert np.array_equal(back[k], arrays[k]), k
+    a, b = g.step(1, np.ones(21), 45), h.step(1, np.ones(21), 45)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_restart_rejects_bad_files(tmp_path):
+    path = str(tmp_path / "x.rst")
+    with open(path, "wb") as f:
+        f.write(b"NOTARESTARTFILE" * 4)
+    with pytest.raises(BDError):
+        restart_read(path)
+    good = str(tmp_path / "g.rst")
+    restart_write(good, 5, _arrays(), np.array([1, 1], dtype=np.int32))
+    data = open(good, "rb").read()
+    with open(path, "wb") as f:
+        f.write(data[:len(data) // 2])
+    with pytest.raises(BDError):
+        restart_read(path)
