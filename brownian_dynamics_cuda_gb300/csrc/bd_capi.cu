@@ -954,6 +954,7 @@ extern "C" int bd_batch_create(int nrep, const bd_model* models, const bd_state*
       bd_batch_destroy(b);
       return rc;
     }
+    c->in_batch = true;
     b->ctx.push_back(c);
   }
   *out = b;
@@ -1065,6 +1066,7 @@ extern "C" int bd_batch_run(bd_batch* b, int nsteps, unsigned long seed_base, do
 
 extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double debye_length) {
   if (!c || !(debye_length > 0.0)) return set_error(BD_ERR_ARG, "bd_set_moduli: bad argument");
+  if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_moduli: the context belongs to a batch");
   DevModel& M = c->M;
   const double kap = 1.0 / debye_length;
   M.debyell = M.debyell * (kap / M.debye);
@@ -1089,6 +1091,7 @@ extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double deb
 // main.cpp:418-447), then takes the place of the old one.
 extern "C" int bd_set_lh_flags(bd_ctx* c, const int* nc_lh_flag, const double* r_lh, const double* lh_rad) {
   if (!c || !nc_lh_flag || !c->model) return set_error(BD_ERR_ARG, "bd_set_lh_flags: null argument");
+  if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_lh_flags: the context belongs to a batch");
   const bdh::ModelCopy& old = *c->model;
   const int nc = old.m.n_c, n = old.m.n, nt = old.m.n_tail, nlh = old.m.n_lh_n + old.m.n_lh_c;
   int bound = 0;

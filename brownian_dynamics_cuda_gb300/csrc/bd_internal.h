@@ -213,6 +213,7 @@ struct bd_ctx {
   std::vector<double> h_rvar;  // rotational noise scale (bd_batch_run draws noise on the host)
   bdh::AdjWork* adj = nullptr;  // allocated by the first bd_adjoint / bd_rollout_loss
   std::shared_ptr<bdh::ModelCopy> model;  // the model it was created from
+  bool in_batch = false;  // owned by a bd_batch (whose graph and plans hold its buffers and constants)
 };
 
 namespace bdh {

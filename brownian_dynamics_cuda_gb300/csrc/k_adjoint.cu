@@ -134,7 +134,7 @@ template <class R>
 __global__ void k_adj_dnadna(DevModel M, const double* __restrict__ x, const double* __restrict__ fb, double* lam,
                              double* th) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n = M.n, n3 = 3 * n;
+  const int n = M.n;
   const int i = t / n, j = t % n;
   R kb = R(0);
   if (t < n * n && i < j && j - i > 1 && M.type[i] == 0 && M.type[j] == 0 && pair_ok(M, i, j)) {
@@ -163,7 +163,6 @@ __global__ void k_adj_dnadna(DevModel M, const double* __restrict__ x, const dou
   }
   kb = warp_sum(kb);
   if ((threadIdx.x & 31) == 0 && kb != R(0)) atomicAdd(th + 4, (double)kb);
-  (void)n3;
 }
 
 // ------------------------------------------------------------ DNA-core

@@ -104,7 +104,7 @@ __device__ __forceinline__ void emit(int i, double z, int n3, const double* r_va
 __global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n3, const double* __restrict__ r_var,
                                                         int nD3, double* rr, double* p) {
   __shared__ uint32_t st[kN];
-  __shared__ int s_idx, s_have, s_o, s_carry_ok, s_stop, s_done;
+  __shared__ int s_idx, s_have, s_o, s_carry_ok, s_stop;
   __shared__ uint32_t s_carry;
   __shared__ double s_cached;
   __shared__ int wsum[kThreads / 32];
@@ -116,7 +116,6 @@ __global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n
     s_cached = G->cached;
     s_o = 0;
     s_carry_ok = 0;
-    s_done = 0;
   }
   __syncthreads();
   const int N = n3 + nD3;
@@ -220,7 +219,6 @@ __global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n
     G->have = s_have;
     G->cached = s_cached;
   }
-  (void)s_done;
 }
 
 }  // namespace
