@@ -50,6 +50,10 @@ def _fibers():
         if fib.sizes["n_LH"] == 0:
             out.append((name, fib))
     out.append(("syn_4nuc_30bp", make_fiber(FiberSpec(4, [30] * 4, lh=False, seed=3), tempfile.mkdtemp())))
+    # uneven linkers (2 to 7 beads) at low salt: longer Debye length, more
+    # pairs inside the cut-offs, DNA-DNA pairs within the 8 nm LJ range
+    out.append(("syn_5nuc_uneven_50mM", make_fiber(FiberSpec(5, [20, 60, 26, 44, 30], lh=False, cs=0.050, seed=7),
+                                                   tempfile.mkdtemp())))
     return out
 
 
