@@ -166,6 +166,7 @@ def load_library(path: str | None = None) -> C.CDLL:
                                     C.c_void_p]
     L.bd_dev_noise_free.argtypes = [C.c_void_p]
     L.bd_set_lh_flags.argtypes = [C.c_void_p, _ip, _dp, _dp]
+    L.bd_em_update.argtypes = [C.c_void_p] + [_dp] * 6
     L.bd_noise_get_state.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), _ip, _ip, _dp]
     L.bd_noise_set_state.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int, C.c_int, C.c_double]
     L.bd_restart_write.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
@@ -457,6 +458,12 @@ class Context:
         rd = np.zeros(self.m)
         _check(self._L.bd_noise_displacement(self._h, _pd(p), _pd(rd)))
         return rd
+
+    def em_update(self, F: np.ndarray, T: np.ndarray, tF: np.ndarray, lF: np.ndarray, rr: np.ndarray,
+                  rd: np.ndarray) -> None:
+        """One Ermak-McCammon move with these forces and noise (bd_em_update)."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (F, T, tF, lF, rr, rd)]
+        _check(self._L.bd_em_update(self._h, *[_pd(x) if x.size else None for x in a]))
 
     def get(self, name: str) -> np.ndarray:
         cnt = C.c_int()

@@ -1169,3 +1169,36 @@ extern "C" int bd_restart_from_context(bd_ctx* c, bd_restart* rs) {
   return BD_OK;
 }
 
+// One Ermak-McCammon move of the context's state with caller forces and
+// noise: rotation_cal + rotate (func_cuda.cu:681-704, func.cpp:1607-1670),
+// translation_cal with the species-block RPY drift (func_cuda.cu:650-679),
+// then the frame refresh (update_Euler_Angle) - one half of main_cuda's
+// predictor-corrector step.
+extern "C" int bd_em_update(bd_ctx* c, const double* F, const double* T, const double* tF, const double* lF,
+                            const double* rr, const double* rd) {
+  if (!c || !F || !T || !rr || !rd || (c->M.n_tail && !tF) || (c->M.n_LH && !lF))
+    return set_error(BD_ERR_ARG, "bd_em_update: null argument");
+  const DevModel& M = c->M;
+  cudaStream_t st = c->stream;
+  const size_t d = sizeof(double), n3 = 3 * (size_t)M.n, nt3 = 3 * (size_t)M.n_tail, nl3 = 3 * (size_t)M.n_LH;
+  CK(cudaMemcpyAsync(c->F0.F, F, n3 * d, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->F0.T, T, n3 * d, cudaMemcpyHostToDevice, st));
+  if (nt3) CK(cudaMemcpyAsync(c->F0.tF, tF, nt3 * d, cudaMemcpyHostToDevice, st));
+  if (nl3) CK(cudaMemcpyAsync(c->F0.lF, lF, nl3 * d, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->rr, rr, n3 * d, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->rd, rd, (size_t)c->m * d, cudaMemcpyHostToDevice, st));
+  const bool mixed = c->precision == BD_PREC_MIXED;
+  bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
+  bdk::rotate_translate(M, c->X, c->Y, c->F0, c->rr, c->rd, c->r_all, c->precision, c->S, st);
+  CK(cudaMemcpyAsync(c->X.r, c->Y.r, n3 * d, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->X.a, c->Y.a, n3 * d, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->X.b, c->Y.b, n3 * d, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->X.c, c->Y.c, n3 * d, cudaMemcpyDeviceToDevice, st));
+  if (nt3) CK(cudaMemcpyAsync(c->X.r_t, c->Y.r_t, nt3 * d, cudaMemcpyDeviceToDevice, st));
+  if (nl3) CK(cudaMemcpyAsync(c->X.r_lh, c->Y.r_lh, nl3 * d, cudaMemcpyDeviceToDevice, st));
+  bdk::frames(M, c->X, st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return BD_OK;
+}
+

@@ -216,6 +216,13 @@ int bd_diffusion_tensor(bd_ctx* ctx, double* D);
 int bd_cholesky(bd_ctx* ctx, double* L);
 /* Noise displacement rd = sqrt(2 dt) L p for the current state, rd[m]. */
 int bd_noise_displacement(bd_ctx* ctx, const double* p, double* rd);
+/* One Ermak-McCammon move of the context's state with the caller's forces
+ * (force, torque [3n], t_force [3 n_tail], LH_force [3 n_LH]) and noise
+ * (rr [3n], rd [3 n_D]): frames rotated by dt tau / zeta + rr, positions
+ * moved by rd + del D_blk F (rotation_cal, rotate, translation_cal:
+ * func_cuda.cu:650-704, func.cpp:1607-1670), then the frames refreshed. */
+int bd_em_update(bd_ctx* ctx, const double* force, const double* torque, const double* t_force,
+                 const double* LH_force, const double* rr, const double* rd);
 
 /* Named state arrays (host copies): r a b c r_t r_lh alpha beta gamma length
  * a_dna b_dna c_dna alpha_p beta_p gamma_p beta_t beta_lh rd force torque

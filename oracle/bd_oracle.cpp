@@ -1225,6 +1225,31 @@ extern "C" double orc_step(void* h, const double* rr, const double* p) {
   return f0.E;
 }
 
+// One move with caller forces and noise: rotation_cal + rotate, then
+// translation_cal with the RPY tensor of the current state, then the
+// frame refresh (the body of one predictor or corrector half of orc_step).
+extern "C" int orc_em_update(void* h, const double* F, const double* T, const double* tF, const double* lF,
+                             const double* rr, const double* rd) {
+  System& S = *static_cast<System*>(h);
+  State& X = S.st;
+  const int m = 3 * S.n_D;
+  Vec ra, D;
+  rall(S, X, ra);
+  rpy(S, ra, D);
+  Forces f;
+  f.zero(S.n, S.n_tail, S.n_LH);
+  for (size_t i = 0; i < f.F.size(); i++) { f.F[i] = F[i]; f.T[i] = T[i]; }
+  for (size_t i = 0; i < f.tF.size(); i++) f.tF[i] = tF[i];
+  for (size_t i = 0; i < f.lF.size(); i++) f.lF[i] = lF[i];
+  Vec rdv(rd, rd + m);
+  State Y = X;
+  rotation(S, f.T, rr, X, Y.a, Y.b, Y.c);
+  translation(S, D, f, X, rdv, Y);
+  X.r = Y.r; X.a = Y.a; X.b = Y.b; X.c = Y.c; X.r_t = Y.r_t; X.r_lh = Y.r_lh;
+  refresh(S, X);
+  return 0;
+}
+
 extern "C" int orc_get(void* h, const char* nm, double* out) {
   System& S = *static_cast<System*>(h);
   State& X = S.st;

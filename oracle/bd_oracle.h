@@ -53,6 +53,8 @@ double orc_forces(void* h, double* force, double* torque, double* t_force, doubl
 void orc_tensor(void* h, double* D, double* L);
 // One predictor-corrector step with the given noise; returns pass-1 energy.
 double orc_step(void* h, const double* rr, const double* p);
+int orc_em_update(void* h, const double* F, const double* T, const double* tF, const double* lF, const double* rr,
+                  const double* rd);
 // Named state arrays: r a b c r_t r_lh alpha beta gamma length a_dna b_dna
 // c_dna alpha_p beta_p gamma_p beta_t beta_lh rd force torque t_force
 // LH_force.  Returns the length, or -1 for an unknown name.

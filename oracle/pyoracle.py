@@ -50,6 +50,7 @@ def lib() -> C.CDLL:
         L.orc_tensor.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_step.restype = C.c_double
         L.orc_step.argtypes = [C.c_void_p, _dp, _dp]
+        L.orc_em_update.argtypes = [C.c_void_p] + [_dp] * 6
         L.orc_get.argtypes = [C.c_void_p, C.c_char_p, _dp]
         L.orc_set.argtypes = [C.c_void_p, C.c_char_p, _dp]
         L.orc_cholesky.argtypes = [C.c_int, _dp, _dp, C.c_int]
@@ -115,6 +116,11 @@ class Oracle:
 
     def step(self, rr: np.ndarray, p: np.ndarray) -> float:
         return lib().orc_step(self._h, _pd(rr), _pd(p))
+
+    def em_update(self, F, T, tF, lF, rr, rd) -> None:
+        """One move with these forces and noise, then the frame refresh (orc_em_update)."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (F, T, tF, lF, rr, rd)]
+        lib().orc_em_update(self._h, *[_pd(x) if x.size else None for x in a])
 
     def get(self, name: str) -> np.ndarray:
         n = lib().orc_get(self._h, name.encode(), None)

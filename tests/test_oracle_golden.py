@@ -50,3 +50,25 @@ def test_oracle_steps(name):
             ref = z[f"step{s}_{k}"]
             if ref.size:
                 assert rel_err(o.get(k), ref) <= TOL, (s, k)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_em_update_composes_the_step(name):
+    """orc_em_update (the reference for bd_em_update) composed as main_cuda
+    does - predictor with the forces at the state, forces at the predicted
+    state, corrector from the state with the averaged forces - reproduces
+    the reference's golden step."""
+    fib, z = load_golden(name)
+    rr, rd = z["noise0_rr"], z["step0_rd"]
+    keys = ("force", "torque", "t_force", "LH_force")
+    o = Oracle(fib)
+    f0 = o.forces()
+    o.em_update(*[f0[k] for k in keys], rr, rd)
+    f1 = o.forces()
+    avg = [0.5 * (f0[k] + f1[k]) for k in keys]
+    c = Oracle(fib)
+    c.em_update(*avg, rr, rd)
+    for k in ("r", "a", "b", "c", "r_t", "r_lh"):
+        ref = z[f"step0_{k}"]
+        if ref.size:
+            assert rel_err(c.get(k), ref) <= TOL, k
