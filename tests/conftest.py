@@ -14,13 +14,18 @@ REF_TESTDATA = "/root/reference/test_data"
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    _ensure_built()  # before collection: some parameter lists load fibers through the library
 
 
 def _ensure_built():
     from brownian_dynamics_cuda_gb300 import build
-    if not os.path.exists(build.LIB):
+    srcs = [os.path.join(build.CSRC, f) for f in os.listdir(build.CSRC)]
+    srcs.append(os.path.join(ROOT, "include", "bd_capi.h"))
+    if not os.path.exists(build.LIB) or os.path.getmtime(build.LIB) < max(os.path.getmtime(f) for f in srcs):
         build.build_lib()
-    if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
+    orc = os.path.join(ROOT, "oracle", "liboracle.so")
+    osrc = [os.path.join(ROOT, "oracle", f) for f in ("bd_oracle.cpp", "bd_oracle.h", "Makefile")]
+    if not os.path.exists(orc) or os.path.getmtime(orc) < max(os.path.getmtime(f) for f in osrc):
         build.build_oracle()
 
 
