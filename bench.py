@@ -415,7 +415,8 @@ def run_batch(args):
 
 
 def run_adjoint(args):
-    """Config 3: gradient of the 200-step rollout observable (mean over the
+    """--config 3, the 24-nucleosome fiber with 30-bp linkers and no linker
+    histone: gradient of the 200-step rollout observable (mean over the
     final 50 states of the squared end-to-end distance plus the radius of
     gyration) with respect to the stretch, bend and twist moduli and the
     Debye length, by bd_adjoint (reverse mode, checkpoints every 20 steps,
@@ -500,7 +501,7 @@ def main():
     ap.add_argument("--frequency-rp", type=int, default=None,
                     help="rebuild and refactor D every k steps (default 1; 10 for config 4)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg of the mixed run")
-    ap.add_argument("--fd", action="store_true", help="config 3: also the FP64 central-difference gradient")
+    ap.add_argument("--fd", action="store_true", help="with --config 3 (rollout gradient): also the FP64 central-difference gradient")
     args = ap.parse_args()
     big = args.config == 4
     args.frequency_rp = args.frequency_rp or (10 if big else 1)
