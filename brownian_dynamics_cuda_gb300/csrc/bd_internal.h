@@ -23,6 +23,7 @@ struct HostSystem {
   std::vector<double> r, a, b, c, rad, phi_o, r_var, core_pos, core_q, tail_pos, r_t, h_t, g_t, lo_t, beta_o_t, t_q,
       t_rad, LH_g_pos, LH_q, LH_vdw_hh, LH_vdw_hc, LH_vdw_hl, LH_vdw_ht, LH_kstr, LH_kben, LH_streq, LH_betaeq,
       r_lh, lh_rad;
+  std::vector<double> lh_tpos, lh_trad;  // LH template as build_LH places it: [3 nlh] core-frame positions, [nlh] radii
 };
 
 int load_system(const char* dir, const char* data_f, const char* core_f, const char* tail_f, const char* lh_f,

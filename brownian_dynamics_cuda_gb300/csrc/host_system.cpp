@@ -290,6 +290,13 @@ int load_system(const char* dir_c, const char* data_f, const char* core_f, const
     }
     // build_LH (func.cpp:2029-2059)
     const int nlh = nn + nc;
+    S.lh_tpos.clear();
+    S.lh_trad.clear();
+    for (int j = 0; j < nlh; j++) {
+      const double* p = j < nn ? &npos[3 * j] : &cpos[3 * j];
+      S.lh_tpos.insert(S.lh_tpos.end(), {p[0], p[1], p[2]});
+      S.lh_trad.push_back(radius[j]);
+    }
     int nLH = 0;
     for (int f : S.nc_lh_flag) if (f == 1) nLH += nlh;
     m.n_LH = nLH;
@@ -617,6 +624,89 @@ extern "C" int bd_restart_read(const char* path, bd_restart* rs, bd_noise* g) {
   if (rc) return rc;
   if (!ok) return set_error(BD_ERR_IO, "bd_restart_read: truncated file");
   rs->step = (long)h.step;
+  return BD_OK;
+}
+
+// ---------------------------------------------------------------- LH binding
+extern "C" int bd_system_lh_template(const bd_system* sys, double* pos, double* rad) {
+  if (!sys || !pos || !rad) return set_error(BD_ERR_ARG, "bd_system_lh_template: null argument");
+  const HostSystem* S = reinterpret_cast<const HostSystem*>(sys);
+  std::memcpy(pos, S->lh_tpos.data(), S->lh_tpos.size() * sizeof(double));
+  std::memcpy(rad, S->lh_trad.data(), S->lh_trad.size() * sizeof(double));
+  return BD_OK;
+}
+
+// main.cpp:386-412
+extern "C" int bd_lh_mc(int n_c, double u_random, double u_core, double unbind, double Pbind, int* nc_lh_flag,
+                        int* changed) {
+  if (n_c <= 0 || !nc_lh_flag) return set_error(BD_ERR_ARG, "bd_lh_mc: bad argument");
+  int n_b = (int)(n_c * u_core);
+  if (n_b >= n_c) n_b = n_c - 1;
+  const int before = nc_lh_flag[n_b];
+  if (nc_lh_flag[n_b] > 0.5) {
+    if (u_random <= unbind) nc_lh_flag[n_b] = 0;
+  } else {
+    if (u_random <= Pbind) nc_lh_flag[n_b] = 1;
+  }
+  if (changed) *changed = nc_lh_flag[n_b] != before;
+  return BD_OK;
+}
+
+// main.cpp:414-447 with build_LH (func.cpp:2029-2059): every bound core's
+// beads placed from the template in its frame, then the beads of the cores
+// bound before overwritten with their previous positions
+extern "C" int bd_lh_rebind(int n, const int* type, int n_c, const double* r, const double* a, const double* b,
+                            const double* c, int nlh, const double* tpos, const double* trad, const int* old_flags,
+                            const double* old_r_lh, const int* new_flags, double* new_r_lh, double* new_lh_rad) {
+  if (n <= 0 || n_c <= 0 || nlh <= 0 || !type || !r || !a || !b || !c || !tpos || !trad || !old_flags || !new_flags ||
+      !new_r_lh || !new_lh_rad)
+    return set_error(BD_ERR_ARG, "bd_lh_rebind: null argument");
+  int k = 0, k1 = 0;
+  for (int i = 0; i < n; i++) {
+    if (type[i] != 1) continue;
+    if (k1 >= n_c) return set_error(BD_ERR_ARG, "bd_lh_rebind: more cores in type[] than n_c");
+    if (new_flags[k1] == 1) {
+      for (int j = 0; j < nlh; j++) {
+        const double* p = tpos + 3 * j;
+        for (int x = 0; x < 3; x++)
+          new_r_lh[(k * nlh + j) * 3 + x] =
+              r[i * 3 + x] + a[i * 3 + x] * p[0] + b[i * 3 + x] * p[1] + c[i * 3 + x] * p[2];
+        new_lh_rad[k * nlh + j] = trad[j];
+      }
+      k++;
+    }
+    k1++;
+  }
+  k = 0;
+  k1 = 0;
+  for (int i = 0; i < n_c; i++) {
+    if (new_flags[i] == 1) {
+      if (old_flags[i] == 1) {
+        if (!old_r_lh) return set_error(BD_ERR_ARG, "bd_lh_rebind: previous LH positions required");
+        for (int j = 0; j < nlh; j++)
+          for (int x = 0; x < 3; x++) new_r_lh[(k * nlh + j) * 3 + x] = old_r_lh[(k1 * nlh + j) * 3 + x];
+        k1++;
+      }
+      k++;
+    } else if (old_flags[i] == 1) {
+      k1++;
+    }
+  }
+  return BD_OK;
+}
+
+extern "C" int bd_noise_uniforms(bd_noise* gp, int count, double* out) {
+  if (!gp || count < 0 || (count > 0 && !out)) return set_error(BD_ERR_ARG, "bd_noise_uniforms: bad argument");
+  Mt19937& g = *reinterpret_cast<Mt19937*>(gp);
+  for (int i = 0; i < count; i++) out[i] = g.real1();
+  return BD_OK;
+}
+
+extern "C" int bd_noise_draws(bd_noise* gp, int n3, const double* r_var, int n_D3, double* rr, double* p) {
+  if (!gp || (n3 > 0 && (!r_var || !rr)) || (n_D3 > 0 && !p)) return set_error(BD_ERR_ARG, "bd_noise_draws: null argument");
+  Mt19937& g = *reinterpret_cast<Mt19937*>(gp);
+  for (int i = 0; i < n3; i++) rr[i] = g.normal(0, r_var[i]);
+  for (int i = 0; i < n_D3; i++) p[i] = g.normal(0, 1);
   return BD_OK;
 }
 

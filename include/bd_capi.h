@@ -135,6 +135,13 @@ int bd_noise_create(unsigned long seed, bd_noise** out);
 int bd_noise_step(bd_noise* g, int step, int n3, const double* r_var, int n_D3, double* rr, double* p);
 int bd_noise_u32(bd_noise* g, int count, uint32_t* out);
 void bd_noise_free(bd_noise* g);
+/* The step's pieces separately, for a driver that runs the LH binding Monte
+ * Carlo between them (bd_lh_mc): `count` uniforms genrand_real1 as main.cpp
+ * draws them on steps with step % 100 == 0 (main.cpp:387-388), then the
+ * step's normal draws.  bd_noise_step(g, step, ...) is exactly
+ * bd_noise_uniforms(g, 2, u) when step % 100 == 0, then bd_noise_draws. */
+int bd_noise_uniforms(bd_noise* g, int count, double* out);
+int bd_noise_draws(bd_noise* g, int n3, const double* r_var, int n_D3, double* rr, double* p);
 /* The generator's full state: the 624 MT19937 words, the index of the next
  * word, and the pending second deviate of the polar method. */
 int bd_noise_get_state(const bd_noise* g, uint32_t* words624, int* index, int* have_cached, double* cached);
@@ -297,6 +304,21 @@ int bd_kernel_bytes(bd_ctx* ctx, double* bytes);
 int bd_launch_count(bd_ctx* ctx, int* out);
 /* Pivots replaced by |pivot| in the last factorisation (func.cpp:827-833). */
 int bd_negative_pivots(bd_ctx* ctx, int* out);
+
+/* ------------------------------------------------------- LH binding (host)
+ * main.cpp:386-465 in three calls: bd_lh_mc decides (core n_b =
+ * (int)(n_c u_core), at most n_c - 1, releases its linker histone when
+ * u_random <= unbind or binds one when u_random <= Pbind; *changed = 1 if
+ * the flag changed); bd_lh_rebind places the beads for the new flags (cores
+ * bound before keep old_r_lh's beads, newly bound ones get the template
+ * tpos [3 nlh] in their frame: build_LH, func.cpp:2029-2059, and
+ * main.cpp:414-447), with the template from bd_system_lh_template; then
+ * bd_set_lh_flags resizes the context. */
+int bd_lh_mc(int n_c, double u_random, double u_core, double unbind, double Pbind, int* nc_lh_flag, int* changed);
+int bd_lh_rebind(int n, const int* type, int n_c, const double* r, const double* a, const double* b, const double* c,
+                 int nlh, const double* tpos, const double* trad, const int* old_flags, const double* old_r_lh,
+                 const int* new_flags, double* new_r_lh, double* new_lh_rad);
+int bd_system_lh_template(const bd_system* sys, double* pos, double* rad);
 
 /* A context's current state (device) into rs's arrays, which must be
  * allocated for the context's sizes (bd_sizes); rs's sizes are set from the
