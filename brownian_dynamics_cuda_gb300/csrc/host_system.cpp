@@ -55,6 +55,24 @@ std::string join(const std::string& dir, const std::string& f) {
   return dir + "/" + f;
 }
 
+// Read_restart_ini / _tail / _LH (readfile.cpp:443-630): the first value of
+// each line, `count` of them
+int read_restart_column(const std::string& dir, const char* name, size_t count, std::vector<double>& out,
+                        std::string& err) {
+  std::ifstream in(join(dir, name));
+  if (!in) { err = std::string("restart = 1 in setup.txt but ") + name + " cannot be opened"; return BD_ERR_IO; }
+  out.resize(count);
+  size_t i = 0;
+  std::string line;
+  while (i < count && std::getline(in, line)) {
+    auto t = tokens(line);
+    if (t.empty()) continue;
+    out[i++] = num(t[0]);
+  }
+  if (i < count) { err = std::string(name) + ": fewer values than the system has"; return BD_ERR_IO; }
+  return BD_OK;
+}
+
 // func.cpp:13-99: intrinsic twist per linker segment for w linker beads
 double twist_angle(int w, bool* ok) {
   static const double table[12] = {0, 0, 0.9007, -0.6754, -0.3519, -0.1463, 0.0215, 0.1178, 0.2025, 0.2726, -0.2415, -0.15};
@@ -144,6 +162,18 @@ int load_system(const char* dir_c, const char* data_f, const char* core_f, const
   const int n = (int)S.type.size();
   int n_c = 0;
   for (int t : S.type) n_c += (t == 1);
+  // restart = 1 in setup.txt: positions and frames from the text restart
+  // files, before the tails and linker histones are built on them
+  // (main.cpp:143-153)
+  const bool restart = S.setup.size() > 12 && (int)S.setup[12] == 1;
+  if (restart) {
+    int rc = 0;
+    if ((rc = read_restart_column(dir, "restart_r.txt", 3 * (size_t)n, S.r, err)) ||
+        (rc = read_restart_column(dir, "restart_a.txt", 3 * (size_t)n, S.a, err)) ||
+        (rc = read_restart_column(dir, "restart_b.txt", 3 * (size_t)n, S.b, err)) ||
+        (rc = read_restart_column(dir, "restart_c.txt", 3 * (size_t)n, S.c, err)))
+      return rc;
+  }
   m.n = n; m.n_c = n_c;
   if (S.type[0] != 1 || S.type[n - 1] != 0) {
     err = "chain must start with a core and end with linker DNA (func.cpp:1062,1283)";
@@ -237,6 +267,10 @@ int load_system(const char* dir_c, const char* data_f, const char* core_f, const
       err = "tail template must have 10 groups (the core lookup (t_grp-1)/10 of func.cpp:2368 assumes it)";
       return BD_ERR_IO;
     }
+    if (restart && n_tail > 0) {  // main.cpp:218-220
+      int rc = read_restart_column(dir, "restart_tail.txt", 3 * (size_t)n_tail, S.r_t, err);
+      if (rc) return rc;
+    }
   }
   // LH table (readfile.cpp:252-337)
   {
@@ -316,6 +350,10 @@ int load_system(const char* dir_c, const char* data_f, const char* core_f, const
         k++;
       }
       k1++;
+    }
+    if (restart && nLH > 0) {  // main.cpp:279-281
+      int rc = read_restart_column(dir, "restart_lh.txt", 3 * (size_t)nLH, S.r_lh, err);
+      if (rc) return rc;
     }
   }
   refresh_model_pointers(S);
@@ -707,6 +745,32 @@ extern "C" int bd_noise_draws(bd_noise* gp, int n3, const double* r_var, int n_D
   Mt19937& g = *reinterpret_cast<Mt19937*>(gp);
   for (int i = 0; i < n3; i++) rr[i] = g.normal(0, r_var[i]);
   for (int i = 0; i < n_D3; i++) p[i] = g.normal(0, 1);
+  return BD_OK;
+}
+
+
+
+// write_restart (readfile.cpp:404-439): one value per line, fixed notation
+// with 15 decimals, one file per array, in dir
+extern "C" int bd_write_restart_text(const char* dir, int n, int n_tail, int n_LH, const double* r, const double* a,
+                                     const double* b, const double* c, const double* Er, const double* r_t,
+                                     const double* r_lh) {
+  if (!dir || n <= 0 || !r || !a || !b || !c || (n_tail > 0 && !r_t) || (n_LH > 0 && !r_lh))
+    return set_error(BD_ERR_ARG, "bd_write_restart_text: bad argument");
+  const std::vector<double> zero(3 * (size_t)n, 0.0);
+  struct F { const char* name; const double* v; size_t cnt; } files[] = {
+      {"restart_r.txt", r, 3 * (size_t)n},        {"restart_a.txt", a, 3 * (size_t)n},
+      {"restart_b.txt", b, 3 * (size_t)n},        {"restart_c.txt", c, 3 * (size_t)n},
+      {"restart_Er.txt", Er ? Er : zero.data(), 3 * (size_t)n},
+      {"restart_tail.txt", r_t, 3 * (size_t)n_tail}, {"restart_lh.txt", r_lh, 3 * (size_t)n_LH}};
+  for (auto& f : files) {
+    FILE* fp = std::fopen(join(dir, f.name).c_str(), "w");
+    if (!fp) return set_error(BD_ERR_IO, "bd_write_restart_text: cannot open a file");
+    bool ok = true;
+    for (size_t i = 0; i < f.cnt && ok; i++) ok = std::fprintf(fp, "%.15f\n", f.v[i]) > 0;
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) return set_error(BD_ERR_IO, "bd_write_restart_text: write failed");
+  }
   return BD_OK;
 }
 

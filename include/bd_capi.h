@@ -121,6 +121,13 @@ int bd_system_state(const bd_system* sys, bd_state* out);
 /* setup.txt values: T steps freq freq_RP sigma x6 Mg Cs restart unbind Pbind (15) */
 int bd_system_setup(const bd_system* sys, double* out15);
 void bd_system_free(bd_system* sys);
+/* The reference's text restart (write_restart, readfile.cpp:404-439):
+ * restart_{r,a,b,c,Er,tail,lh}.txt in dir, one value per line with 15
+ * decimals (Er NULL: zeros).  bd_system_load reads them back in place of
+ * the start structure when setup.txt has restart = 1 (main.cpp:143-153,
+ * :218-220, :279-281). */
+int bd_write_restart_text(const char* dir, int n, int n_tail, int n_LH, const double* r, const double* a,
+                          const double* b, const double* c, const double* Er, const double* r_t, const double* r_lh);
 /* Appends one out.xyz frame (readfile.cpp:346-405 format). */
 int bd_write_xyz(const bd_model* m, const double* r, const double* a, const double* b, const double* c,
                  const double* r_t, const double* r_lh, const char* path);

@@ -58,3 +58,36 @@ def test_restart_rejects_bad_files(tmp_path):
         f.write(data[:len(data) // 2])
     with pytest.raises(BDError):
         restart_read(path)
+
+
+def test_text_restart_is_read_back_by_the_loader(tmp_path):
+    """bd_write_restart_text writes the reference's restart_*.txt files
+    (write_restart: 15 decimals, one value per line); with restart = 1 in
+    setup.txt the loader takes r, a, b, c, r_t and r_lh from them
+    (main.cpp:143-153, :218-220, :279-281)."""
+    import ctypes as C
+    import re
+    from brownian_dynamics_cuda_gb300 import Fiber, load_library
+    from brownian_dynamics_cuda_gb300.capi import _check
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, write_fiber
+    d = str(tmp_path)
+    files = write_fiber(FiberSpec(3, [30] * 3, lh=True, seed=8), d)
+    f0 = Fiber.load(d, **files)
+    rng = np.random.default_rng(1)
+    new = {k: f0.state[k] + rng.normal(scale=0.3, size=f0.state[k].size) for k in ("r", "a", "b", "c", "r_t", "r_lh")}
+    L = load_library()
+    dp = C.POINTER(C.c_double)
+    L.bd_write_restart_text.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int] + [dp] * 7
+    sz = f0.sizes
+    p = lambda a: a.ctypes.data_as(dp)
+    _check(L.bd_write_restart_text(d.encode(), sz["n"], sz["n_tail"], sz["n_LH"], p(new["r"]), p(new["a"]),
+                                   p(new["b"]), p(new["c"]), None, p(new["r_t"]), p(new["r_lh"])))
+    lines = open(f"{d}/restart_r.txt").read().splitlines()
+    assert len(lines) == 3 * sz["n"] and all(re.fullmatch(r"-?\d+\.\d{15}", x) for x in lines)
+    setup = open(f"{d}/setup.txt").read()
+    setup = re.sub(r"^(restart\s+)0$", r"\g<1>1", setup, flags=re.M)
+    open(f"{d}/setup.txt", "w").write(setup)
+    f1 = Fiber.load(d, **files)
+    for k in new:
+        assert np.allclose(f1.state[k], new[k], rtol=0, atol=6e-16 * max(1.0, np.abs(new[k]).max()) * 10), k
+    assert f1.sizes == f0.sizes
