@@ -186,6 +186,8 @@ int ref_init(const char* dir, const char* core_file, const char* tail_file, cons
   std::vector<double> tr, ta, tb, tc, trad, tEr; std::vector<int> ttype;
   Read_initial_struc(s.n, s.n_c, s.n3, s.nc3, tr, ta, tb, tc, trad, tEr, ttype, "data_mod");
   s.r = tr; s.a = ta; s.b = tb; s.c = tc; s.Er = tEr; s.rad = trad; s.type = ttype;
+  const bool restart = (int)ic[12] == 1;  // main.cpp:143-153
+  if (restart) Read_restart_ini(s.n3, s.r.data(), s.a.data(), s.b.data(), s.c.data(), s.Er.data());
   s.alpha.assign(s.n, 0); s.beta.assign(s.n, 0); s.gamma.assign(s.n, 0); s.phi_o.assign(s.n, 0); s.length.assign(s.n, 0);
   s.a_dna.assign(std::max(s.nc3, 1), 0); s.b_dna = s.a_dna; s.c_dna = s.a_dna;
   s.alpha_p.assign(std::max(s.n_c, 1), 0); s.beta_p = s.alpha_p; s.gamma_p = s.alpha_p;
@@ -206,6 +208,7 @@ int ref_init(const char* dir, const char* core_file, const char* tail_file, cons
       s.tail_bond_v, s.tail_angle_c, s.tail_angle_v, s.r.data(), s.a.data(), s.b.data(), s.c.data(), s.n_tail,
       s.nc_t_flag.data(), s.r_t.data(), s.h_t.data(), s.g_t.data(), s.lo_t.data(), s.beta_o_t.data(), s.t_q.data(),
       s.t_rad.data(), s.t_grp.data(), s.t_fix.data());
+  if (restart && s.n_tail3 > 0) Read_restart_tail(s.n_tail3, s.r_t.data());  // main.cpp:218-220
   update_tail_beta(s.n_tail, s.r_t.data(), s.beta_t.data(), s.t_grp.data());
   Read_LH(s.n_lh_g, s.n_lh_n, s.n_lh_c, s.LH_g_pos, s.LH_n_pos, s.LH_c_pos, s.LH_conn, s.LH_q, s.LH_vdw_hh,
       s.LH_vdw_hc, s.LH_vdw_hl, s.LH_vdw_ht, s.LH_kstr, s.LH_kben, s.LH_streq, s.LH_betaeq, s.LH_radius, lh_file);
@@ -222,6 +225,7 @@ int ref_init(const char* dir, const char* core_file, const char* tail_file, cons
   s.r_lh.assign(rlh_tmp.begin(), rlh_tmp.begin() + std::max(s.n_LH3, 3));
   s.lh_rad.assign(lrad_tmp.begin(), lrad_tmp.begin() + std::max(s.n_LH, 1));
   s.beta_lh.assign(std::max(s.n_LH, 1), 0.0);
+  if (restart && s.n_LH3 > 0) Read_restart_LH(s.n_LH3, s.r_lh.data());  // main.cpp:279-281
   if (s.n_LH > 0) update_LH_beta(s.n_LH, s.n_lh_c, s.r_lh.data(), s.beta_lh.data());
   s.r_var.assign(s.n3, 0.0);
   for (int i = 0; i < s.n; i++) {

@@ -80,3 +80,33 @@ def test_oracle_parallel_cholesky_bitwise(testdata):
     D, L = Oracle(fib).tensor()
     L4, neg = cholesky(D, nthreads=4)
     assert neg == 0 and np.array_equal(np.tril(L4), L)
+
+
+def test_text_restart_matches_reference_readers(tmp_path):
+    """restart = 1 in setup.txt: the loader takes the start structure, tails
+    and LH beads from restart_*.txt exactly as the reference's own readers
+    (Read_restart_ini / _tail / _LH, readfile.cpp) do in main.cpp."""
+    import re
+    from brownian_dynamics_cuda_gb300 import Fiber
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, write_fiber
+    from oracle.pyoracle import Oracle, Reference
+    d = str(tmp_path)
+    files = write_fiber(FiberSpec(3, [30] * 3, lh=True, seed=8), d)
+    f0 = Fiber.load(d, **files)
+    rng = np.random.default_rng(2)
+    for k, fn in (("r", "restart_r.txt"), ("a", "restart_a.txt"), ("b", "restart_b.txt"), ("c", "restart_c.txt"),
+                  ("r_t", "restart_tail.txt"), ("r_lh", "restart_lh.txt")):
+        v = f0.state[k] + rng.normal(scale=0.1, size=f0.state[k].size)
+        with open(os.path.join(d, fn), "w") as f:
+            f.write("".join(f"{x:.15f}\n" for x in v))
+    with open(os.path.join(d, "restart_Er.txt"), "w") as f:
+        f.write("0.000000000000000\n" * f0.state["r"].size)
+    setup = open(os.path.join(d, "setup.txt")).read()
+    open(os.path.join(d, "setup.txt"), "w").write(re.sub(r"^(restart\s+)0$", r"\g<1>1", setup, flags=re.M))
+    fib = Fiber.load(d, **files)
+    ref = Reference(d, files["core_file"], files["tail_file"], files["lh_file"], seed=1)
+    for k in ("r", "r_t", "r_lh"):
+        assert np.array_equal(fib.state[k], ref.get(k)), k
+    o = Oracle(fib)  # frames refreshed as main.cpp:164 does after the restart read
+    for k in ("a", "b", "c", "beta_t", "beta_lh"):
+        assert np.array_equal(o.get(k), ref.get(k)), k
