@@ -314,7 +314,7 @@ def run_ours(args):
                 "frac": achieved / pk["hbm_gbs"] if achieved else None,
                 "traffic": byt * NCU_TRAFFIC_PER_ALG_BYTE,
                 "traffic_source": "DRAM read+write per algorithmic byte of one ncu capture "
-                                  "(profiles/k_chol_step_cfg1_mixed.md), times this step's algorithmic bytes",
+                                  "of k_chol_step at 3N = 11,700, times this step's algorithmic bytes",
                 "kernel": "k_chol_step (every launch of the mixed factorisation: next panel in its own CTAs beside "
                           "tcgen05 column and bulk trailing updates of one or two panels, double-float tile "
                           "read-modify-write), %d launches/step, avg %.3f ms" % (nk, ms_k / max(nk, 1)),

@@ -8,7 +8,7 @@
  * pointers and sizes, host arrays in the reference's own layouts (xyz
  * interleaved per bead, row-major matrices), an int status from every call,
  * no globals and no C++ types.  A shim in the same library re-exports the
- * four reference symbols on top of it (see INTEGRATION.md), so the
+ * four reference symbols on top of it, so the
  * reference's main.cpp links against this library unchanged.
  *
  * Threading: a context is used by one host thread at a time; different
