@@ -20,9 +20,14 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "bd_internal.h"
 
 namespace bdh {
+Range::Range(const char* name) { nvtxRangePushA(name); }
+Range::~Range() { nvtxRangePop(); }
+
 static thread_local std::string g_err;
 int set_error(int code, const char* msg) {
   g_err = msg ? msg : "";
@@ -124,6 +129,9 @@ static int pack_ns(bd_ctx* c, const DevState& Y, double* dst) {
 enum { kPre = 1, kChol = 2, kPost = 4 };
 
 static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double* const* saves, int phases) {
+  bdh::Range range(phases == (kPre | kChol | kPost) ? "bd_step" : phases == kPre ? "bd_step: positions, tensor"
+                                                                  : phases == kPost ? "bd_step: forces, moves"
+                                                                                    : "bd_step: factorisation");
   DevModel& M = c->M;
   cudaStream_t st = c->stream;
   int L = 0, rc = 0;
@@ -894,7 +902,10 @@ static int batch_enqueue(bd_batch* b) {
     return rc;
   }
   if ((rc = batch_lanes(b, kPre))) return rc;
-  bdk::mixed_batch_run(b->chol, b->stream);  // alone on the GPU: the only tensor-core kernel of the step
+  {
+    bdh::Range range("bd_batch: factorisations");
+    bdk::mixed_batch_run(b->chol, b->stream);  // alone on the GPU: the only tensor-core kernel of the step
+  }
   CK(cudaGetLastError());
   return batch_lanes(b, kPost);
 }

@@ -218,6 +218,13 @@ struct bd_ctx {
 };
 
 namespace bdh {
+// An NVTX range around host-side phases, for profilers (nsys, ncu's NVTX
+// filters); without a tool attached the calls do nothing.
+struct Range {
+  explicit Range(const char* name);
+  ~Range();
+};
+
 // The device part of one step (bd_capi.cu).  With saves != nullptr the
 // predictor state before and after its frame refresh and the corrector state
 // before its refresh are copied to saves[0..2] ([r a b c r_t], 12n + 3 n_tail).

@@ -1062,12 +1062,16 @@ int run(bd_ctx* c, int N, int K, int Wn, const double* rr, const double* p, doub
   CK(cudaMemsetAsync(w.loss, 0, 8 * sizeof(double), st));
   const double scale = 1.0 / Wn;
   w.launches = 0;
-  for (int s = 0; s < N; s++) {
-    if (grad && s % K == 0 && (rc = pack_full(c, w.ckpt + (size_t)(s / K) * w.nfull, true))) return rc;
-    if ((rc = bdh::step_device(c, w.rr + (size_t)s * n3, w.p + (size_t)s * m))) return rc;
-    if (s + 1 >= N - Wn + 1) k_loss<<<1, 256, 0, st>>>(M.n, c->X.r, scale, w.loss, nullptr);
+  {
+    bdh::Range fwd_range("bd_adjoint: forward sweep");
+    for (int s = 0; s < N; s++) {
+      if (grad && s % K == 0 && (rc = pack_full(c, w.ckpt + (size_t)(s / K) * w.nfull, true))) return rc;
+      if ((rc = bdh::step_device(c, w.rr + (size_t)s * n3, w.p + (size_t)s * m))) return rc;
+      if (s + 1 >= N - Wn + 1) k_loss<<<1, 256, 0, st>>>(M.n, c->X.r, scale, w.loss, nullptr);
+    }
   }
   if (grad) {
+    bdh::Range rev_range("bd_adjoint: reverse sweep");
     CK(cudaMemsetAsync(w.lam, 0, w.ns * sizeof(double), st));
     CK(cudaMemsetAsync(w.th, 0, 8 * sizeof(double), st));
     k_loss<<<1, 256, 0, st>>>(M.n, c->X.r, scale, w.scratch, w.lam);
