@@ -20,13 +20,21 @@
 #include <string>
 #include <vector>
 
+#if __has_include(<nvtx3/nvToolsExt.h>)
 #include <nvtx3/nvToolsExt.h>
+#define BD_HAVE_NVTX 1
+#endif
 
 #include "bd_internal.h"
 
 namespace bdh {
+#ifdef BD_HAVE_NVTX
 Range::Range(const char* name) { nvtxRangePushA(name); }
 Range::~Range() { nvtxRangePop(); }
+#else
+Range::Range(const char*) {}
+Range::~Range() {}
+#endif
 
 static thread_local std::string g_err;
 int set_error(int code, const char* msg) {
