@@ -108,3 +108,28 @@ def test_adjoint_reference_fixture_is_the_oracle():
     g3 = (mk.observable(mk.with_theta(fib, tp), z["rr"], z["p"]) -
           mk.observable(mk.with_theta(fib, tm), z["rr"], z["p"])) / (2 * d)
     assert abs(g3 - z["grad"][3]) <= 1e-5 * abs(z["grad"][3])
+
+
+def test_cholesky_backward_identity():
+    """The Cholesky backward the adjoint kernels implement: for
+    f(D) = u_bar . (s L(D) p), D = L L^T, the gradient contracted with any
+    symmetric dD is <V (Phi V^T), dD>, V = L^-T, Phi = s tril(u p^T) with the
+    diagonal halved, u = L^T u_bar (numpy, against central differences)."""
+    rng = np.random.default_rng(4)
+    m, s = 24, 0.7
+    Q = rng.normal(size=(m, m))
+    D = Q @ Q.T + m * np.eye(m)
+    p, ub = rng.normal(size=m), rng.normal(size=m)
+    f = lambda Dm: ub @ (s * np.linalg.cholesky(Dm) @ p)
+    L = np.linalg.cholesky(D)
+    u = L.T @ ub
+    Phi = s * np.tril(np.outer(u, p))
+    Phi[np.diag_indices(m)] *= 0.5
+    V = np.linalg.inv(L.T)
+    Dbar = V @ (Phi @ V.T)
+    for _ in range(5):
+        E = rng.normal(size=(m, m))
+        E = E + E.T
+        h = 1e-6
+        fd = (f(D + h * E) - f(D - h * E)) / (2 * h)
+        assert abs(np.sum(Dbar * E) - fd) <= 1e-7 * max(1.0, abs(fd))
