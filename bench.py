@@ -37,6 +37,8 @@ METRIC = "BD steps/s vs plain FP64 on 1 GB300 at <=1e-6 rel. error; replica-step
 # the K = 384 bulk update by panels 0-2, 3N = 11,700: 1,015.5 MB of DRAM
 # traffic for 1,024.6 MB algorithmic)
 NCU_TRAFFIC_PER_ALG_BYTE = 1015.5 / 1024.6
+# largest 3N for which the GPU line's CPU baseline times complete oracle steps
+CPU_STEP_MAX_M = 20000
 
 
 def peaks():
@@ -162,6 +164,50 @@ def fp64_comparison(fib, rr_d, p_d, host, args, local, stream) -> dict:
             "rel_displacement_err": num / den, "tolerance": 1e-6}
 
 
+def library_bar(fib, local, dpotrf: bool) -> dict:
+    """The library bar for the factorisation phase: cuSOLVER's potrf through
+    torch.linalg.cholesky (cusolverDnXpotrf) on this fiber's own FP64 RPY
+    tensor (3N <= 20,000; above that a synthetic SPD matrix of the same size,
+    since the timing does not depend on the values), in FP32 (the accuracy
+    class of the mixed factor) and FP64 (what func_cuda.cu:3526-3529 calls).
+    Measurement only: the product never calls it."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, Context
+    torch.backends.cuda.preferred_linalg_library("cusolver")
+    m = fib.m
+    if m <= 20000:
+        c = Context(fib, precision=PREC_FP64, device=local)
+        D = torch.tensor(c.diffusion_tensor(), device="cuda")
+        c.close()
+        src = "the fiber's FP64 RPY tensor"
+    else:
+        g = torch.Generator(device="cuda").manual_seed(0)
+        X = torch.randn(m, 64, device="cuda", dtype=torch.float64, generator=g)
+        D = X @ X.T / 64 + 2.0 * torch.eye(m, device="cuda", dtype=torch.float64)
+        del X
+        src = "synthetic SPD matrix of the same size"
+    out = {"input": src, "3N": m}
+    legs = [("cusolver_spotrf_ms", torch.float32, 5)] + ([("cusolver_dpotrf_ms", torch.float64, 2)] if dpotrf else [])
+    for key, dt, reps in legs:
+        A = D.to(dt)
+        torch.linalg.cholesky(A)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            Lc = torch.linalg.cholesky(A)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+            del Lc
+        out[key] = best
+        del A
+    del D
+    torch.cuda.empty_cache()
+    return out
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -173,48 +219,61 @@ def make_fiber(cfg: int, seed: int):
     return mk(spec, d), spec
 
 
-def cpu_sample(fib, threads: int, n0_beads: int = 400) -> dict:
-    """Bounded CPU sample of one step with the oracle port: one full force
-    pass (x2 for the corrector), the RPY assembly and the reference Cholesky
-    of the leading n0 beads, extrapolated by (m/m0)^2 and (m/m0)^3."""
-    from oracle.pyoracle import Oracle, cholesky, rpy
+def oracle_fiber(cfg: int, seed: int):
+    """The workload's input files read by the oracle's restatement of the
+    reference readers (oracle/ref_loader.py): the CPU legs load no product
+    library."""
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, write_fiber
+    from oracle import ref_loader
+    d = tempfile.mkdtemp(prefix="bdfiber_ref_")
+    spec = config(cfg, seed=seed)
+    return ref_loader.load(d, **write_fiber(spec, d)), spec
+
+
+def cpu_steps(fib, threads: int, warmup: int, steps: int, seed: int = 1000) -> dict:
+    """Complete BD steps of the CPU oracle (oracle/bd_oracle.cpp, the
+    reference's func.cpp step restated): RPY assembly, the reference's full
+    Cholesky, rd = s2dt L p, both force passes and both moves, with the
+    reference's MT19937 noise.  The assembly, the Cholesky (bit for bit the
+    reference's row loop, column-blocked over `threads`) and rd run on
+    `threads` host threads; the force passes on one, as in the reference."""
+    from oracle.pyoracle import Oracle, OracleNoise, set_threads
+    set_threads(threads)
     o = Oracle(fib)
-    t = time.perf_counter()
-    o.forces()
-    t_f = time.perf_counter() - t
-    r_all = np.concatenate([fib.state["r"], fib.state["r_t"], fib.state["r_lh"]])
-    rad = np.concatenate([fib.arrays["rad"], fib.arrays["t_rad"], fib.arrays["lh_rad"]])
-    n0 = min(n0_beads, fib.n_D)
-    t = time.perf_counter()
-    D = rpy(r_all[:3 * n0], rad[:n0], fib.scalars["a1"], fib.scalars["a2"])
-    t_r = time.perf_counter() - t
-    t = time.perf_counter()
-    cholesky(D, nthreads=threads)
-    t_c = time.perf_counter() - t
-    m, m0 = fib.m, 3 * n0
-    step_s = 2 * t_f + t_r * (m / m0) ** 2 + t_c * (m / m0) ** 3
-    return {"step_s": step_s, "t_forces": t_f, "t_rpy0": t_r, "t_chol0": t_c, "m0": m0,
-            "sample": f"one force pass of the full fiber (x2), RPY assembly + reference Cholesky of the leading "
-                      f"{m0}x{m0} block extrapolated by (m/m0)^2 and (m/m0)^3 to m={m}"}
+    gen = OracleNoise(seed)
+    times = []
+    for i in range(warmup + steps):
+        rr, p = gen.step(i, fib.arrays["r_var"], fib.m)
+        t = time.perf_counter()
+        o.step(rr, p)
+        if i >= warmup:
+            times.append(time.perf_counter() - t)
+    total = float(np.sum(times))
+    return {"steps_timed": steps, "total_s": total, "step_s": total / max(steps, 1),
+            "sample": f"{steps} complete oracle steps of the full fiber (3N = {fib.m}) after {warmup} untimed: "
+                      f"RPY assembly, the reference Cholesky (func.cpp:806-836; same factor bit for bit, "
+                      f"column-blocked on {threads} threads), rd, two force passes (1 thread) and two moves; "
+                      f"nothing extrapolated"}
 
 
 def run_reference(args):
+    """The reference's CPU path on this host's cores: complete steps of the
+    oracle port (oracle/_ref is not built on the GPU host), the fiber read by
+    the oracle's own restatement of the reference readers."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    fib, spec = make_fiber(args.config, 1)
+    fib, spec = oracle_fiber(args.config, 1)
     threads = os.cpu_count() or 1
-    samples = []
-    for i in range(args.warmup + args.steps):
-        s = cpu_sample(fib, threads)
-        if i >= args.warmup:
-            samples.append(s["step_s"])
-    step_s = float(np.mean(samples))
-    v = 1.0 / step_s
+    t0 = time.perf_counter()
+    s = cpu_steps(fib, threads, args.warmup, args.steps)
+    wall = time.perf_counter() - t0
+    v = 1.0 / s["step_s"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s["step_s"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fiber generator)",
-            "config": {"workload": spec.name, "n_D": fib.n_D, "3N": fib.m, "precision": "fp64"},
+            "config": {"workload": spec.name, "n_D": fib.n_D, "3N": fib.m, "precision": "fp64",
+                       "timed_s": s["total_s"], "wall_s": wall},
             "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port", "sample": s["sample"]},
             "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -333,10 +392,23 @@ def run_ours(args):
         if world > 1:
             vs64["fp64_steps_per_s"] = replica_rate(max_over_ranks(1000.0 / vs64["fp64_steps_per_s"]), world)
         vs64["speedup_vs_fp64"] = value / vs64["fp64_steps_per_s"]
+    lib = None
+    if rank == 0 and not args.no_library_bar:
+        lib = library_bar(fib, local, dpotrf=fib.m <= 20000)
+        lib["ours_chol_phase_ms"] = float(phases[1])
+        if "cusolver_spotrf_ms" in lib:
+            lib["spotrf_over_ours"] = lib["cusolver_spotrf_ms"] / float(phases[1])
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        s = cpu_sample(fib, 1)
-        cpu = {"value": 1.0 / s["step_s"], "unit": "steps/s", "cores": 1, "kind": "port", "sample": s["sample"]}
+        if fib.m <= CPU_STEP_MAX_M:
+            ofib, _ = oracle_fiber(args.config, 1)
+            threads = os.cpu_count() or 1
+            s = cpu_steps(ofib, threads, 0, 2)
+            cpu = {"value": 1.0 / s["step_s"], "unit": "steps/s", "cores": threads, "kind": "port",
+                   "sample": s["sample"]}
+        else:
+            cpu = {"value": None, "unit": "steps/s", "cores": None, "kind": "port",
+                   "sample": f"not run: one complete oracle step at 3N = {fib.m} takes minutes (O((3N)^3) Cholesky)"}
     if rank == 0:
         names = ["rpy", "chol", "rd", "forces1", "move1", "frames", "forces2", "move2+frames", "total"]
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -351,7 +423,7 @@ def run_ours(args):
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "clocks": clocks, "roofline": roof, "vs_fp64": vs64,
                 "phases_ms": dict(zip(names, [round(float(x), 4) for x in phases])),
-                "cpu_baseline": cpu}
+                "library_bar": lib, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -501,8 +573,12 @@ def main():
     ap.add_argument("--frequency-rp", type=int, default=None,
                     help="rebuild and refactor D every k steps (default 1; 10 for config 4)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg of the mixed run")
+    ap.add_argument("--no-library-bar", action="store_true", help="skip the cuSOLVER potrf timing leg")
     ap.add_argument("--fd", action="store_true", help="with --config 3 (rollout gradient): also the FP64 central-difference gradient")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(f"bench.py --gpus {args.gpus}: launch one process per GPU, e.g. python -m torch.distributed.run "
+                 f"--nnodes=1 --nproc-per-node {args.gpus} --master-addr 127.0.0.1 bench.py --gpus {args.gpus}")
     big = args.config == 4
     args.frequency_rp = args.frequency_rp or (10 if big else 1)
     args.steps = args.steps if args.steps is not None else (10 if big else 5)

@@ -82,7 +82,7 @@ def build_oracle(verbose: bool = False) -> None:
     """Builds oracle/liboracle.so and, when the reference tree is present, oracle/_ref/libbdref.so."""
     odir = os.path.join(ROOT, "oracle")
     targets = ["liboracle.so"]
-    if os.path.isdir("/root/reference/BD_cuda"):
+    if subprocess.run(["make", "-s", "-C", odir, "have-ref"], capture_output=True).returncode == 0:
         targets.append("ref")
     for t in targets:
         p = subprocess.run(["make", "-s", "-C", odir, t], capture_output=True, text=True)

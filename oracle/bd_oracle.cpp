@@ -6,6 +6,7 @@
 // floating-point sum.
 #include "bd_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -25,6 +26,10 @@ constexpr double kRh = 1.2;
 
 using Vec = std::vector<double>;
 using IVec = std::vector<int>;
+
+// Host threads for the O(m^2) and O(m^3) parts of a step (RPY assembly,
+// Cholesky, rd); none of them changes a floating-point sum.
+static int g_threads = 1;
 
 // ---------------------------------------------------------------- primitives
 // func.cpp:134-151
@@ -966,6 +971,8 @@ static void rpy(const System& S, const Vec& r, Vec& D) {
   const Vec& rad = S.rad_all;
   D.assign((size_t)m * m, 0.0);
   auto at = [&](int i, int j) -> double& { return D[(size_t)i * m + j]; };
+  // each pair (i, j >= i) writes only its own two 3x3 blocks
+#pragma omp parallel for schedule(dynamic, 8) num_threads(g_threads)
   for (int i = 0; i < N; i++) {
     for (int j = i; j < N; j++) {
       if (i == j) {
@@ -1007,8 +1014,85 @@ static void rpy(const System& S, const Vec& r, Vec& D) {
 
 using namespace orc;
 
-// func.cpp:806-836.  Column-parallel form: L[i][j] for all i > j depends
-// only on columns < j, and each inner product keeps the reference's k order.
+extern "C" void orc_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+
+// Multi-threaded form of func.cpp:806-836 with the same result bit for bit.
+// L[i][j] depends only on columns < j, and every inner product
+//   ssq = 0.0; for k = 0 .. j-1: ssq = ssq + L[i][k] * L[j][k]
+// is still summed one product at a time in increasing k, each product and
+// each sum rounded on its own (the file is built without FMA contraction).
+// Only the schedule changes: columns go in blocks of four; the four rows of
+// the diagonal block are finished first, one after another as in the
+// reference; then every group of four rows below carries the 16 running sums
+// of its four rows against the block's four columns through k < j0 together
+// (two-wide vectors whose lanes are separate sums, the block's columns packed
+// k-major), and finishes each row's four entries in column order.
+typedef double orc_v2d __attribute__((vector_size(16)));
+
+static int chol_blocked(int m, const double* D, double* L, int nthreads) {
+  constexpr int CB = 4;
+  int neg = 0;
+  std::vector<double> P((size_t)m * CB + 2 * CB, 0.0);
+#pragma omp parallel num_threads(nthreads)
+  for (int j0 = 0; j0 < m; j0 += CB) {
+    const int cb = std::min(CB, m - j0);
+#pragma omp single
+    {
+      // diagonal block: rows j0 .. j0+cb-1, columns j0 .. j, in the reference's order
+      for (int j = j0; j < j0 + cb; j++) {
+        double* Lj = L + (size_t)j * m;
+        for (int c = j0; c < j; c++) {
+          const double* Lc = L + (size_t)c * m;
+          double s = 0.0;
+          for (int k = 0; k < c; k++) s = s + Lj[k] * Lc[k];
+          Lj[c] = (D[(size_t)j * m + c] - s) / Lc[c];
+        }
+        double s = 0.0;
+        for (int k = 0; k < j; k++) s = s + Lj[k] * Lj[k];
+        double f = D[(size_t)j * m + j] - s;
+        if (f < 0) { neg++; f = -f; }
+        Lj[j] = std::sqrt(f);
+      }
+      // the block's columns k-major: P[4k + c] = L[j0 + c][k], k < j0
+      for (int k = 0; k < j0; k++)
+        for (int c = 0; c < CB; c++) P[(size_t)CB * k + c] = c < cb ? L[(size_t)(j0 + c) * m + k] : 0.0;
+    }
+    const int first = j0 + cb, groups = (m - first + 3) / 4;
+#pragma omp for schedule(static)
+    for (int g = 0; g < groups; g++) {
+      const int i0 = first + 4 * g, nr = std::min(4, m - i0);
+      const double* Li[4];
+      for (int r = 0; r < 4; r++) Li[r] = L + (size_t)(i0 + std::min(r, nr - 1)) * m;
+      orc_v2d a00 = {0.0, 0.0}, a01 = a00, a10 = a00, a11 = a00, a20 = a00, a21 = a00, a30 = a00, a31 = a00;
+      for (int k = 0; k < j0; k++) {
+        orc_v2d p0, p1;
+        std::memcpy(&p0, &P[(size_t)CB * k], sizeof p0);
+        std::memcpy(&p1, &P[(size_t)CB * k + 2], sizeof p1);
+        const orc_v2d b0 = {Li[0][k], Li[0][k]}, b1 = {Li[1][k], Li[1][k]};
+        const orc_v2d b2 = {Li[2][k], Li[2][k]}, b3 = {Li[3][k], Li[3][k]};
+        a00 = a00 + b0 * p0; a01 = a01 + b0 * p1;
+        a10 = a10 + b1 * p0; a11 = a11 + b1 * p1;
+        a20 = a20 + b2 * p0; a21 = a21 + b2 * p1;
+        a30 = a30 + b3 * p0; a31 = a31 + b3 * p1;
+      }
+      const orc_v2d acc[4][2] = {{a00, a01}, {a10, a11}, {a20, a21}, {a30, a31}};
+      for (int r = 0; r < nr; r++) {
+        double* Lr = L + (size_t)(i0 + r) * m;
+        for (int c = 0; c < cb; c++) {
+          const int j = j0 + c;
+          const double* Lj = L + (size_t)j * m;
+          double s = acc[r][c >> 1][c & 1];
+          for (int k = j0; k < j; k++) s = s + Lr[k] * Lj[k];
+          Lr[j] = (D[(size_t)(i0 + r) * m + j] - s) / Lj[j];
+        }
+      }
+    }
+  }
+  return neg;
+}
+
+// func.cpp:806-836.  One thread: the reference's row loop as written; more
+// threads: chol_blocked, which gives the same factor bit for bit.
 extern "C" int orc_cholesky(int m, const double* D, double* L, int nthreads) {
   int neg = 0;
   if (m <= 0) return 0;
@@ -1031,24 +1115,7 @@ extern "C" int orc_cholesky(int m, const double* D, double* L, int nthreads) {
     }
     return neg;
   }
-  // column 0, then for each column j: diagonal of row j, then rows i > j
-  for (int i = 1; i < m; i++) L[(size_t)i * m] = D[(size_t)i * m] / L[0];
-  for (int j = 1; j < m; j++) {
-    double* Lj = L + (size_t)j * m;
-    double ssq = 0.0;
-    for (int k = 0; k < j; k++) ssq = ssq + Lj[k] * Lj[k];
-    double f = D[(size_t)j * m + j] - ssq;
-    if (f < 0) { neg++; f = -f; }
-    Lj[j] = std::sqrt(f);
-#pragma omp parallel for num_threads(nthreads) schedule(static)
-    for (int i = j + 1; i < m; i++) {
-      double* Li = L + (size_t)i * m;
-      double s2 = 0.0;
-      for (int k = 0; k < j; k++) s2 = s2 + Li[k] * Lj[k];
-      Li[j] = (D[(size_t)i * m + j] - s2) / Lj[j];
-    }
-  }
-  return neg;
+  return chol_blocked(m, D, L, nthreads);
 }
 
 // Diffusion_Tensor's assembly part alone (func.cpp:737-804) for nD beads,
@@ -1197,8 +1264,9 @@ extern "C" double orc_step(void* h, const double* rr, const double* p) {
   Vec ra, D, L((size_t)m * m, 0.0);
   rall(S, X, ra);
   rpy(S, ra, D);
-  orc_cholesky(m, D.data(), L.data(), 1);
+  orc_cholesky(m, D.data(), L.data(), g_threads);
   S.rd.assign(m, 0.0);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(g_threads)
   for (int col = 0; col < m; col++) {  // rd_cal, func_cuda.cu:634-647
     double v = 0.0;
     for (int k = 0; k <= col; k++) v += S.s2dt * L[(size_t)col * m + k] * p[k];

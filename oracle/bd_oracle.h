@@ -65,6 +65,8 @@ int orc_set(void* h, const char* name, const double* in);
 // arithmetic column-parallel; results are bitwise identical.  Returns the
 // number of negative pivots that were replaced by their absolute value.
 int orc_cholesky(int m, const double* D, double* L, int nthreads);
+// Host threads used by orc_step for the RPY assembly, the Cholesky and rd.
+void orc_set_threads(int n);
 
 // RPY assembly alone (func.cpp:737-804) for nD beads, row-major 3nD x 3nD.
 void orc_rpy(int nD, const double* r, const double* rad, double a1, double a2, double* D);

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
         L.orc_set.argtypes = [C.c_void_p, C.c_char_p, _dp]
         L.orc_cholesky.argtypes = [C.c_int, _dp, _dp, C.c_int]
         L.orc_rpy.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]
+        L.orc_set_threads.argtypes = [C.c_int]
         L.orc_noise_create.restype = C.c_void_p
         L.orc_noise_create.argtypes = [C.c_ulong]
         L.orc_noise_destroy.argtypes = [C.c_void_p]
@@ -134,6 +135,11 @@ class Oracle:
         arr = np.ascontiguousarray(v, dtype=np.float64)
         if lib().orc_set(self._h, name.encode(), arr.ctypes.data_as(_dp)) < 0:
             raise KeyError(name)
+
+
+def set_threads(n: int) -> None:
+    """Host threads for the RPY assembly, Cholesky and rd of Oracle.step (results unchanged)."""
+    lib().orc_set_threads(int(n))
 
 
 def cholesky(D: np.ndarray, nthreads: int = 1) -> tuple[np.ndarray, int]:

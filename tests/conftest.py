@@ -9,7 +9,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_TESTDATA = "/root/reference/test_data"
+from oracle.refpath import REF_TESTDATA  # noqa: E402
 
 
 def pytest_configure(config):

@@ -26,7 +26,7 @@ from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, write_fiber  # noq
 from oracle.pyoracle import Reference  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF_DATA = "/root/reference/test_data"
+from oracle.refpath import REF_TESTDATA as REF_DATA  # noqa: E402
 
 
 def capture(name: str, directory: str, files: dict, seed: int, steps: int) -> None:
