@@ -585,6 +585,12 @@ extern "C" int bd_step_device(bd_ctx* c, const double* d_rr, const double* d_p, 
 
 extern "C" int bd_step(bd_ctx* c, const double* rr, const double* p, double* energy) {
   if (!c || !rr || !p) return set_error(BD_ERR_ARG, "bd_step: null argument");
+  // host noise is checked before anything is launched: a NaN or Inf would
+  // otherwise reach the positions and only show in the next step's energy
+  for (size_t i = 0, n = 3 * (size_t)c->M.n; i < n; i++)
+    if (!std::isfinite(rr[i])) return set_error(BD_ERR_NONFINITE, "bd_step: non-finite rotational noise");
+  for (size_t i = 0; i < (size_t)c->m; i++)
+    if (!std::isfinite(p[i])) return set_error(BD_ERR_NONFINITE, "bd_step: non-finite translational noise");
   CK(cudaMemcpyAsync(c->rr, rr, 3 * (size_t)c->M.n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   int rc = run_step(c, c->rr, c->p);

@@ -650,17 +650,26 @@ extern "C" int bd_restart_read(const char* path, bd_restart* rs, bd_noise* g) {
     if (a.second) ok = std::fread(a.first, sizeof(double), a.second, f) == a.second;
   }
   ok = ok && std::fread(rs->nc_lh_flag, sizeof(int32_t), rs->n_c, f) == (size_t)rs->n_c;
+  bool bad_idx = false;
   if (ok && g && h.has_noise) {
-    Mt19937& m = *reinterpret_cast<Mt19937*>(g);
+    // read into a copy first: the generator is changed only by a complete,
+    // valid state (its index must lie in [0, 625]; next() reads st[idx])
+    Mt19937 tmp;
     int32_t idx = 0, have = 0;
     double cached = 0.0;
-    ok = std::fread(m.st, sizeof m.st, 1, f) == 1 && std::fread(&idx, 4, 1, f) == 1 &&
+    ok = std::fread(tmp.st, sizeof tmp.st, 1, f) == 1 && std::fread(&idx, 4, 1, f) == 1 &&
          std::fread(&have, 4, 1, f) == 1 && std::fread(&cached, 8, 1, f) == 1;
-    m.idx = idx, m.have = have != 0, m.cached = cached;
+    bad_idx = ok && (idx < 0 || idx > 625);
+    if (ok && !bad_idx) {
+      Mt19937& m = *reinterpret_cast<Mt19937*>(g);
+      std::memcpy(m.st, tmp.st, sizeof m.st);
+      m.idx = idx, m.have = have != 0, m.cached = cached;
+    }
   }
   std::fclose(f);
   if (rc) return rc;
   if (!ok) return set_error(BD_ERR_IO, "bd_restart_read: truncated file");
+  if (bad_idx) return set_error(BD_ERR_IO, "bd_restart_read: generator index out of range");
   rs->step = (long)h.step;
   return BD_OK;
 }

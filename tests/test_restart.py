@@ -91,3 +91,25 @@ def test_text_restart_is_read_back_by_the_loader(tmp_path):
     for k in new:
         assert np.allclose(f1.state[k], new[k], rtol=0, atol=6e-16 * max(1.0, np.abs(new[k]).max()) * 10), k
     assert f1.sizes == f0.sizes
+
+
+def test_restart_rejects_generator_index_out_of_range(tmp_path):
+    """A restart file whose generator index lies outside [0, 625] is refused
+    and leaves the caller's generator as it was (next() would read st[idx])."""
+    import struct
+    g = Noise(11)
+    g.step(0, np.ones(21), 45)
+    good = str(tmp_path / "g.rst")
+    restart_write(good, 9, _arrays(), np.array([1, 1], dtype=np.int32), g)
+    data = bytearray(open(good, "rb").read())
+    # the generator's state ends the file: 624 words, index, cached flag, cached deviate
+    assert struct.unpack_from("<i", data, len(data) - 16)[0] == g.get_state()[1]
+    for bad in (626, 100000, -1):
+        struct.pack_into("<i", data, len(data) - 16, bad)
+        path = str(tmp_path / f"bad{bad}.rst")
+        open(path, "wb").write(bytes(data))
+        h, ref = Noise(3), Noise(3)
+        with pytest.raises(BDError, match="index"):
+            restart_read(path, h)
+        a, b = h.step(0, np.ones(21), 45), ref.step(0, np.ones(21), 45)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
