@@ -15,13 +15,21 @@
 //    (4 MiB), resident on every device that loads the library until exit.
 //  * Host code cannot use `g_scratch` as a device address (it names a host
 //    stand-in).  The first call on each device looks the real address up
-//    with cudaGetSymbolAddress, with that device current, and caches it;
-//    make that first call before any stream capture on the device.
+//    with cudaGetSymbolAddress, with that device current, and caches it
+//    together with the device's current CUDA context; a call that finds a
+//    different context (after cudaDeviceReset, say) looks it up again.
+//    With lazy module loading (the CUDA default) that first look-up loads
+//    this library's device code, and the 4 MiB array is committed at that
+//    moment: the first call on a device (and the first after a reset)
+//    allocates as any first use of a CUDA library does.  Make it once as a
+//    warm-up, before the region that must not allocate and before any stream
+//    capture on the device; every later call allocates nothing.
 //  * All calls share the one scratch array and it keeps the last call's
 //    contents.  Nothing in it has to start at zero: every partial sum a call
 //    reads was written by the same call.  Calls whose kernels overlap on
 //    the GPU (e.g. on two streams) race on the scratch and must be ordered
 //    by the caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -61,7 +69,33 @@ __global__ void k_na_sum(int m, int nchunk, const double* __restrict__ part, dou
 
 std::mutex g_mu;
 constexpr int kMaxDevices = 64;
-double* g_addr[kMaxDevices] = {};
+struct ScratchAddr {
+  CUcontext ctx = nullptr;  // context the address was looked up in
+  double* addr = nullptr;
+};
+ScratchAddr g_addr[kMaxDevices];
+
+// cuCtxGetCurrent through the runtime's driver entry point, so that the
+// library does not link libcuda itself (it must load on hosts without a GPU).
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+CtxGetCurrent ctx_get_current() {
+  static CtxGetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrent>(f);
+  }();
+  return fn;
+}
+
+CUcontext current_context() {
+  CUcontext c = nullptr;
+  CtxGetCurrent fn = ctx_get_current();
+  if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
 
 }  // namespace
 
@@ -81,8 +115,10 @@ extern "C" int bd_noise_displacement_noalloc(int m, const double* d_L, int lda, 
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-      // set-up, once per device, with that device current
+    ScratchAddr& a = g_addr[dev];
+    CUcontext cur = current_context();
+    if (!a.addr || !cur || cur != a.ctx) {
+      // set-up, once per device and context, with that device current
       void* ptr = nullptr;
       e = cudaGetSymbolAddress(&ptr, g_scratch);
       if (e != cudaSuccess) {
@@ -90,9 +126,10 @@ extern "C" int bd_noise_displacement_noalloc(int m, const double* d_L, int lda, 
         snprintf(b, sizeof b, "bd_noise_displacement_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
         return bdh::set_error(BD_ERR_CUDA, b);
       }
-      g_addr[dev] = static_cast<double*>(ptr);
+      a.addr = static_cast<double*>(ptr);
+      a.ctx = current_context();  // current now, if it was not before the look-up
     }
-    scratch = g_addr[dev];
+    scratch = a.addr;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nchunk = (m + kChunk - 1) / kChunk;

@@ -208,7 +208,10 @@ int bd_sizes(const bd_ctx* ctx, int* out8);
 /* One predictor-corrector BD step (main_cuda, func_cuda.cu:3434-3680).
  * rr[3n] and p[3 n_D] are host noise arrays; energy (may be NULL) receives
  * the pass-1 energy.  Host copies of the state are refreshed on return for
- * every non-NULL pointer in out_state-like arguments of bd_get_state. */
+ * every non-NULL pointer in out_state-like arguments of bd_get_state.
+ * Returns BD_ERR_NONFINITE, before launching anything, if rr or p holds a
+ * NaN or Inf, and after the step if its energy is not finite (the reference
+ * checks neither). */
 int bd_step(bd_ctx* ctx, const double* rr, const double* p, double* energy);
 
 /* Same step, noise already on the device (device pointers, stream-ordered). */
@@ -262,10 +265,15 @@ int bd_dev_potrf(bd_ctx* ctx, int m, double* d_A, int lda, int precision, int* d
  * partial sums live in a fixed 4 MiB device array inside the library, so
  * m must not exceed 16384 (BD_ERR_ARG otherwise).  The first call on a
  * device looks that array's device address up (cudaGetSymbolAddress, with
- * the device current) and caches it; make that first call before any stream
- * capture.  All calls share the array: calls whose kernels overlap on the
- * GPU race and must be ordered by the caller.  Nothing in the array needs
- * to start at zero. */
+ * the device current) and caches it with the device's current context; a
+ * call in a new context (after cudaDeviceReset) looks it up again.  Under
+ * lazy module loading (the CUDA default) that first look-up loads the
+ * library's device code and commits the 4 MiB array, so the first call on a
+ * device, and the first after a reset, allocates: make it once as a warm-up,
+ * before the region that must not allocate and before any stream capture.
+ * Later calls allocate nothing.  All calls share the array: calls whose
+ * kernels overlap on the GPU race and must be ordered by the caller.
+ * Nothing in the array needs to start at zero. */
 int bd_noise_displacement_noalloc(int m, const double* d_L, int lda, const double* d_p, double s2dt, double* d_rd,
                                   void* stream);
 
