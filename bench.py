@@ -430,20 +430,138 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def mixed_schedule_bytes(m: int, kT: int = 128, triple_min: int = 40, pair_min: int = 24) -> float:
+    """Algorithmic HBM bytes of one mixed factorisation of a 3N = m tensor: the
+    schedule of bdk::potrf_mixed (one launch per panel; three panels per bulk
+    pass while 40 tile rows remain, two while 24 do), 16 B (double-float read +
+    write) per element of the panel's column and of every trailing tile a bulk
+    pass updates.  Equals the library's own count (bd_kernel_bytes; 12.70 GB at
+    3N = 11,700)."""
+    nt = -(-m // kT)
+    kb = lambda k: m - k * kT if m - k * kT < kT else kT  # noqa: E731
+
+    def elems(j0, j1):
+        e = 0.0
+        for J in range(j0, min(j1, nt)):
+            cols = kb(J)
+            e += cols * (m - J * kT) - cols * (cols - 1) / 2
+        return e
+
+    total = 0.0
+
+    def launch(pn, jobs):
+        nonlocal total
+        total += 16.0 * (m - pn * kT) * kb(pn)
+        for mode, jlo in jobs:
+            n = nt - jlo
+            if n > 0:
+                total += 16.0 * elems(jlo, jlo + 1 if mode == "col" else nt)
+
+    launch(0, [])
+    k = 0
+    while k + 1 < nt:
+        if nt - (k + 4) >= triple_min:
+            launch(k + 1, [("col", k + 2)])
+            launch(k + 2, [("col", k + 3)])
+            launch(k + 3, [("tri", k + 4)])
+            k += 3
+        elif nt - (k + 3) >= pair_min:
+            launch(k + 1, [("col", k + 2)])
+            launch(k + 2, [("tri", k + 3)])
+            k += 2
+        else:
+            launch(k + 1, [("tri", k + 2)])
+            k += 1
+    return total
+
+
+def batch_fp64_comparison(fibers, host, d_rr, d_p, local, stream) -> dict:
+    """The plain FP64 GPU step on the same replicas and noise: one step of a
+    mixed and an FP64 batch from the same start states (relative displacement
+    error of every replica: max |dr_mixed - dr_fp64| / max |dr_fp64| over r,
+    r_t, r_lh), then two timed FP64 batch steps (CUDA graph, CUDA events)."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Batch
+    R = len(fibers)
+    bm = Batch(fibers, precision=PREC_MIXED, use_graph=False, device=local, stream=stream.cuda_stream)
+    b64 = Batch(fibers, precision=PREC_FP64, use_graph=True, device=local, stream=stream.cuda_stream)
+    rr0, p0 = [h[0][0] for h in host], [h[0][1] for h in host]
+    bm.step(rr0, p0)
+    b64.step(rr0, p0)
+    errs = []
+    for cm, c64, f in zip(bm.contexts, b64.contexts, fibers):
+        num = den = 0.0
+        for k in ("r", "r_t", "r_lh"):
+            if f.state[k].size == 0:
+                continue
+            d64 = c64.get(k) - f.state[k]
+            dm = cm.get(k) - f.state[k]
+            num = max(num, float(np.abs(dm - d64).max()))
+            den = max(den, float(np.abs(d64).max()))
+        errs.append(num / den)
+    bm.close()
+    steps = 2
+    with torch.cuda.stream(stream):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(1, 1 + steps):
+            b64.step_device([x[s].data_ptr() for x in d_rr], [x[s].data_ptr() for x in d_p])
+        e1.record(stream)
+        stream.synchronize()
+    ms64 = e0.elapsed_time(e1) / steps
+    b64.close()
+    return {"fp64_replica_steps_per_s": R * 1000.0 / ms64, "fp64_ms_per_step": ms64, "fp64_steps_timed": steps,
+            "rel_displacement_err_max": max(errs), "rel_displacement_err_median": float(np.median(errs)),
+            "tolerance": 1e-6}
+
+
+def batch_cpu_sample(dirs, budget_s: float = 15.0) -> dict:
+    """Complete oracle steps of the replicas in order (one each, the fibers
+    read by the oracle's reader restatement) until `budget_s` of CPU time;
+    replica-steps/s over the replicas done."""
+    from oracle import ref_loader
+    from oracle.pyoracle import Oracle, OracleNoise, set_threads
+    threads = os.cpu_count() or 1
+    set_threads(threads)
+    done, total, ms = 0, 0.0, []
+    for i, (d, files) in enumerate(dirs):
+        fib = ref_loader.load(d, **files)
+        o = Oracle(fib)
+        rr, p = OracleNoise(1000 + i).step(0, fib.arrays["r_var"], fib.m)
+        t = time.perf_counter()
+        o.step(rr, p)
+        total += time.perf_counter() - t
+        done += 1
+        ms.append(fib.m)
+        if total >= budget_s:
+            break
+    return {"value": done / total, "unit": "replica-steps/s", "cores": threads, "kind": "port",
+            "sample": f"one complete oracle step of each of the first {done} replicas (3N {min(ms)}-{max(ms)}), "
+                      f"{total:.1f} s; RPY, the reference Cholesky (bit for bit, column-blocked on {threads} "
+                      f"threads), rd, two force passes, two moves"}
+
+
 def run_batch(args):
     """Config 2: replicas of uneven size and salt (nucleosomes 12-48, linkers
     20-60 bp, 50/100/150 mM) advanced together through bd_batch_* (one CUDA
-    graph per batch step); metric replica-steps/s."""
+    graph per batch step); metric replica-steps/s.  Beside it: the batched
+    factorisation's roofline (phase times of one eager step), the plain FP64
+    batch on the same replicas (rate and every replica's displacement error),
+    and complete CPU oracle steps of a bounded sample of the replicas."""
     import torch
-    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Batch, Noise
-    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber as mk
+    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Batch, Fiber, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, write_fiber
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
-    fibers = [mk(config(2, seed=1 + rank, replica=i), tempfile.mkdtemp(prefix="bdrep_")) for i in range(args.replicas)]
+    dirs = []
+    for i in range(args.replicas):
+        d = tempfile.mkdtemp(prefix="bdrep_")
+        dirs.append((d, write_fiber(config(2, seed=1 + rank, replica=i), d)))
+    fibers = [Fiber.load(d, **files) for d, files in dirs]
     stream = torch.cuda.Stream()
     b = Batch(fibers, precision=prec, use_graph=True, device=local, stream=stream.cuda_stream)
-    nsteps = args.warmup + args.steps
+    nsteps = max(args.warmup + args.steps, 3)
     gens = [Noise(1000 + i) for i in range(len(fibers))]
     host = [[g.step(s, f.arrays["r_var"], f.m) for s in range(nsteps)] for g, f in zip(gens, fibers)]
     d_rr = [[torch.tensor(h[s][0], device="cuda") for s in range(nsteps)] for h in host]
@@ -457,20 +575,44 @@ def run_batch(args):
         clk.start()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for s in range(args.warmup, nsteps):
+        for s in range(args.warmup, args.warmup + args.steps):
             b.step_device([x[s].data_ptr() for x in d_rr], [x[s].data_ptr() for x in d_p])
         e1.record(stream)
         stream.synchronize()
         clocks = clk.stop()
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     value = world * len(fibers) * 1000.0 / ms
+    launches = b.launch_count() * args.steps
     # e2e: host noise per replica per step through bd_batch_step
     t0 = time.perf_counter()
-    for s in range(args.warmup, nsteps):
+    for s in range(args.warmup, args.warmup + args.steps):
         b.step([h[s][0] for h in host], [h[s][1] for h in host])
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     h2d = sum((3 * f.sizes["n"] + f.m) * 8 for f in fibers)
     sizes = [f.m for f in fibers]
+    # phases of one eager step (timing on: no graph), for the roofline
+    b.phase_times()
+    b.step([h[0][0] for h in host], [h[0][1] for h in host])
+    ph = b.phase_times()
+    roof = None
+    if prec == PREC_MIXED and ph[1] > 0:
+        pk = peaks()
+        byt = sum(mixed_schedule_bytes(m) for m in sizes)
+        achieved = byt / (ph[1] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": byt * NCU_TRAFFIC_PER_ALG_BYTE,
+                "traffic_source": "DRAM read+write per algorithmic byte of one ncu capture of k_chol_step at "
+                                  "3N = 11,700, times this batch's algorithmic bytes",
+                "kernel": "k_chol_step_multi (every replica's mixed factorisation, launch i carrying step i of "
+                          "every replica's schedule), phase time of one eager batch step",
+                "algorithmic_bytes_per_step": byt, "factorisation_phase_ms": float(ph[1]),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    b.close()
+    vs64 = None
+    if prec == PREC_MIXED and not args.no_fp64:
+        vs64 = batch_fp64_comparison(fibers, host, d_rr, d_p, local, stream)
+        vs64["speedup_vs_fp64"] = value / (world * vs64["fp64_replica_steps_per_s"])
+    cpu = batch_cpu_sample(dirs) if rank == 0 and world == 1 and not args.no_cpu else None
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "replica-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -481,9 +623,11 @@ def run_batch(args):
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2"},
                 "e2e": {"value": world * len(fibers) / e2e_s, "unit": "replica-steps/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": 8 * len(fibers)},
-                "gpu_launches": None, "clocks": clocks, "roofline": None, "cpu_baseline": None}
+                "gpu_launches": launches, "clocks": clocks, "roofline": roof, "vs_fp64": vs64,
+                "phases_ms": {"positions+tensors": float(ph[0]), "factorisation": float(ph[1]),
+                              "forces+moves": float(ph[2])},
+                "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
-    b.close()
 
 
 def run_adjoint(args):

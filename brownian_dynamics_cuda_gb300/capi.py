@@ -144,6 +144,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_batch_step.argtypes = [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp), _dp]
     L.bd_batch_step_device.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
     L.bd_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_ulong, _dp]
+    L.bd_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    L.bd_batch_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.bd_step_reference.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp] + [_dp] * 6
     L.bd_forces.argtypes = [C.c_void_p] + [_dp] * 5
     L.bd_diffusion_tensor.argtypes = [C.c_void_p, _dp]
@@ -592,6 +594,19 @@ class Batch:
         a = (C.c_void_p * R)(*[C.c_void_p(x) for x in d_rr])
         b = (C.c_void_p * R)(*[C.c_void_p(x) for x in d_p])
         _check(self._L.bd_batch_step_device(self._h, a, b))
+
+    def phase_times(self) -> np.ndarray:
+        """bd_batch_phase_times: [positions + tensors, factorisation, forces + moves] ms of
+        the last eager step; the first call switches timing on."""
+        out = (C.c_float * 3)()
+        _check(self._L.bd_batch_phase_times(self._h, out))
+        return np.array(list(out))
+
+    def launch_count(self) -> int:
+        """Kernel launches of the last batch step enqueued (bd_batch_launch_count)."""
+        n = C.c_int()
+        _check(self._L.bd_batch_launch_count(self._h, C.byref(n)))
+        return n.value
 
     def run(self, nsteps: int, seed_base: int) -> np.ndarray:
         e = np.zeros(len(self))

@@ -849,6 +849,11 @@ struct bd_batch {
   // kBatchLanes streams side by side (no tensor-core kernel among them)
   std::vector<cudaStream_t> lane;
   std::vector<cudaEvent_t> ev;  // [0]: fork, [1 + k]: join of lane k
+  // phase timing (bd_batch_phase_times): while on, steps run eagerly with
+  // events around the three phases of a batched mixed step
+  bool timing = false, timed = false;
+  cudaEvent_t tev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int launches = 0;  // kernel launches of the last batch step enqueued
 };
 
 constexpr int kBatchLanes = 64;
@@ -900,6 +905,7 @@ static int batch_lanes(bd_batch* b, int ph) {
     c->stream = b->lane[i % nl];
     rc = step_phases(c, c->rr, c->p, nullptr, ph);
     c->stream = b->stream;
+    b->launches += c->last_launches;
   }
   for (int k = 0; k < nl; k++) {
     CK(cudaEventRecord(b->ev[1 + k], b->lane[k]));
@@ -910,24 +916,36 @@ static int batch_lanes(bd_batch* b, int ph) {
 
 static int batch_enqueue(bd_batch* b) {
   int rc = BD_OK;
+  b->launches = 0;
   if (!b->chol) {
-    for (bd_ctx* c : b->ctx)
+    for (bd_ctx* c : b->ctx) {
       if (!rc) rc = step_device(c, c->rr, c->p);
+      b->launches += c->last_launches;
+    }
     return rc;
   }
+  const bool ev = b->timing;
+  if (ev) CK(cudaEventRecord(b->tev[0], b->stream));
   if ((rc = batch_lanes(b, kPre))) return rc;
+  if (ev) CK(cudaEventRecord(b->tev[1], b->stream));
   {
     bdh::Range range("bd_batch: factorisations");
-    bdk::mixed_batch_run(b->chol, b->stream);  // alone on the GPU: the only tensor-core kernel of the step
+    b->launches += bdk::mixed_batch_run(b->chol, b->stream);  // alone on the GPU: the only tensor-core kernel of the step
   }
   CK(cudaGetLastError());
-  return batch_lanes(b, kPost);
+  if (ev) CK(cudaEventRecord(b->tev[2], b->stream));
+  rc = batch_lanes(b, kPost);
+  if (ev && !rc) {
+    CK(cudaEventRecord(b->tev[3], b->stream));
+    b->timed = true;
+  }
+  return rc;
 }
 
 static int batch_device_step(bd_batch* b) {
   int prc = batch_prepare(b);
   if (prc) return prc;
-  bool graph_ok = b->use_graph;
+  bool graph_ok = b->use_graph && !b->timing;
   for (bd_ctx* c : b->ctx) graph_ok = graph_ok && c->freq_rp == 1;
   if (graph_ok) {
     if (!b->graph) {
@@ -995,6 +1013,8 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
     if (s) cudaStreamDestroy(s);
   for (auto e : b->ev)
     if (e) cudaEventDestroy(e);
+  for (auto e : b->tev)
+    if (e) cudaEventDestroy(e);
   for (bd_ctx* c : b->ctx) bd_destroy(c);
   for (bd_noise* g : b->noise) bd_noise_free(g);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -1005,6 +1025,28 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
 extern "C" int bd_batch_size(const bd_batch* b, int* nrep) {
   if (!b || !nrep) return set_error(BD_ERR_ARG, "bd_batch_size: null argument");
   *nrep = (int)b->ctx.size();
+  return BD_OK;
+}
+
+extern "C" int bd_batch_launch_count(const bd_batch* b, int* out) {
+  if (!b || !out) return set_error(BD_ERR_ARG, "bd_batch_launch_count: null argument");
+  *out = b->launches;
+  return BD_OK;
+}
+
+extern "C" int bd_batch_phase_times(bd_batch* b, float* out3) {
+  if (!b || !out3) return set_error(BD_ERR_ARG, "bd_batch_phase_times: null argument");
+  for (int k = 0; k < 3; k++) out3[k] = 0.f;
+  if (!b->timing) {
+    for (auto& e : b->tev)
+      if (!e) CK(cudaEventCreate(&e));
+    b->timing = true;
+    b->timed = false;
+    return BD_OK;
+  }
+  if (!b->timed) return BD_OK;
+  CK(cudaEventSynchronize(b->tev[3]));
+  for (int k = 0; k < 3; k++) CK(cudaEventElapsedTime(&out3[k], b->tev[k], b->tev[k + 1]));
   return BD_OK;
 }
 

@@ -45,7 +45,10 @@ const char* bd_version(void);
 /* --------------------------------------------------------------- precision */
 enum {
   BD_PREC_FP64 = 0,   /* plain FP64 step: parity path against the FP64 oracle */
-  BD_PREC_MIXED = 1   /* tensor-core Cholesky (BF16 split operands), FP64 refinement */
+  BD_PREC_MIXED = 1   /* FP32-class: RPY tensor in FP32 into double-float storage, Cholesky with
+                         FP32 panels and BF16x3 tensor-core (tcgen05) trailing updates, FP32
+                         pair forces with compensated sums; no refinement.  Displacement
+                         within 7e-7 of the FP64 path at 3N <= 46,200 (bound 1e-6) */
 };
 
 /* ------------------------------------------------------------ model (host)
@@ -291,6 +294,16 @@ int bd_batch_destroy(bd_batch* b);
 int bd_batch_size(const bd_batch* b, int* nrep);
 /* The context of replica i (for bd_get_state, bd_set_state, bd_forces ...). */
 int bd_batch_context(bd_batch* b, int i, bd_ctx** out);
+/* Phase times of a batched mixed step, in ms: every replica's positions and
+ * tensor, the batched factorisation, every replica's forces and moves.  The
+ * first call switches timing on (zeros returned); while on, batch steps run
+ * eagerly (no graph) with CUDA events around the phases, and later calls
+ * return the last step's times.  Measurement only; no counterpart in the
+ * reference. */
+int bd_batch_phase_times(bd_batch* b, float* out3);
+/* Kernel launches of the last batch step enqueued (a graph replays the same
+ * launches).  No counterpart in the reference. */
+int bd_batch_launch_count(const bd_batch* b, int* out);
 /* One step of every replica: rr[i], p[i] are replica i's host noise (as for
  * bd_step); energies[i] (optional) receives its energy. */
 int bd_batch_step(bd_batch* b, const double* const* rr, const double* const* p, double* energies);

@@ -86,3 +86,48 @@ def test_mixed_factor_more_panels_than_sms(tmp_path):
     assert cm.negative_pivots() == 0
     r64 = Context(fib, precision=PREC_FP64).noise_displacement(p)
     assert np.abs(rm - r64).max() <= 1e-6 * np.abs(r64).max()
+
+
+def test_concurrent_mixed_steps_on_two_streams(cfg1):
+    """Two contexts' mixed steps (each a CUDA graph with the 92-launch
+    tensor-core factorisation) replayed on two streams at once, so that
+    k_chol_step launches of the two run side by side on the GPU: every
+    state equals that of the same steps run one context after the other,
+    bit for bit, eight steps each."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import PREC_MIXED, Context, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber
+    import tempfile
+    fibs = [cfg1, make_fiber(config(1, seed=2), tempfile.mkdtemp())]
+    steps = 8
+    noise = []
+    for i, f in enumerate(fibs):
+        g = Noise(300 + i)
+        rows = [g.step(s, f.arrays["r_var"], f.m) for s in range(steps)]
+        noise.append(([torch.tensor(r[0], device="cuda") for r in rows],
+                      [torch.tensor(r[1], device="cuda") for r in rows]))
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+
+    def run(concurrent):
+        ctx = [Context(f, precision=PREC_MIXED, use_graph=True, stream=s.cuda_stream) for f, s in zip(fibs, streams)]
+        torch.cuda.synchronize()
+        if concurrent:
+            for s in range(steps):
+                for c, (rr, p) in zip(ctx, noise):
+                    c.step_device(rr[s].data_ptr(), p[s].data_ptr())
+        else:
+            for c, (rr, p), st in zip(ctx, noise, streams):
+                for s in range(steps):
+                    c.step_device(rr[s].data_ptr(), p[s].data_ptr())
+                st.synchronize()
+        torch.cuda.synchronize()
+        out = [{k: c.get(k) for k in ("r", "a", "r_t", "r_lh")} for c in ctx]
+        assert all(c.negative_pivots() == 0 for c in ctx)
+        for c in ctx:
+            c.close()
+        return out
+
+    seq, conc = run(False), run(True)
+    for i in range(2):
+        for k in seq[i]:
+            assert np.array_equal(seq[i][k], conc[i][k]), (i, k)
