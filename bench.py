@@ -475,44 +475,56 @@ def mixed_schedule_bytes(m: int, kT: int = 128, triple_min: int = 40, pair_min: 
     return total
 
 
-def batch_fp64_comparison(fibers, host, d_rr, d_p, local, stream) -> dict:
-    """The plain FP64 GPU step on the same replicas and noise: one step of a
-    mixed and an FP64 batch from the same start states (relative displacement
-    error of every replica: max |dr_mixed - dr_fp64| / max |dr_fp64| over r,
-    r_t, r_lh), then two timed FP64 batch steps (CUDA graph, CUDA events)."""
+def batch_fp64_comparison(fibers, host, d_rr, d_p, local, stream, passes_list=(3, 1)) -> dict:
+    """The plain FP64 GPU step on the same replicas and noise: one FP64 batch
+    step from the start states (its displacements kept), two timed FP64 batch
+    steps (CUDA graph, CUDA events); then, for each mixed schedule (at most
+    `passes` panels per trailing pass; 3 is the default), one mixed batch step
+    from the same start states — every replica's relative displacement error
+    max |dr_mixed - dr_fp64| / max |dr_fp64| over r, r_t, r_lh — and two timed
+    mixed steps of that schedule."""
     import torch
     from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Batch
     R = len(fibers)
-    bm = Batch(fibers, precision=PREC_MIXED, use_graph=False, device=local, stream=stream.cuda_stream)
-    b64 = Batch(fibers, precision=PREC_FP64, use_graph=True, device=local, stream=stream.cuda_stream)
     rr0, p0 = [h[0][0] for h in host], [h[0][1] for h in host]
-    bm.step(rr0, p0)
+    keys = ("r", "r_t", "r_lh")
+
+    def timed(b, steps=2):
+        with torch.cuda.stream(stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for s in range(1, 1 + steps):
+                b.step_device([x[s].data_ptr() for x in d_rr], [x[s].data_ptr() for x in d_p])
+            e1.record(stream)
+            stream.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    b64 = Batch(fibers, precision=PREC_FP64, use_graph=True, device=local, stream=stream.cuda_stream)
     b64.step(rr0, p0)
-    errs = []
-    for cm, c64, f in zip(bm.contexts, b64.contexts, fibers):
-        num = den = 0.0
-        for k in ("r", "r_t", "r_lh"):
-            if f.state[k].size == 0:
-                continue
-            d64 = c64.get(k) - f.state[k]
-            dm = cm.get(k) - f.state[k]
-            num = max(num, float(np.abs(dm - d64).max()))
-            den = max(den, float(np.abs(d64).max()))
-        errs.append(num / den)
-    bm.close()
-    steps = 2
-    with torch.cuda.stream(stream):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for s in range(1, 1 + steps):
-            b64.step_device([x[s].data_ptr() for x in d_rr], [x[s].data_ptr() for x in d_p])
-        e1.record(stream)
-        stream.synchronize()
-    ms64 = e0.elapsed_time(e1) / steps
+    ref = [{k: c.get(k) - f.state[k] for k in keys if f.state[k].size} for c, f in zip(b64.contexts, fibers)]
+    ms64 = timed(b64)
     b64.close()
-    return {"fp64_replica_steps_per_s": R * 1000.0 / ms64, "fp64_ms_per_step": ms64, "fp64_steps_timed": steps,
-            "rel_displacement_err_max": max(errs), "rel_displacement_err_median": float(np.median(errs)),
-            "tolerance": 1e-6}
+    out = {"fp64_replica_steps_per_s": R * 1000.0 / ms64, "fp64_ms_per_step": ms64, "fp64_steps_timed": 2,
+           "tolerance": 1e-6}
+    for passes in passes_list:
+        bm = Batch(fibers, precision=PREC_MIXED, use_graph=True, device=local, stream=stream.cuda_stream)
+        bm.set_mixed_passes(passes)
+        bm.step(rr0, p0)
+        errs = []
+        for c, f, d64 in zip(bm.contexts, fibers, ref):
+            num = max(float(np.abs((c.get(k) - f.state[k]) - d64[k]).max()) for k in d64)
+            den = max(float(np.abs(d64[k]).max()) for k in d64)
+            errs.append(num / den)
+        ms = timed(bm)
+        bm.close()
+        leg = {"replica_steps_per_s": R * 1000.0 / ms, "ms_per_step": ms, "rel_displacement_err_max": max(errs),
+               "rel_displacement_err_median": float(np.median(errs)),
+               "replicas_over_tolerance": int(sum(e > 1e-6 for e in errs))}
+        out[f"mixed_passes{passes}"] = leg
+        if passes == 3:
+            out["rel_displacement_err_max"] = leg["rel_displacement_err_max"]
+            out["rel_displacement_err_median"] = leg["rel_displacement_err_median"]
+    return out
 
 
 def batch_cpu_sample(dirs, budget_s: float = 15.0) -> dict:

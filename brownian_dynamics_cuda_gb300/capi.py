@@ -146,6 +146,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_ulong, _dp]
     L.bd_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.bd_batch_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    L.bd_set_mixed_passes.argtypes = [C.c_void_p, C.c_int]
+    L.bd_batch_set_mixed_passes.argtypes = [C.c_void_p, C.c_int]
     L.bd_step_reference.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp] + [_dp] * 6
     L.bd_forces.argtypes = [C.c_void_p] + [_dp] * 5
     L.bd_diffusion_tensor.argtypes = [C.c_void_p, _dp]
@@ -506,6 +508,11 @@ class Context:
         _check(self._L.bd_launch_count(self._h, C.byref(v)))
         return v.value
 
+    def set_mixed_passes(self, passes: int) -> None:
+        """bd_set_mixed_passes: at most `passes` panels per trailing pass of the mixed
+        factorisation (3 fastest, 1 most accurate)."""
+        _check(self._L.bd_set_mixed_passes(self._h, int(passes)))
+
     def negative_pivots(self) -> int:
         v = C.c_int()
         _check(self._L.bd_negative_pivots(self._h, C.byref(v)))
@@ -601,6 +608,10 @@ class Batch:
         out = (C.c_float * 3)()
         _check(self._L.bd_batch_phase_times(self._h, out))
         return np.array(list(out))
+
+    def set_mixed_passes(self, passes: int) -> None:
+        """bd_batch_set_mixed_passes: at most `passes` panels per trailing pass (1 = most accurate)."""
+        _check(self._L.bd_batch_set_mixed_passes(self._h, int(passes)))
 
     def launch_count(self) -> int:
         """Kernel launches of the last batch step enqueued (bd_batch_launch_count)."""

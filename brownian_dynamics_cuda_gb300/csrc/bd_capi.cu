@@ -165,7 +165,7 @@ static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double*
       c->kev_pairs = 0;
       L += bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, st, kt ? c->kev.data() : nullptr,
                             kt ? &c->kev_pairs : nullptr, kt ? &c->kflop : nullptr,
-                            kt ? &c->kbytes : nullptr);
+                            kt ? &c->kbytes : nullptr, c->mixed_passes);
     }
     else L += bdk::potrf_fp64(c->m, c->A, c->lda, nullptr, nullptr, 0.0, c->negpiv, st);
   }
@@ -681,7 +681,8 @@ static int factor_now(bd_ctx* c) {
   assemble_now(c);
   CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
   if (c->precision == BD_PREC_MIXED) {
-    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream);
+    bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream, nullptr, nullptr, nullptr, nullptr,
+                     c->mixed_passes);
     int derr = 0;
     CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -882,13 +883,16 @@ static int batch_prepare(bd_batch* b) {
       bd_ctx* c = b->ctx[i];
       m[i] = c->m, lda[i] = c->lda, A[i] = c->A, PS[i] = c->PS, np[i] = c->negpiv, er[i] = c->d_err;
     }
-    b->chol = bdk::mixed_batch_create((int)nr, m.data(), A.data(), lda.data(), PS.data(), np.data(), er.data());
+    b->chol = bdk::mixed_batch_create((int)nr, m.data(), A.data(), lda.data(), PS.data(), np.data(), er.data(),
+                                      b->ctx[0]->mixed_passes);
     if (!b->chol) return set_error(BD_ERR_NOMEM, "bd_batch: batched factorisation plan");
-    const int nl = (int)std::min<size_t>(nr, kBatchLanes);
-    b->lane.resize(nl, nullptr);
-    b->ev.resize(1 + nl, nullptr);
-    for (auto& s : b->lane) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    for (auto& e : b->ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (b->lane.empty()) {  // kept when the plan is rebuilt (bd_batch_set_mixed_passes)
+      const int nl = (int)std::min<size_t>(nr, kBatchLanes);
+      b->lane.resize(nl, nullptr);
+      b->ev.resize(1 + nl, nullptr);
+      for (auto& s : b->lane) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      for (auto& e : b->ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
   }
   return BD_OK;
 }
@@ -1025,6 +1029,28 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
 extern "C" int bd_batch_size(const bd_batch* b, int* nrep) {
   if (!b || !nrep) return set_error(BD_ERR_ARG, "bd_batch_size: null argument");
   *nrep = (int)b->ctx.size();
+  return BD_OK;
+}
+
+extern "C" int bd_set_mixed_passes(bd_ctx* c, int passes) {
+  if (!c || passes < 1 || passes > 3) return set_error(BD_ERR_ARG, "bd_set_mixed_passes: passes is 1, 2 or 3");
+  if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_mixed_passes: the context belongs to a batch");
+  if (c->mixed_passes != passes && c->graph) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(c->graph);  // the captured step holds the old schedule
+    c->graph = nullptr;
+  }
+  c->mixed_passes = passes;
+  return BD_OK;
+}
+
+extern "C" int bd_batch_set_mixed_passes(bd_batch* b, int passes) {
+  if (!b || passes < 1 || passes > 3) return set_error(BD_ERR_ARG, "bd_batch_set_mixed_passes: passes is 1, 2 or 3");
+  CK(cudaStreamSynchronize(b->stream));
+  if (b->graph) cudaGraphExecDestroy(b->graph), b->graph = nullptr;
+  bdk::mixed_batch_free(b->chol);  // the plan is built again at the next step
+  b->chol = nullptr;
+  for (bd_ctx* c : b->ctx) c->mixed_passes = passes;
   return BD_OK;
 }
 

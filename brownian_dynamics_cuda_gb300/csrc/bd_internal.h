@@ -146,9 +146,10 @@ int set_mixed_attributes();
 // (the dominant kernel); *kev_pairs = how many were recorded, *kflop and
 // *kbytes accumulate the tensor work those launches issue and their
 // algorithmic HBM bytes.
+// max_pass: at most this many panels (1..3) per bulk trailing pass.
 int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
                 cudaEvent_t* kev = nullptr, int* kev_pairs = nullptr, double* kflop = nullptr,
-                double* kbytes = nullptr);
+                double* kbytes = nullptr, int max_pass = 3);
 int mixed_tiles(int m);
 int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at most
 // Many mixed factorisations (replicas) advanced together: launch i runs step
@@ -156,7 +157,7 @@ int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at
 // scatter for all.  The plan holds the matrices' addresses.
 struct MixedBatch;
 MixedBatch* mixed_batch_create(int nrep, const int* m, double* const* A, const int* lda, unsigned char* const* PS,
-                               int* const* negpiv, int* const* err);
+                               int* const* negpiv, int* const* err, int max_pass = 3);
 int mixed_batch_run(const MixedBatch* b, cudaStream_t st);  // returns the launches issued
 void mixed_batch_free(MixedBatch* b);
 
@@ -188,6 +189,7 @@ struct bd_ctx {
   int precision = BD_PREC_FP64;
   int freq_rp = 1;
   int use_graph = 0;
+  int mixed_passes = 3;  // panels per bulk trailing pass of the mixed factorisation (bd_set_mixed_passes)
   long step_count = 0;
   DevModel M{};
   DevState X{}, Y{};

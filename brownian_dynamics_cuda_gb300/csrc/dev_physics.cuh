@@ -109,6 +109,17 @@ __device__ __forceinline__ V3 pair_f1(double q1, double q2, double eps, double k
 
 __device__ __forceinline__ float clamp09f(float v) { return fminf(fmaxf(v, -0.9f), 0.9f); }
 
+// The Debye-Hueckel (7 nm) and Lennard-Jones (4 nm) cut-offs truncate the
+// pair force without a shift, so it jumps there.  An FP32 distance carries an
+// error of ~2e-6 nm near 7 nm; a pair closer than that to a cut-off can fall
+// on the other side than in the FP64 path and move a bead by the whole jump.
+// Inside this guard band (50x that error) the FP32 pair terms decide the
+// cut-offs from the FP64 distance instead; the band holds ~3e-5 of the pairs.
+constexpr float kCutGuard = 1e-4f;
+__device__ __forceinline__ bool near_cutoff(float d) {
+  return fabsf(d - 7.f) < kCutGuard || fabsf(d - 4.f) < kCutGuard;
+}
+
 // Mixed-precision form of pair_f1 for the tensor-core step: the separation
 // is formed in FP64 (large absolute coordinates cost nothing), the rest of
 // the pair in FP32 (sqrt, exp, powers of sigma/d by multiplication), and the
@@ -119,15 +130,20 @@ __device__ __forceinline__ V3 pair_f1_mx(double q1, double q2, double eps, doubl
   const float dx = (float)(c1.x - c2.x), dy = (float)(c1.y - c2.y), dz = (float)(c1.z - c2.z);
   const float d2 = dx * dx + dy * dy + dz * dz;
   const float d = sqrtf(d2);
+  bool in7 = d < 7.f, in4 = d < 4.f;
+  if (near_cutoff(d)) {  // the cut-offs make the force jump: decide as the FP64 path does
+    const double d64 = dist3(c1, c2);
+    in7 = d64 < 7.0, in4 = d64 < 4.0;
+  }
   float t = 0.f;
-  if (DH && d < 7.f) {
+  if (DH && in7) {
     const float kap = (float)kappa;
     const float qq = (float)(q1 * q2 / (4 * kPi * eps));
     const float ex = expf(-kap * d);
     t = qq * (kap * d + 1.f) * ex / d2;
     if (E) *E = *E + (double)(qq * ex / d);
   }
-  if (LJ && d < 4.f) {
+  if (LJ && in4) {
     const float sr = (float)sig / d, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
     const float kv = (float)kev;
     t = t - kv * (6.f * sr6 - 12.f * sr12) / d;

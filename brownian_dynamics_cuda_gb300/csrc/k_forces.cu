@@ -1164,19 +1164,34 @@ __global__ void k_mirror(DevModel M, DevState X, float4* ph, float4* pl, int npo
   pl[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.f);
 }
 
-// force on particle 1 from particle 2, d = c1 - c2; qq = k_e q1 q2
+// The FP64 distance of two double-float positions, formed as dist3 forms it
+// from the FP64 positions (hi + lo is the FP64 position to 2^-48 relative).
+__device__ __noinline__ double dist_pf64(const PF& a, const PF& b) {
+  const V3 u{(double)a.h.x + (double)a.l.x, (double)a.h.y + (double)a.l.y, (double)a.h.z + (double)a.l.z};
+  const V3 v{(double)b.h.x + (double)b.l.x, (double)b.h.y + (double)b.l.y, (double)b.h.z + (double)b.l.z};
+  return dist3(u, v);
+}
+
+// force on particle 1 (a) from particle 2 (b); qq = k_e q1 q2.  Near a
+// cut-off the decision is the FP64 path's (near_cutoff).
 template <bool DH, bool LJ>
-__device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float sig, float3 d, float& E) {
+__device__ __forceinline__ float3 pairf(float qq, float kap, float kev, float sig, const PF& a, const PF& b, float& E) {
+  const float3 d = sepf(a, b);
   const float d2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
   const float rinv = rsqrtf(d2);  // 1/d: one reciprocal square root instead of a root and divisions
   const float dd = d2 * rinv;
+  bool in7 = dd < 7.f, in4 = dd < 4.f;
+  if (near_cutoff(dd)) {
+    const double d64 = dist_pf64(a, b);
+    in7 = d64 < 7.0, in4 = d64 < 4.0;
+  }
   float t = 0.f;
-  if (DH && dd < 7.f) {
+  if (DH && in7) {
     const float qe = qq * expf(-kap * dd) * rinv;  // k_e q1 q2 e^{-kappa d} / d
     t = qe * fmaf(kap, dd, 1.f) * rinv;
     E += qe;
   }
-  if (LJ && dd < 4.f) {
+  if (LJ && in4) {
     const float sr = sig * rinv, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
     t = t - kev * (6.f * sr6 - 12.f * sr12) * rinv;
     E += kev * (sr12 - sr6);
@@ -1336,25 +1351,25 @@ __global__ void __launch_bounds__(256) k_tail_gather_mx(DevModel M, DevState X, 
       const int x = u - base;
       if (u == t || (tg[x] == gt && abs(u - t) <= 2)) continue;  // bonded neighbours of one tail
       float e = 0.f;
-      A.force(pairf<true, false>(qt * tq[x], kap, 0.f, 0.f, sepf(pt, PF{th[x], tl[x]}), e));
+      A.force(pairf<true, false>(qt * tq[x], kap, 0.f, 0.f, pt, PF{th[x], tl[x]}, e));
       if (t < u) A.f[6] += e;
       A.tick();
     }
   }
   const float ql = (float)M.q_l, sTL = (float)M.sTL;
   for (int q = lane; q < M.n_dna; q += 32) {  // linker DNA (func.cpp:1898-1917); energy here
-    A.force(pairf<true, true>(qt * ql, kap, kex, sTL, sepf(pt, ldpf(S, M.dna_bead[q])), A.f[6]));
+    A.force(pairf<true, true>(qt * ql, kap, kex, sTL, pt, ldpf(S, M.dna_bead[q]), A.f[6]));
     A.tick();
   }
   if (M.t_fix[t] == 0) {  // LH beads and globular heads on free tail beads (energies on their side)
     for (int b = lane; b < M.n_LH; b += 32) {
       int p = M.lh_p[b];
-      A.force(pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], sepf(pt, ldpf(S, S.ol + b)), dummy));
+      A.force(pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], pt, ldpf(S, S.ol + b), dummy));
       A.tick();
     }
     for (Idx2 x(lane, 32, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {
       const int m = x.lo;
-      A.force(pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + x.s)), dummy));
+      A.force(pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], pt, ldpf(S, S.og + x.s), dummy));
       A.tick();
     }
   }
@@ -1445,20 +1460,20 @@ __global__ void __launch_bounds__(256) k_lh_gather_mx(DevModel M, DevState X, De
     const int pu = M.lh_p[u];
     const float sig = (P.hh[pb] + P.hh[pu]) * 0.5f;
     float e = 0.f;
-    const float3 d = sepf(pp, ldpf(S, S.ol + u));
+    const PF pu4 = ldpf(S, S.ol + u);
     if ((unsigned)(u - own0) < (unsigned)nlh) {  // same LH molecule
       int lo = bI < u ? bI : u, hi = bI < u ? u : bI;
       if (!(hi > lo + 1)) continue;
-      A.force(pairf<false, true>(0.f, kap, kex, sig, d, e));
+      A.force(pairf<false, true>(0.f, kap, kex, sig, pp, pu4, e));
     } else {
-      A.force(pairf<true, true>(qb * P.q[pu], kap, kex, sig, d, e));
+      A.force(pairf<true, true>(qb * P.q[pu], kap, kex, sig, pp, pu4, e));
     }
     if (bI < u) A.f[6] += e;
     A.tick();
   }
   const float ql = (float)M.q_l;
   for (int q = lane; q < M.n_dna; q += 32) {  // linker DNA; energy here
-    A.force(pairf<true, true>(qb * ql, kap, kex, P.hl[pb], sepf(pp, ldpf(S, M.dna_bead[q])), A.f[6]));
+    A.force(pairf<true, true>(qb * ql, kap, kex, P.hl[pb], pp, ldpf(S, M.dna_bead[q]), A.f[6]));
     A.tick();
   }
   for (int base = 0; base < M.n_tail; base += kTailTile) {  // tails; energy here
@@ -1472,7 +1487,7 @@ __global__ void __launch_bounds__(256) k_lh_gather_mx(DevModel M, DevState X, De
     const int te = min(M.n_tail, base + kTailTile);
     for (int t = base + lane; t < te; t += 32) {
       const int x = t - base;
-      A.force(pairf<true, true>(qb * tq[x], kap, kex, P.ht[pb], sepf(pp, PF{th[x], tl[x]}), A.f[6]));
+      A.force(pairf<true, true>(qb * tq[x], kap, kex, P.ht[pb], pp, PF{th[x], tl[x]}, A.f[6]));
       A.tick();
     }
   }
@@ -1480,7 +1495,7 @@ __global__ void __launch_bounds__(256) k_lh_gather_mx(DevModel M, DevState X, De
   for (Idx2 x(lane, 32, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {  // other LHs' globular heads; energy on the core
     const int K = x.hi, m = x.lo;
     if (K == own) continue;
-    A.force(pairf<true, true>(qb * P.q[m], kap, kex, (P.hh[m] + P.hh[pb]) * 0.5f, sepf(pp, ldpf(S, S.og + x.s)), dummy));
+    A.force(pairf<true, true>(qb * P.q[m], kap, kex, (P.hh[m] + P.hh[pb]) * 0.5f, pp, ldpf(S, S.og + x.s), dummy));
     A.tick();
   }
   A.finish();
@@ -1537,17 +1552,17 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
     }
     const float qlk = ke * ql, sTL = (float)M.sTL;
     for (int t = tid; t < M.n_tail; t += nt) {  // tails on this DNA bead; energy on the tail side
-      A.force(pairf<true, true>(qlk * M.t_qf[t], kap, kex, sTL, sepf(pj, ldpf(S, S.ot + t)), dummy));
+      A.force(pairf<true, true>(qlk * M.t_qf[t], kap, kex, sTL, pj, ldpf(S, S.ot + t), dummy));
       A.tick();
     }
     for (int b = tid; b < M.n_LH; b += nt) {  // LH beads; energy on the LH side
       int p = M.lh_p[b];
-      A.force(pairf<true, true>(qlk * P.q[p], kap, kex, P.hl[p], sepf(pj, ldpf(S, S.ol + b)), dummy));
+      A.force(pairf<true, true>(qlk * P.q[p], kap, kex, P.hl[p], pj, ldpf(S, S.ol + b), dummy));
       A.tick();
     }
     for (Idx2 x(tid, nt, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {  // globular heads; energy on the core side
       const int m = x.lo, s = x.s;
-      A.force(pairf<true, true>(qlk * P.q[m], kap, kex, P.hl[m], sepf(pj, ldpf(S, S.og + s)), dummy));
+      A.force(pairf<true, true>(qlk * P.q[m], kap, kex, P.hl[m], pj, ldpf(S, S.og + s), dummy));
       A.tick();
     }
   } else {
@@ -1559,7 +1574,7 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
         const int m = x.hi, l = x.lo;
         if (M.type[l] != 0) continue;
         const PF g = ldpf(S, S.og + lc * ng + m);
-        const float3 f1 = pairf<true, true>(ke * P.q[m] * ql, kap, kex, P.hl[m], sepf(g, ldpf(S, l)), A.f[6]);
+        const float3 f1 = pairf<true, true>(ke * P.q[m] * ql, kap, kex, P.hl[m], g, ldpf(S, l), A.f[6]);
         A.force(f1);
         A.torque(crossf(sepf(g, pj), f1));
         A.tick();
@@ -1567,7 +1582,7 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
       for (Idx2 x(tid, nt, M.n_tail); x.s < ng * M.n_tail; x.next()) {  // G-head vs tails (func.cpp:2403-2476)
         const int m = x.hi, t = x.lo;
         const PF g = ldpf(S, S.og + lc * ng + m);
-        const float3 f1 = pairf<true, true>(ke * P.q[m] * M.t_qf[t], kap, kex, P.ht[m], sepf(g, ldpf(S, S.ot + t)),
+        const float3 f1 = pairf<true, true>(ke * P.q[m] * M.t_qf[t], kap, kex, P.ht[m], g, ldpf(S, S.ot + t),
                                             A.f[6]);
         A.force(f1);
         A.torque(crossf(sepf(g, pj), f1));
@@ -1579,7 +1594,7 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
         int p2 = M.lh_p[b];
         const PF g = ldpf(S, S.og + lc * ng + m);
         const float3 f1 = pairf<true, true>(ke * P.q[m] * P.q[p2], kap, kex, (P.hh[m] + P.hh[p2]) * 0.5f,
-                                            sepf(g, ldpf(S, S.ol + b)), A.f[6]);
+                                            g, ldpf(S, S.ol + b), A.f[6]);
         A.force(f1);
         A.torque(crossf(sepf(g, pj), f1));
         A.tick();
@@ -1591,7 +1606,7 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
         const PF g = ldpf(S, S.og + lc * ng + m);
         float e = 0.f;
         const float3 f1 = pairf<true, true>(ke * P.q[m] * P.q[m1], kap, kex, (P.hh[m] + P.hh[m1]) * 0.5f,
-                                            sepf(g, ldpf(S, S.og + K * ng + m1)), e);
+                                            g, ldpf(S, S.og + K * ng + m1), e);
         if (lc < K) A.f[6] += e;
         A.force(f1);
         A.torque(crossf(sepf(g, pj), f1));
@@ -1642,14 +1657,14 @@ __global__ void __launch_bounds__(kGatherCoreThreads) k_chain_gather_mx(DevModel
       const float qt = ke * M.t_qf[t0];
       for (int b = tid; b < M.n_LH; b += nt) {
         int p = M.lh_p[b];
-        const float3 f2 = pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], sepf(pt, ldpf(S, S.ol + b)), dummy);
+        const float3 f2 = pairf<true, true>(qt * P.q[p], kap, kex, P.ht[p], pt, ldpf(S, S.ol + b), dummy);
         A.force(f2);
         A.torque(crossf(lever, f2));
         A.tick();
       }
       for (Idx2 x(tid, nt, M.n_lh_g); x.s < M.n_lhcore * M.n_lh_g; x.next()) {
         const int m = x.lo, s = x.s;
-        const float3 f2 = pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], sepf(pt, ldpf(S, S.og + s)), dummy);
+        const float3 f2 = pairf<true, true>(qt * P.q[m], kap, kex, P.ht[m], pt, ldpf(S, S.og + s), dummy);
         A.force(f2);
         A.torque(crossf(lever, f2));
         A.tick();

@@ -1078,9 +1078,13 @@ struct Job {
 
 // The launches of one factorisation: issued on st, or (plan != nullptr)
 // only recorded with their grid sizes, without the final diagonal scatter.
+// max_pass (1..3): most panels one bulk pass carries (K = 128 max_pass).
+// Fewer panels per pass mean fewer FP32 tensor-memory accumulation steps per
+// stored update and more read-modify-write passes: 3 is the fastest, 1 the
+// most accurate.
 static int potrf_mixed_impl(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
                             cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes,
-                            std::vector<std::pair<StepArgs, int>>* plan) {
+                            std::vector<std::pair<StepArgs, int>>* plan, int max_pass) {
   float2* A = reinterpret_cast<float2*>(A64);  // double-float storage, 8 bytes per element
   const int nt = cdiv(m, kT);
   const size_t buf = (size_t)nt * kTileBytes;
@@ -1166,12 +1170,12 @@ static int potrf_mixed_impl(int m, double* A64, int lda, unsigned char* PS, int*
   launch(0, none, none, false);  // panel 0 alone
   int k = 0;
   while (k + 1 < nt) {
-    if (nt - (k + 4) >= BD_TRIPLE_MIN) {
+    if (max_pass >= 3 && nt - (k + 4) >= BD_TRIPLE_MIN) {
       launch(k + 1, col_job(k, k + 2), none, true);
       launch(k + 2, col_job(k, k + 3, 2), none, true);
       launch(k + 3, tri_job(k, 3, k + 4), none, true);
       k += 3;
-    } else if (nt - (k + 3) >= BD_PAIR_MIN) {
+    } else if (max_pass >= 2 && nt - (k + 3) >= BD_PAIR_MIN) {
       launch(k + 1, col_job(k, k + 2), none, true);
       launch(k + 2, tri_job(k, 2, k + 3), none, true);
       k += 2;
@@ -1188,8 +1192,8 @@ static int potrf_mixed_impl(int m, double* A64, int lda, unsigned char* PS, int*
 }
 
 int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int* err, cudaStream_t st,
-                cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes) {
-  return potrf_mixed_impl(m, A64, lda, PS, negpiv, err, st, kev, kev_pairs, kflop, kbytes, nullptr);
+                cudaEvent_t* kev, int* kev_pairs, double* kflop, double* kbytes, int max_pass) {
+  return potrf_mixed_impl(m, A64, lda, PS, negpiv, err, st, kev, kev_pairs, kflop, kbytes, nullptr, max_pass);
 }
 
 // Factorisations of a batch advanced together: launch i of the batch runs
@@ -1206,7 +1210,7 @@ struct MixedBatch {
 };
 
 MixedBatch* mixed_batch_create(int nrep, const int* m, double* const* A, const int* lda, unsigned char* const* PS,
-                               int* const* negpiv, int* const* err) {
+                               int* const* negpiv, int* const* err, int max_pass) {
   std::vector<std::vector<std::pair<StepArgs, int>>> plans(nrep);
   size_t steps = 0;
   MixedBatch* b = new MixedBatch();
@@ -1214,7 +1218,7 @@ MixedBatch* mixed_batch_create(int nrep, const int* m, double* const* A, const i
   std::vector<ScatterArgs> sc(nrep);
   for (int r = 0; r < nrep; r++) {
     potrf_mixed_impl(m[r], A[r], lda[r], PS[r], negpiv[r], err[r], nullptr, nullptr, nullptr, nullptr, nullptr,
-                     &plans[r]);
+                     &plans[r], max_pass);
     steps = std::max(steps, plans[r].size());
     const int nt = cdiv(m[r], kT);
     b->max_nt = std::max(b->max_nt, nt);

@@ -304,6 +304,16 @@ int bd_batch_phase_times(bd_batch* b, float* out3);
 /* Kernel launches of the last batch step enqueued (a graph replays the same
  * launches).  No counterpart in the reference. */
 int bd_batch_launch_count(const bd_batch* b, int* out);
+/* Accuracy/speed setting of the mixed factorisation: at most `passes` (1, 2
+ * or 3; default 3) panels per trailing read-modify-write pass.  Each pass
+ * accumulates its panels' products in FP32 tensor memory before adding them
+ * to the double-float tensor, so fewer panels per pass give a more accurate
+ * factor at more HBM traffic (measured at 3N = 11,700: 3 -> 6.9 ms, noise
+ * displacement 7.8e-7 from FP64; 2 -> 7.3 ms, 6.3e-7; 1 -> 9.4 ms, 5.4e-7).
+ * The next step captures its graph again.  No counterpart in the reference
+ * (its factorisation is FP64 cuSOLVER). */
+int bd_set_mixed_passes(bd_ctx* ctx, int passes);
+int bd_batch_set_mixed_passes(bd_batch* b, int passes);
 /* One step of every replica: rr[i], p[i] are replica i's host noise (as for
  * bd_step); energies[i] (optional) receives its energy. */
 int bd_batch_step(bd_batch* b, const double* const* rr, const double* const* p, double* energies);

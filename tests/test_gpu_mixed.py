@@ -74,3 +74,38 @@ def test_mixed_graph_matches_eager(case):
     rr, p = z["noise0_rr"], z["noise0_p"]
     assert a.step(rr, p) == b.step(rr, p)
     assert np.array_equal(a.get("r"), b.get("r")) and np.array_equal(a.get("r_t"), b.get("r_t"))
+
+
+def test_mixed_passes_setting():
+    """bd_set_mixed_passes: at most one panel per trailing pass makes the
+    factor more accurate on the config-2 replica where the default schedule
+    is least accurate (3N = 7,977, 50 mM; noise displacement 1.07e-6 from the
+    FP64 one with three panels per pass, 4.2e-7 with one), and a graph-captured
+    context picks the new schedule up at its next step (bitwise equal to an
+    eager context switched the same way)."""
+    import tempfile
+    from brownian_dynamics_cuda_gb300 import BDError, PREC_FP64, PREC_MIXED, Context, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import config, make_fiber
+    fib = make_fiber(config(2, seed=1, replica=132), tempfile.mkdtemp())
+    p = np.random.default_rng(3).normal(size=fib.m)
+    rd64 = Context(fib, precision=PREC_FP64).noise_displacement(p)
+    errs = {}
+    for passes in (3, 1):
+        c = Context(fib, precision=PREC_MIXED)
+        c.set_mixed_passes(passes)
+        errs[passes] = rel_err(c.noise_displacement(p), rd64)
+        c.close()
+    assert errs[1] <= 6e-7 and errs[1] < errs[3], errs
+    g = Noise(9)
+    n0 = g.step(0, fib.arrays["r_var"], fib.m)
+    n1 = g.step(1, fib.arrays["r_var"], fib.m)
+    a, b = Context(fib, precision=PREC_MIXED, use_graph=True), Context(fib, precision=PREC_MIXED)
+    a.step(*n0)
+    b.step(*n0)
+    a.set_mixed_passes(1)
+    b.set_mixed_passes(1)
+    assert a.step(*n1) == b.step(*n1)
+    for k in ("r", "r_t", "a"):
+        assert np.array_equal(a.get(k), b.get(k)), k
+    with pytest.raises(BDError):
+        a.set_mixed_passes(4)
