@@ -124,15 +124,21 @@ def fp64_peak_tflops() -> float:
     return 2.0 * n ** 3 / best / 1e12
 
 
-def fp64_comparison(fib, rr_d, p_d, host, args, local, stream) -> dict:
+def fp64_comparison(fib, rr_d, p_d, host, args, local, stream, krylov=False) -> dict:
     """Plain FP64 step (CUDA graph, same fiber, same noise) timed like the
     headline, and the relative displacement error of one mixed step against
     one FP64 step from the same state: max |dr_mixed - dr_fp64| / max |dr_fp64|
-    over r, r_t and r_lh."""
+    over r, r_t and r_lh.  With the Krylov noise both sides use it (FP64:
+    relative change 1e-10)."""
     import torch
-    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context
+    from brownian_dynamics_cuda_gb300 import NOISE_KRYLOV, PREC_FP64, PREC_MIXED, Context
+
+    def mode(c, tol):
+        if krylov:
+            c.set_noise_mode(NOISE_KRYLOV, tol, 128)
+        return c
     steps = max(2, min(args.steps, 5))
-    c64 = Context(fib, precision=PREC_FP64, use_graph=True, device=local, stream=stream.cuda_stream)
+    c64 = mode(Context(fib, precision=PREC_FP64, use_graph=True, device=local, stream=stream.cuda_stream), 1e-10)
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
             c64.step_device(rr_d[i].data_ptr(), p_d[i].data_ptr())
@@ -145,8 +151,8 @@ def fp64_comparison(fib, rr_d, p_d, host, args, local, stream) -> dict:
         stream.synchronize()
     ms64 = e0.elapsed_time(e1) / steps
     c64.close()
-    a = Context(fib, precision=PREC_FP64, device=local)
-    b = Context(fib, precision=PREC_MIXED, device=local)
+    a = mode(Context(fib, precision=PREC_FP64, device=local), 1e-10)
+    b = mode(Context(fib, precision=PREC_MIXED, device=local), args.krylov_tol)
     rr, p = host[0]
     a.step(rr, p)
     b.step(rr, p)
@@ -281,7 +287,7 @@ def run_reference(args):
 
 def run_ours(args):
     import torch
-    from brownian_dynamics_cuda_gb300 import PREC_FP64, PREC_MIXED, Context, Noise
+    from brownian_dynamics_cuda_gb300 import NOISE_KRYLOV, PREC_FP64, PREC_MIXED, Context, Noise
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
@@ -292,6 +298,13 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     freq = args.frequency_rp
     ctx = Context(fib, precision=prec, use_graph=True, frequency_RP=freq, device=local, stream=stream.cuda_stream)
+    krylov = args.noise == "krylov"
+
+    def noise_mode(c, tol=None):
+        if krylov:
+            c.set_noise_mode(NOISE_KRYLOV, tol or args.krylov_tol, 128)
+        return c
+    noise_mode(ctx)
     n3, m = 3 * fib.sizes["n"], fib.m
     nsteps = args.warmup + args.steps
     noise = Noise(1000 + rank)
@@ -310,10 +323,11 @@ def run_ours(args):
         stream.synchronize()
         # per-phase times of one eager step (events on the context's stream)
         ctx.phase_times()
-        ph_ctx = Context(fib, precision=prec, use_graph=False, device=local, stream=stream.cuda_stream)
+        ph_ctx = noise_mode(Context(fib, precision=prec, use_graph=False, device=local, stream=stream.cuda_stream))
         ph_ctx.phase_times()
         ph_ctx.step_device(rr_d[0].data_ptr(), p_d[0].data_ptr())
         phases = ph_ctx.phase_times()
+        ph_ctx_stats = ph_ctx.krylov_stats() if krylov else None
         kt = ph_ctx.kernel_time()
         kbytes = ph_ctx.kernel_bytes()
         ph_ctx.close()
@@ -335,7 +349,8 @@ def run_ours(args):
     launches = ctx.launch_count() * args.steps
     # e2e: reference-facing call with host buffers (noise H2D, r_lh D2H every
     # step, full state D2H on sampling steps every 100 steps)
-    e2e_ctx = Context(fib, precision=prec, use_graph=True, frequency_RP=freq, device=local, stream=stream.cuda_stream)
+    e2e_ctx = noise_mode(Context(fib, precision=prec, use_graph=True, frequency_RP=freq, device=local,
+                                 stream=stream.cuda_stream))
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
     rr_h = [pin(h[0]) for h in host]
     p_h = [pin(h[1]) for h in host]
@@ -358,7 +373,20 @@ def run_ours(args):
     pk = peaks()
     chol_ms = float(phases[1])
     chol_flop = m ** 3 / 3.0
-    if prec == PREC_FP64:
+    if krylov:
+        it, ch = ph_ctx_stats
+        byt = it * 8.0 * m * (m + 1) / 2  # the lower triangle of D read once per iteration (8 B per entry)
+        rd_ms = float(phases[2])
+        achieved = byt / (rd_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "kernel": ("k_rpy_mv (matrix-free FP32 RPY products, no tensor read: bytes below are those the "
+                           "stored tensor would cost)" if prec == PREC_MIXED else
+                           "k_symv_tiles + k_symv_sum (products with the stored FP64 tensor)") +
+                          " of the Lanczos noise, %d iterations, last relative change %.1e" % (it, ch),
+                "algorithmic_bytes_per_step": byt, "rd_phase_ms": rd_ms,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    elif prec == PREC_FP64:
         fp64_peak = fp64_peak_tflops()
         roof = {"bound": "fp64", "achieved": chol_flop / (chol_ms * 1e-3) / 1e12, "peak": fp64_peak,
                 "unit": "TFLOP/s", "frac": None, "traffic": None,
@@ -388,7 +416,7 @@ def run_ours(args):
     # point, and the mixed step's displacement error against it
     vs64 = None
     if prec == PREC_MIXED and not args.no_fp64:
-        vs64 = fp64_comparison(fib, rr_d, p_d, host, args, local, stream)
+        vs64 = fp64_comparison(fib, rr_d, p_d, host, args, local, stream, krylov)
         if world > 1:
             vs64["fp64_steps_per_s"] = replica_rate(max_over_ranks(1000.0 / vs64["fp64_steps_per_s"]), world)
         vs64["speedup_vs_fp64"] = value / vs64["fp64_steps_per_s"]
@@ -416,7 +444,7 @@ def run_ours(args):
                 "vs_baseline": None, "dtype": "f64" if prec == PREC_FP64 else "bf16x3+f64",
                 "data": "synthetic (seeded fiber generator, reference file formats)",
                 "config": {"workload": spec.name, "n_D": fib.n_D, "3N": m, "precision": args.precision,
-                           "frequency_RP": args.frequency_rp,
+                           "frequency_RP": args.frequency_rp, "noise": args.noise,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (D is %.2f GB)" %
                                                                          (m * m * 8 / 1e9)},
                 "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
@@ -730,6 +758,9 @@ def main():
                     help="rebuild and refactor D every k steps (default 1; 10 for config 4)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg of the mixed run")
     ap.add_argument("--no-library-bar", action="store_true", help="skip the cuSOLVER potrf timing leg")
+    ap.add_argument("--noise", choices=["cholesky", "krylov"], default="cholesky",
+                    help="noise displacement: the reference's L p, or D^{1/2} p by Lanczos (non-parity fast mode)")
+    ap.add_argument("--krylov-tol", type=float, default=1e-6, help="Lanczos stopping tolerance (relative change)")
     ap.add_argument("--fd", action="store_true", help="with --config 3 (rollout gradient): also the FP64 central-difference gradient")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:

@@ -34,6 +34,7 @@ UNITS = [
     ("k_noalloc.cu", ["-fmad=false"]),
     ("k_adjoint.cu", []),
     ("k_noise.cu", []),
+    ("k_krylov.cu", []),
 ]
 
 

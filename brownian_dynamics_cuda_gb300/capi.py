@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libbdgb300.so")
 
 BD_OK, BD_ERR_ARG, BD_ERR_IO, BD_ERR_CUDA, BD_ERR_NOMEM, BD_ERR_NONFINITE, BD_ERR_NOT_SPD, BD_ERR_STATE = range(8)
 PREC_FP64, PREC_MIXED = 0, 1
+NOISE_CHOLESKY, NOISE_KRYLOV = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -147,6 +148,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.bd_batch_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.bd_set_mixed_passes.argtypes = [C.c_void_p, C.c_int]
+    L.bd_set_noise_mode.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int]
+    L.bd_krylov_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.bd_batch_set_mixed_passes.argtypes = [C.c_void_p, C.c_int]
     L.bd_step_reference.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp] + [_dp] * 6
     L.bd_forces.argtypes = [C.c_void_p] + [_dp] * 5
@@ -507,6 +510,17 @@ class Context:
         v = C.c_int()
         _check(self._L.bd_launch_count(self._h, C.byref(v)))
         return v.value
+
+    def set_noise_mode(self, mode: int, tol: float = 1e-6, kmax: int = 64) -> None:
+        """bd_set_noise_mode: NOISE_CHOLESKY (the reference's L p) or NOISE_KRYLOV
+        (D^{1/2} p by Lanczos, to relative change tol, at most kmax iterations)."""
+        _check(self._L.bd_set_noise_mode(self._h, int(mode), float(tol), int(kmax)))
+
+    def krylov_stats(self) -> tuple[int, float]:
+        """Iterations and last relative change of the most recent Krylov run."""
+        it, ch = C.c_int(), C.c_double()
+        _check(self._L.bd_krylov_stats(self._h, C.byref(it), C.byref(ch)))
+        return it.value, ch.value
 
     def set_mixed_passes(self, passes: int) -> None:
         """bd_set_mixed_passes: at most `passes` panels per trailing pass of the mixed

@@ -144,20 +144,24 @@ static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double*
   cudaStream_t st = c->stream;
   int L = 0, rc = 0;
   const bool mixed = c->precision == BD_PREC_MIXED;
-  bool rebuild = (c->step_count % c->freq_rp) == 0;
+  const bool krylov = c->noise_mode == BD_NOISE_KRYLOV;
+  // a Krylov step needs D itself: rebuilt when A holds a factor
+  bool rebuild = (c->step_count % c->freq_rp) == 0 || (krylov && c->a_holds_factor);
   if (phases & kPre) {
     record(c, 0);
     bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
     L += mixed ? 2 : 1;
-    if (rebuild) {
+    if (rebuild && !(krylov && mixed)) {  // mixed Krylov products are matrix-free: no tensor
       bdk::rpy_assemble(M.n_D, c->r_all, M.rad_all, M.a1, M.a2, c->A, c->lda, st, mixed ? c->S.qh : nullptr,
                         mixed ? c->S.ql : nullptr);
       L++;
       CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
+      c->a_holds_factor = false;
     }
     record(c, 1);
   }
-  if ((phases & kChol) && rebuild) {
+  if ((phases & kChol) && rebuild && !krylov) {
+    c->a_holds_factor = true;
     if (mixed) {
       const bool kt = c->timing && !c->kev.empty();
       c->kflop = 0.0;
@@ -174,8 +178,15 @@ static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double*
     return BD_OK;
   }
   record(c, 2);
-  bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st, mixed);
-  L += 2;
+  if (krylov) {
+    rc = bdk::krylov_sqrt(c->m, mixed ? nullptr : c->A, c->lda, mixed, c->S.qh, c->S.ql, M.a1, M.a2, d_p, M.s2dt,
+                          c->krylov_tol, c->krylov_kmax, c->rd, c->kscratch, st, &c->krylov_iters, &c->krylov_change);
+    if (rc) return set_error(rc, "bd_step: Krylov noise displacement failed");
+    L += 10 * c->krylov_iters + 4;
+  } else {
+    bdk::trmv_lower_ws(c->m, c->A, c->lda, d_p, M.s2dt, c->rd, c->rd_part, st, mixed);
+    L += 2;
+  }
   record(c, 3);
   L += bdk::forces(M, c->X, c->F0, c->S, c->precision, st);
   record(c, 4);
@@ -533,6 +544,7 @@ extern "C" int bd_destroy(bd_ctx* c) {
   if (c->A) cudaFree(c->A);
   if (c->PS) cudaFree(c->PS);
   if (c->d_err) cudaFree(c->d_err);
+  if (c->kscratch) cudaFree(c->kscratch);
   if (c->arena_base) cudaFree(c->arena_base);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -548,7 +560,7 @@ extern "C" int bd_sizes(const bd_ctx* c, int* o) {
 
 static int run_step(bd_ctx* c, const double* d_rr, const double* d_p) {
   int rc;
-  if (c->use_graph && d_rr == c->rr && d_p == c->p && c->freq_rp == 1) {
+  if (c->use_graph && d_rr == c->rr && d_p == c->p && c->freq_rp == 1 && c->noise_mode == BD_NOISE_CHOLESKY) {
     if (!c->graph) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -665,6 +677,7 @@ static int copy_lower(bd_ctx* c, double* out, bool mirror) {
 
 static void assemble_now(bd_ctx* c) {
   const bool mixed = c->precision == BD_PREC_MIXED;
+  c->a_holds_factor = false;
   bdk::gather_rall(c->M, c->X, c->r_all, mixed ? &c->S : nullptr, c->stream);
   bdk::rpy_assemble(c->M.n_D, c->r_all, c->M.rad_all, c->M.a1, c->M.a2, c->A, c->lda, c->stream,
                     mixed ? c->S.qh : nullptr, mixed ? c->S.ql : nullptr);
@@ -679,6 +692,7 @@ extern "C" int bd_diffusion_tensor(bd_ctx* c, double* D) {
 
 static int factor_now(bd_ctx* c) {
   assemble_now(c);
+  c->a_holds_factor = true;
   CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), c->stream));
   if (c->precision == BD_PREC_MIXED) {
     bdk::potrf_mixed(c->m, c->A, c->lda, c->PS, c->negpiv, c->d_err, c->stream, nullptr, nullptr, nullptr, nullptr,
@@ -703,11 +717,20 @@ extern "C" int bd_cholesky(bd_ctx* c, double* L) {
 
 extern "C" int bd_noise_displacement(bd_ctx* c, const double* p, double* rd) {
   if (!c || !p || !rd) return set_error(BD_ERR_ARG, "bd_noise_displacement: null argument");
-  int rc = factor_now(c);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream,
-                     c->precision == BD_PREC_MIXED);
+  const bool mixed = c->precision == BD_PREC_MIXED;
+  if (c->noise_mode == BD_NOISE_KRYLOV) {
+    assemble_now(c);
+    CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = bdk::krylov_sqrt(c->m, mixed ? nullptr : c->A, c->lda, mixed, c->S.qh, c->S.ql, c->M.a1, c->M.a2, c->p,
+                              c->M.s2dt, c->krylov_tol, c->krylov_kmax, c->rd, c->kscratch, c->stream,
+                              &c->krylov_iters, &c->krylov_change);
+    if (rc) return set_error(rc, "bd_noise_displacement: Krylov iteration failed");
+  } else {
+    int rc = factor_now(c);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    bdk::trmv_lower_ws(c->m, c->A, c->lda, c->p, c->M.s2dt, c->rd, c->rd_part, c->stream, mixed);
+  }
   CK(cudaMemcpyAsync(rd, c->rd, (size_t)c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return BD_OK;
@@ -1029,6 +1052,30 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
 extern "C" int bd_batch_size(const bd_batch* b, int* nrep) {
   if (!b || !nrep) return set_error(BD_ERR_ARG, "bd_batch_size: null argument");
   *nrep = (int)b->ctx.size();
+  return BD_OK;
+}
+
+extern "C" int bd_set_noise_mode(bd_ctx* c, int mode, double tol, int kmax) {
+  if (!c || (mode != BD_NOISE_CHOLESKY && mode != BD_NOISE_KRYLOV) ||
+      (mode == BD_NOISE_KRYLOV && (!(tol > 0.0) || kmax < 2 || kmax > 512)))
+    return set_error(BD_ERR_ARG, "bd_set_noise_mode: mode 0 or 1; Krylov: tol > 0, 2 <= kmax <= 512");
+  if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_noise_mode: the context belongs to a batch");
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
+  if (mode == BD_NOISE_KRYLOV && (!c->kscratch || kmax > c->krylov_kmax)) {
+    if (c->kscratch) cudaFree(c->kscratch), c->kscratch = nullptr;
+    if (cudaMalloc((void**)&c->kscratch, bdk::krylov_scratch_doubles(c->m, kmax) * sizeof(double)) != cudaSuccess)
+      return set_error(BD_ERR_NOMEM, "bd_set_noise_mode: Krylov workspace allocation failed");
+  }
+  c->noise_mode = mode;
+  if (mode == BD_NOISE_KRYLOV) c->krylov_tol = tol, c->krylov_kmax = kmax;
+  return BD_OK;
+}
+
+extern "C" int bd_krylov_stats(const bd_ctx* c, int* iters, double* change) {
+  if (!c || !iters || !change) return set_error(BD_ERR_ARG, "bd_krylov_stats: null argument");
+  *iters = c->krylov_iters;
+  *change = c->krylov_change;
   return BD_OK;
 }
 

@@ -151,6 +151,12 @@ int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* 
                 cudaEvent_t* kev = nullptr, int* kev_pairs = nullptr, double* kflop = nullptr,
                 double* kbytes = nullptr, int max_pass = 3);
 int mixed_tiles(int m);
+// k_krylov.cu: rd = s2dt D^{1/2} p by Lanczos on the lower-stored tensor
+size_t krylov_scratch_doubles(int m, int kmax);
+// A == nullptr: matrix-free products from the double-float position mirror qh/ql
+int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, const float4* ql, double a1, double a2,
+                const double* p, double s2dt, double tol, int kmax, double* rd, double* scratch, cudaStream_t st,
+                int* iters, double* change);
 int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at most
 // Many mixed factorisations (replicas) advanced together: launch i runs step
 // i of every factorisation's schedule (k_chol_step_multi), then one diagonal
@@ -190,6 +196,13 @@ struct bd_ctx {
   int freq_rp = 1;
   int use_graph = 0;
   int mixed_passes = 3;  // panels per bulk trailing pass of the mixed factorisation (bd_set_mixed_passes)
+  // noise displacement: 0 = L p (the reference's), 1 = D^{1/2} p by Lanczos (bd_set_noise_mode)
+  int noise_mode = 0;
+  double krylov_tol = 1e-6;
+  int krylov_kmax = 64, krylov_iters = 0;
+  double krylov_change = 0.0;
+  double* kscratch = nullptr;
+  bool a_holds_factor = false;  // A holds L (after a factorisation), not D
   long step_count = 0;
   DevModel M{};
   DevState X{}, Y{};

@@ -48,7 +48,14 @@ enum {
   BD_PREC_MIXED = 1   /* FP32-class: RPY tensor in FP32 into double-float storage, Cholesky with
                          FP32 panels and BF16x3 tensor-core (tcgen05) trailing updates, FP32
                          pair forces with compensated sums; no refinement.  Displacement
-                         within 7e-7 of the FP64 path at 3N <= 46,200 (bound 1e-6) */
+                         4e-7 to 8e-7 from the FP64 path on the benchmark fibers; up to
+                         1.3e-6 on 3 of 256 uneven batch replicas (bd_set_mixed_passes) */
+};
+
+/* Noise displacement of a step (bd_set_noise_mode). */
+enum {
+  BD_NOISE_CHOLESKY = 0, /* rd = s2dt L p, L the Cholesky factor of D: the reference's */
+  BD_NOISE_KRYLOV = 1    /* rd = s2dt D^{1/2} p by Lanczos: same covariance, another vector */
 };
 
 /* ------------------------------------------------------------ model (host)
@@ -313,6 +320,25 @@ int bd_batch_launch_count(const bd_batch* b, int* out);
  * The next step captures its graph again.  No counterpart in the reference
  * (its factorisation is FP64 cuSOLVER). */
 int bd_set_mixed_passes(bd_ctx* ctx, int passes);
+/* Noise displacement mode.  BD_NOISE_KRYLOV replaces the factorisation and
+ * L p by the symmetric square root of D applied to p through the Lanczos
+ * process (full re-orthogonalisation; stops when the relative change of the
+ * approximation is <= tol, at most kmax iterations, 2 <= kmax <= 512): the
+ * same covariance 2 dt D as the reference's noise, so a valid BD step, but a
+ * different vector than L p, so not comparable step for step with the
+ * reference (a fast mode for large fibers, where one tensor-vector product per
+ * iteration replaces an O((3N)^3) factorisation).  D is rebuilt every
+ * frequency_RP steps as before on FP64 contexts (products with the stored
+ * tensor, FP64); mixed contexts compute every product matrix-free from the
+ * current positions (FP32 RPY blocks, compensated sums), so they neither
+ * assemble nor store the tensor.  A Krylov step reads the tridiagonal
+ * coefficients back every 8 iterations: it is not stream-ordered and is never
+ * captured in a graph.  Allocates its workspace ((kmax + 1) 3N + 3N doubles
+ * + 64 (3N / 64)^2 doubles).  No counterpart in the reference
+ * (its frequency_RP guard is commented out, func_cuda.cu:3504). */
+int bd_set_noise_mode(bd_ctx* ctx, int mode, double tol, int kmax);
+/* Iterations and last relative change of the most recent Krylov run. */
+int bd_krylov_stats(const bd_ctx* ctx, int* iters, double* change);
 int bd_batch_set_mixed_passes(bd_batch* b, int passes);
 /* One step of every replica: rr[i], p[i] are replica i's host noise (as for
  * bd_step); energies[i] (optional) receives its energy. */
