@@ -146,7 +146,7 @@ static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double*
   const bool mixed = c->precision == BD_PREC_MIXED;
   const bool krylov = c->noise_mode == BD_NOISE_KRYLOV;
   // a Krylov step needs D itself: rebuilt when A holds a factor
-  bool rebuild = (c->step_count % c->freq_rp) == 0 || (krylov && c->a_holds_factor);
+  bool rebuild = (c->step_count % c->freq_rp) == 0 || (krylov && c->a_holds_factor) || c->need_rebuild;
   if (phases & kPre) {
     record(c, 0);
     bdk::gather_rall(M, c->X, c->r_all, mixed ? &c->S : nullptr, st);
@@ -157,6 +157,7 @@ static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double*
       L++;
       CK(cudaMemsetAsync(c->negpiv, 0, sizeof(int), st));
       c->a_holds_factor = false;
+      c->need_rebuild = false;
     }
     record(c, 1);
   }
@@ -344,53 +345,60 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   for (int i = 0; i < n; i++) rad_all[i] = m->rad[i];
   for (int i = 0; i < nt; i++) rad_all[n + i] = m->t_rad[i];
   for (int i = 0; i < nL; i++) rad_all[n + nt + i] = m->lh_rad[i];
-  // sizes
+  // sizes.  Every buffer that depends on the linker-histone binding is sized
+  // for every core bound (capacity), so that bd_set_lh_flags resizes the
+  // context in place; the logical sizes (M.n_LH, M.n_D, c->m) follow the flags.
   c->m = 3 * M.n_D;
-  c->lda = (c->m + 31) & ~31;
+  const int nL_cap = M.nlh * nc, nD_cap = n + nt + nL_cap, m_cap = 3 * nD_cap;
+  c->m_cap = m_cap;
+  c->lda = (m_cap + 31) & ~31;
   const size_t ndna = M.n_dna, nlhc = M.n_lhcore;
+  const size_t nlhc_cap = (M.nlh > 0 || M.n_lh_g > 0) ? (size_t)nc : nlhc;
   size_t ebuf = (size_t)8 * n + nt + nL;
+  const size_t ebuf_cap = (size_t)8 * n + nt + nL_cap;
   size_t tot = 0;
   auto addD = [&](size_t k) { tot += slab<double>(k); };
   auto addI = [&](size_t k) { tot += slab<int>(k); };
   // model
-  addI(n); addI(n); addI(nc); addI(ndna); addI(nlhc); addI(nc); addD(n); addD(M.n_D); addD(3 * M.Nq); addD(M.Nq);
+  addI(n); addI(n); addI(nc); addI(ndna); addI(nlhc_cap); addI(nc); addD(n); addD(nD_cap); addD(3 * M.Nq); addD(M.Nq);
   addD(3 * M.n_t); addI(M.n_t); addI(nc); for (int q = 0; q < 5; q++) addD(nt); addI(nt + 2); addI(nt); addI(nt);
   addD(3 * M.n_lh_g); addI(np); addI(nc); for (int q = 0; q < 9; q++) addD(np);
   // two states
   for (int q = 0; q < 2; q++) {
     for (int k = 0; k < 4; k++) addD(3 * n);
-    addD(3 * nt); addD(3 * nL);
+    addD(3 * nt); addD(3 * (size_t)nL_cap);
     for (int k = 0; k < 4; k++) addD(n);
     for (int k = 0; k < 3; k++) addD(3 * nc);
     for (int k = 0; k < 3; k++) addD(nc);
-    addD(nt); addD(nL); addD(3 * nlhc * M.n_lh_g);
+    addD(nt); addD(nL_cap); addD(3 * nlhc_cap * M.n_lh_g);
   }
-  for (int q = 0; q < 3; q++) { addD(3 * n); addD(3 * n); addD(3 * nt); addD(3 * nL); addD(1); }
-  addD((size_t)nc * nc * 10); addD(ndna * nc * 7); addD(nlhc * nc * 10); addD(ebuf);
-  addD(3 * (size_t)M.n_D); addD(c->m); addD(c->m); addD(3 * n); addD(bdk::trmv_scratch_doubles(c->m)); addD(1); addI(1);
-  const int npos = n + nt + nL + nlhc * M.n_lh_g;
-  addD((nt + 4 * (size_t)M.Nq + 1) / 2); addD(2 * (size_t)npos); addD(2 * (size_t)npos);
-  for (int q = 0; q < 3; q++) addD(2 * (size_t)M.n_D);
-  addD(4 * ((size_t)nt + nL));
-  addI(nL);
+  for (int q = 0; q < 3; q++) { addD(3 * n); addD(3 * n); addD(3 * nt); addD(3 * (size_t)nL_cap); addD(1); }
+  addD((size_t)nc * nc * 10); addD(ndna * nc * 7); addD(nlhc_cap * nc * 10); addD(ebuf_cap);
+  addD(3 * (size_t)nD_cap); addD(m_cap); addD(m_cap); addD(3 * n); addD(bdk::trmv_scratch_doubles(m_cap)); addD(1); addI(1);
+  const int npos = n + nt + nL + (int)nlhc * M.n_lh_g;
+  const int npos_cap = n + nt + nL_cap + (int)nlhc_cap * M.n_lh_g;
+  addD((nt + 4 * (size_t)M.Nq + 1) / 2); addD(2 * (size_t)npos_cap); addD(2 * (size_t)npos_cap);
+  for (int q = 0; q < 3; q++) addD(2 * (size_t)nD_cap);
+  addD(4 * ((size_t)nt + nL_cap));
+  addI(nL_cap);
   addD(37 * (size_t)n);
   e = cudaMalloc(&c->arena_base, tot);
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: device arena allocation failed"));
   if (c->precision != BD_PREC_MIXED && c->precision != BD_PREC_FP64)
     return fail(set_error(BD_ERR_ARG, "bd_create: unknown precision"));
-  e = cudaMalloc((void**)&c->A, (size_t)c->m * c->lda * sizeof(double));
+  e = cudaMalloc((void**)&c->A, (size_t)m_cap * c->lda * sizeof(double));
   if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
   if (c->precision == BD_PREC_MIXED) {
     if (bdk::set_mixed_attributes()) return fail(set_error(BD_ERR_CUDA, "bd_create: kernel attributes (shared memory)"));
-    e = cudaMalloc((void**)&c->PS, bdk::mixed_panel_bytes(c->m));
+    e = cudaMalloc((void**)&c->PS, bdk::mixed_panel_bytes(m_cap));
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
     if (e != cudaSuccess) return fail(set_error(BD_ERR_NOMEM, "bd_create: tensor allocation failed"));
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(BD_ERR_CUDA, "bd_create: memset failed"));
   }
   Arena ar{(char*)c->arena_base, tot, 0};
   int *d_type = ar.take<int>(n), *d_core_rank = ar.take<int>(n), *d_core_bead = ar.take<int>(nc),
-      *d_dna_bead = ar.take<int>(ndna), *d_lhcb = ar.take<int>(nlhc), *d_core_lh = ar.take<int>(nc);
-  double *d_phi = ar.take<double>(n), *d_rad_all = ar.take<double>(M.n_D), *d_cpos = ar.take<double>(3 * M.Nq),
+      *d_dna_bead = ar.take<int>(ndna), *d_lhcb = ar.take<int>(nlhc_cap), *d_core_lh = ar.take<int>(nc);
+  double *d_phi = ar.take<double>(n), *d_rad_all = ar.take<double>(nD_cap), *d_cpos = ar.take<double>(3 * M.Nq),
          *d_cq = ar.take<double>(M.Nq), *d_tpos = ar.take<double>(3 * M.n_t);
   int *d_tfix_tmpl = ar.take<int>(M.n_t), *d_nct = ar.take<int>(nc);
   double *d_ht = ar.take<double>(nt), *d_gt = ar.take<double>(nt), *d_lot = ar.take<double>(nt),
@@ -404,36 +412,37 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   for (int q = 0; q < 2; q++) {
     DevState& D = *sts[q];
     D.r = ar.take<double>(3 * n); D.a = ar.take<double>(3 * n); D.b = ar.take<double>(3 * n); D.c = ar.take<double>(3 * n);
-    D.r_t = ar.take<double>(3 * nt); D.r_lh = ar.take<double>(3 * nL);
+    D.r_t = ar.take<double>(3 * nt); D.r_lh = ar.take<double>(3 * (size_t)nL_cap);
     D.alpha = ar.take<double>(n); D.beta = ar.take<double>(n); D.gamma = ar.take<double>(n); D.length = ar.take<double>(n);
     D.a_dna = ar.take<double>(3 * nc); D.b_dna = ar.take<double>(3 * nc); D.c_dna = ar.take<double>(3 * nc);
     D.alpha_p = ar.take<double>(nc); D.beta_p = ar.take<double>(nc); D.gamma_p = ar.take<double>(nc);
-    D.beta_t = ar.take<double>(nt); D.beta_lh = ar.take<double>(nL); D.gpos = ar.take<double>(3 * nlhc * M.n_lh_g);
+    D.beta_t = ar.take<double>(nt); D.beta_lh = ar.take<double>(nL_cap);
+    D.gpos = ar.take<double>(3 * nlhc_cap * M.n_lh_g);
   }
   DevForces* fs[3] = {&c->F0, &c->F1, &c->Fa};
   for (int q = 0; q < 3; q++) {
     fs[q]->F = ar.take<double>(3 * n); fs[q]->T = ar.take<double>(3 * n); fs[q]->tF = ar.take<double>(3 * nt);
-    fs[q]->lF = ar.take<double>(3 * nL); fs[q]->E = ar.take<double>(1);
+    fs[q]->lF = ar.take<double>(3 * (size_t)nL_cap); fs[q]->E = ar.take<double>(1);
   }
   c->S.cc = ar.take<double>((size_t)nc * nc * 10);
   c->S.dc = ar.take<double>(ndna * nc * 7);
-  c->S.gc = ar.take<double>(nlhc * nc * 10);
-  c->S.ebuf = ar.take<double>(ebuf);
+  c->S.gc = ar.take<double>(nlhc_cap * nc * 10);
+  c->S.ebuf = ar.take<double>(ebuf_cap);
   c->S.nE = (int)ebuf;
-  c->r_all = ar.take<double>(3 * (size_t)M.n_D);
-  c->rd = ar.take<double>(c->m);
-  c->p = ar.take<double>(c->m);
+  c->r_all = ar.take<double>(3 * (size_t)nD_cap);
+  c->rd = ar.take<double>(m_cap);
+  c->p = ar.take<double>(m_cap);
   c->rr = ar.take<double>(3 * n);
-  c->rd_part = ar.take<double>(bdk::trmv_scratch_doubles(c->m));
+  c->rd_part = ar.take<double>(bdk::trmv_scratch_doubles(m_cap));
   c->energy = ar.take<double>(1);
   float* d_tqf = ar.take<float>(nt + 4 * (size_t)m->Nq);  // tail charges, core sites, core charges (FP32)
-  c->S.ph = ar.take<float4>(npos);
-  c->S.pl = ar.take<float4>(npos);
-  c->S.qh = ar.take<float4>(M.n_D);
-  c->S.ql = ar.take<float4>(M.n_D);
-  c->S.qf = ar.take<float4>(M.n_D);
-  c->S.bond = ar.take<double>(4 * ((size_t)nt + nL));
-  int* d_lhp_idx = ar.take<int>(nL);
+  c->S.ph = ar.take<float4>(npos_cap);
+  c->S.pl = ar.take<float4>(npos_cap);
+  c->S.qh = ar.take<float4>(nD_cap);
+  c->S.ql = ar.take<float4>(nD_cap);
+  c->S.qf = ar.take<float4>(nD_cap);
+  c->S.bond = ar.take<double>(4 * ((size_t)nt + nL_cap));
+  int* d_lhp_idx = ar.take<int>(nL_cap);
   c->S.bonds = ar.take<double>(37 * (size_t)n);
   c->S.ot = n; c->S.ol = n + nt; c->S.og = n + nt + nL; c->S.npos = npos;
   c->negpiv = ar.take<int>(1);
@@ -522,7 +531,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
   }
   for (int k = 0; k < 10; k++) cudaEventCreate(&c->ev[k]);
   if (c->precision == BD_PREC_MIXED) {
-    c->kev.resize(2 * (size_t)bdk::mixed_max_launches(c->m));
+    c->kev.resize(2 * (size_t)bdk::mixed_max_launches(c->m_cap));
     for (auto& ev : c->kev) cudaEventCreate(&ev);
   }
   e = cudaStreamSynchronize(st);
@@ -1064,7 +1073,7 @@ extern "C" int bd_set_noise_mode(bd_ctx* c, int mode, double tol, int kmax) {
   if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
   if (mode == BD_NOISE_KRYLOV && (!c->kscratch || kmax > c->krylov_kmax)) {
     if (c->kscratch) cudaFree(c->kscratch), c->kscratch = nullptr;
-    if (cudaMalloc((void**)&c->kscratch, bdk::krylov_scratch_doubles(c->m, kmax) * sizeof(double)) != cudaSuccess)
+    if (cudaMalloc((void**)&c->kscratch, bdk::krylov_scratch_doubles(c->m_cap, kmax) * sizeof(double)) != cudaSuccess)
       return set_error(BD_ERR_NOMEM, "bd_set_noise_mode: Krylov workspace allocation failed");
   }
   c->noise_mode = mode;
@@ -1232,8 +1241,8 @@ extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double deb
 extern "C" int bd_set_lh_flags(bd_ctx* c, const int* nc_lh_flag, const double* r_lh, const double* lh_rad) {
   if (!c || !nc_lh_flag || !c->model) return set_error(BD_ERR_ARG, "bd_set_lh_flags: null argument");
   if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_lh_flags: the context belongs to a batch");
-  const bdh::ModelCopy& old = *c->model;
-  const int nc = old.m.n_c, n = old.m.n, nt = old.m.n_tail, nlh = old.m.n_lh_n + old.m.n_lh_c;
+  DevModel& M = c->M;
+  const int nc = M.n_c, n = M.n, nt = M.n_tail, nlh = M.nlh;
   int bound = 0;
   for (int k = 0; k < nc; k++) {
     if (nc_lh_flag[k] != 0 && nc_lh_flag[k] != 1) return set_error(BD_ERR_ARG, "bd_set_lh_flags: flags are 0 or 1");
@@ -1241,52 +1250,61 @@ extern "C" int bd_set_lh_flags(bd_ctx* c, const int* nc_lh_flag, const double* r
   }
   const int nLH = bound * nlh;
   if (nLH > 0 && !r_lh) return set_error(BD_ERR_ARG, "bd_set_lh_flags: LH positions required");
-  auto cp = std::make_shared<bdh::ModelCopy>(old);
-  cp->nc_lh_flag.assign(nc_lh_flag, nc_lh_flag + nc);
-  cp->m.n_LH = nLH;
+  if (3 * (n + nt + nLH) > c->m_cap) return set_error(BD_ERR_STATE, "bd_set_lh_flags: more LH beads than the context holds");
+  // the new binding's per-bead tables, as bd_create builds them
+  bdh::ModelCopy& mc = *c->model;
+  std::vector<double> rad(nLH);
   if (lh_rad) {
-    cp->lh_rad.assign(lh_rad, lh_rad + nLH);
+    rad.assign(lh_rad, lh_rad + nLH);
   } else {  // every linker histone has the same beads: repeat the first one's radii
     std::vector<double> one(nlh, 0.5);
-    if ((int)old.lh_rad.size() >= nlh) one.assign(old.lh_rad.begin(), old.lh_rad.begin() + nlh);
-    cp->lh_rad.clear();
-    for (int k = 0; k < bound; k++) cp->lh_rad.insert(cp->lh_rad.end(), one.begin(), one.end());
+    if ((int)mc.lh_rad.size() >= nlh) one.assign(mc.lh_rad.begin(), mc.lh_rad.begin() + nlh);
+    for (int k = 0; k < nLH; k++) rad[k] = one[k % std::max(nlh, 1)];
   }
-  cp->bind();
+  std::vector<int> core_bead, core_lh(nc, -1), lh_core_bead, lhp(nLH);
+  for (int i = 0; i < n; i++)
+    if (c->h_type[i] == 1) core_bead.push_back(i);
+  for (int k = 0; k < nc; k++)
+    if (nc_lh_flag[k] == 1) core_lh[k] = (int)lh_core_bead.size(), lh_core_bead.push_back(core_bead[k]);
+  for (int b = 0; b < nLH; b++) {
+    const int idx = b % nlh;
+    lhp[b] = idx < M.n_lh_n ? idx : idx + M.n_lh_g;
+  }
   cudaStream_t st = c->stream;
-  auto down = [&](const double* d, long cnt, std::vector<double>& h) -> int {
-    h.resize(cnt);
-    if (cnt) CK(cudaMemcpyAsync(h.data(), d, cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
-    return BD_OK;
-  };
-  std::vector<double> r, a, b, cc, rt, al, be, ga, le, ad, bd, cd, ap, bp, gp;
-  const DevState& X = c->X;
-  int rc = 0;
-  if ((rc = down(X.r, 3L * n, r)) || (rc = down(X.a, 3L * n, a)) || (rc = down(X.b, 3L * n, b)) ||
-      (rc = down(X.c, 3L * n, cc)) || (rc = down(X.r_t, 3L * nt, rt)) || (rc = down(X.alpha, n, al)) ||
-      (rc = down(X.beta, n, be)) || (rc = down(X.gamma, n, ga)) || (rc = down(X.length, n, le)) ||
-      (rc = down(X.a_dna, 3L * nc, ad)) || (rc = down(X.b_dna, 3L * nc, bd)) || (rc = down(X.c_dna, 3L * nc, cd)) ||
-      (rc = down(X.alpha_p, nc, ap)) || (rc = down(X.beta_p, nc, bp)) || (rc = down(X.gamma_p, nc, gp)))
+  CK(cudaStreamSynchronize(st));  // no step of the old size in flight
+  int rc;
+  if ((rc = up(const_cast<int*>(M.core_lh), core_lh.data(), nc, st)) ||
+      (rc = up(const_cast<int*>(M.lh_core_bead), lh_core_bead.data(), (int)lh_core_bead.size(), st)) ||
+      (rc = up(const_cast<int*>(M.lh_p), lhp.data(), nLH, st)) ||
+      (rc = up(const_cast<int*>(M.nc_lh_flag), nc_lh_flag, nc, st)) ||
+      (rc = up(const_cast<double*>(M.rad_all) + n + nt, rad.data(), nLH, st)) ||
+      (rc = up(c->X.r_lh, r_lh, 3 * nLH, st)))
     return rc;
+  // logical sizes and the offsets that depend on them
+  M.n_LH = nLH;
+  M.n_D = n + nt + nLH;
+  M.n_lhcore = (int)lh_core_bead.size();
+  c->m = 3 * M.n_D;
+  c->S.og = n + nt + nLH;
+  c->S.npos = n + nt + nLH + M.n_lhcore * M.n_lh_g;
+  c->S.nE = 8 * n + nt + nLH;
+  // the LH bend angles of the new beads; the frame pass is left out, since
+  // its re-orthonormalisation of b and c is not bit-idempotent
+  bdk::frame_angles(M, c->X, st);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
-  bd_state s{};
-  s.r = r.data(); s.a = a.data(); s.b = b.data(); s.c = cc.data(); s.r_t = rt.data(); s.r_lh = r_lh;
-  s.refresh_frames = 0;
-  s.alpha = al.data(); s.beta = be.data(); s.gamma = ga.data(); s.length = le.data();
-  s.a_dna = ad.data(); s.b_dna = bd.data(); s.c_dna = cd.data();
-  s.alpha_p = ap.data(); s.beta_p = bp.data(); s.gamma_p = gp.data();
-  bd_options o{};
-  o.precision = c->precision;
-  o.frequency_RP = c->freq_rp;
-  o.use_graph = c->use_graph;
-  o.device = c->device;
-  o.stream = c->stream;
-  bd_ctx* fresh = nullptr;
-  if ((rc = bd_create(&cp->m, &s, &o, &fresh))) return rc;
-  fresh->step_count = c->step_count;
-  std::swap(*c, *fresh);
-  std::swap(c->own_stream, fresh->own_stream);  // the stream stays with the caller's handle
-  return bd_destroy(fresh);
+  // everything planned for the old size goes
+  if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
+  bdh::adj_free(c->adj);
+  c->adj = nullptr;
+  c->a_holds_factor = false;
+  c->need_rebuild = true;  // the next step assembles and factors the tensor of the new size
+  // the host copy of the model follows
+  mc.nc_lh_flag.assign(nc_lh_flag, nc_lh_flag + nc);
+  mc.lh_rad = rad;
+  mc.m.n_LH = nLH;
+  mc.bind();
+  return BD_OK;
 }
 
 extern "C" int bd_restart_from_context(bd_ctx* c, bd_restart* rs) {

@@ -122,6 +122,9 @@ struct DevScratch {
 namespace bdk {
 // frames.cu
 void frames(const DevModel& M, DevState& S, cudaStream_t st);
+// the angle pass alone: reads positions and frames, writes angles (and the
+// tail and LH bend angles) without touching the frames
+void frame_angles(const DevModel& M, DevState& S, cudaStream_t st);
 // mixed: the drift from S.qh / S.ql (filled by gather_rall) and S.qf
 void rotate_translate(const DevModel& M, const DevState& X, DevState& Y, const DevForces& Fo, const double* rr,
                       const double* rd, const double* r_all, int mixed, const DevScratch& S, cudaStream_t st);
@@ -203,6 +206,7 @@ struct bd_ctx {
   double krylov_change = 0.0;
   double* kscratch = nullptr;
   bool a_holds_factor = false;  // A holds L (after a factorisation), not D
+  bool need_rebuild = false;    // the next step assembles D whatever frequency_RP says (after a resize)
   long step_count = 0;
   DevModel M{};
   DevState X{}, Y{};
@@ -212,7 +216,8 @@ struct bd_ctx {
   double* A = nullptr;   // m x lda, column-major; holds D then L (FP64 path)
   unsigned char* PS = nullptr;  // mixed path: BF16 panel slices
   int* d_err = nullptr;         // device error code of the tensor-core kernels
-  int m = 0, lda = 0;
+  int m = 0, lda = 0;  // 3 n_D now, and the leading dimension of A (for m_cap)
+  int m_cap = 0;       // largest m the buffers hold: every core with a linker histone
   double *r_all = nullptr, *rd = nullptr, *p = nullptr, *rr = nullptr, *rd_part = nullptr, *energy = nullptr;
   int* negpiv = nullptr;
   cudaGraphExec_t graph = nullptr;

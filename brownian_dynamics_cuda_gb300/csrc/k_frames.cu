@@ -433,6 +433,12 @@ void frames(const DevModel& M, DevState& S, cudaStream_t st) {
   if (tot > 0) k_frames_angles<<<cdiv(tot, kFrameThreads), kFrameThreads, 0, st>>>(M, S);
 }
 
+void frame_angles(const DevModel& M, DevState& S, cudaStream_t st) {
+  const int nb = M.n - 1 > 0 ? M.n - 1 : 0;
+  const int tot = nb + M.n_tail + M.n_LH;
+  if (tot > 0) k_frames_angles<<<cdiv(tot, kFrameThreads), kFrameThreads, 0, st>>>(M, S);
+}
+
 void gather_rall(const DevModel& M, const DevState& X, double* r_all, const DevScratch* S, cudaStream_t st) {
   int tot = 3 * M.n_D;
   k_gather_rall<<<cdiv(tot, 256), 256, 0, st>>>(M.n, M.n_tail, M.n_LH, X.r, X.r_t, X.r_lh, r_all);

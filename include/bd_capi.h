@@ -391,11 +391,16 @@ int bd_restart_from_context(bd_ctx* ctx, bd_restart* rs);
 
 /* Linker-histone binding changed (main.cpp:386-465: every 100 steps one
  * core may bind or release its linker histone, which changes n_LH and the
- * size of D): the context is rebuilt in place for the new flags [n_c] from
- * its current device state, with r_lh [3 n_LH] the new LH bead positions
- * (bound cores in order, as main.cpp:418-447 builds them) and lh_rad [n_LH]
- * their radii (NULL: the first linker histone's radii repeated).  The handle
- * stays valid; sizes (bd_sizes) change.  Not for contexts inside a batch. */
+ * size of D): the context is resized on the device for the new flags [n_c],
+ * with r_lh [3 n_LH] the new LH bead positions (bound cores in order, as
+ * main.cpp:418-447 builds them) and lh_rad [n_LH] their radii (NULL: the
+ * first linker histone's radii repeated).  Nothing is reallocated and no
+ * state leaves the device: bd_create sizes every binding-dependent buffer
+ * (D, its factor, the LH arrays, the mirrors) for every core bound, and the
+ * call uploads the new LH tables and beads, sets the logical sizes, and makes
+ * the next step assemble and factor the tensor of the new size (its graph is
+ * captured again).  The handle stays valid; sizes (bd_sizes) change.  Not
+ * for contexts inside a batch. */
 int bd_set_lh_flags(bd_ctx* ctx, const int* nc_lh_flag, const double* r_lh, const double* lh_rad);
 
 /* ---------------------------------------------------------------- gradients

@@ -38,10 +38,53 @@ def test_release_one_linker_histone(tmp_path, prec):
     arrays = dict(fib.arrays, nc_lh_flag=flags, lh_rad=lh_rad)
     fib2 = dataclasses.replace(fib, sizes=sizes, arrays=arrays, state=dict(state, r_lh=r_lh))
     b = Context(fib2, precision=prec, refresh=False, angles=angles)
-    for k in ("r", "a", "r_t", "r_lh", "beta"):
+    for k in ("r", "a", "b", "c", "r_t", "r_lh", "beta", "length", "a_dna", "beta_p", "beta_lh"):
         assert np.array_equal(a.get(k), b.get(k)), k
     for s in range(2, 4):
         rr, p = nz.step(s, fib.arrays["r_var"], a.m)
+        assert a.step(rr, p) == b.step(rr, p)
+        for k in ("r", "a", "r_t", "r_lh"):
+            assert np.array_equal(a.get(k), b.get(k)), (s, k)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_bind_one_linker_histone_in_place(tmp_path, prec):
+    """Growth: a context created with core 1's linker histone released binds
+    it again; the resize stays inside the buffers bd_create sized for every
+    core bound (the device's free memory is unchanged), and the context
+    continues exactly as one created from scratch with the new binding."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import Context, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, make_fiber
+    full = make_fiber(FiberSpec(4, [30] * 4, lh=True, seed=3), str(tmp_path))
+    nlh = full.sizes["n_lh_n"] + full.sizes["n_lh_c"]
+    flags = full.arrays["nc_lh_flag"].copy()
+    flags[1] = 0
+    keep = np.ones(full.sizes["n_LH"], bool)
+    keep[nlh:2 * nlh] = False
+    part = dataclasses.replace(full, sizes=dict(full.sizes, n_LH=int(flags.sum()) * nlh),
+                               arrays=dict(full.arrays, nc_lh_flag=flags, lh_rad=full.arrays["lh_rad"][keep]),
+                               state=dict(full.state, r_lh=full.state["r_lh"].reshape(-1, 3)[keep].ravel()))
+    a = Context(part, precision=prec)
+    nz = Noise(8)
+    for s in range(2):
+        a.step(*nz.step(s, full.arrays["r_var"], a.m))
+    r_lh_now = a.get("r_lh").reshape(-1, 3)
+    r_lh_new = np.concatenate([r_lh_now[:nlh], full.state["r_lh"].reshape(-1, 3)[nlh:2 * nlh], r_lh_now[nlh:]]).ravel()
+    state = {k: a.get(k) for k in ("r", "a", "b", "c", "r_t")}
+    angles = {k: a.get(k) for k in ANGLES}
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    a.set_lh_flags(full.arrays["nc_lh_flag"], r_lh_new, full.arrays["lh_rad"])
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert a.n_LH == full.sizes["n_LH"] and a.m == full.m
+    b = Context(dataclasses.replace(full, state=dict(state, r_lh=r_lh_new)), precision=prec, refresh=False,
+                angles=angles)
+    for k in ("r", "a", "b", "c", "r_t", "r_lh", "beta", "length", "a_dna", "beta_p", "beta_lh"):
+        assert np.array_equal(a.get(k), b.get(k)), k
+    for s in range(2, 4):
+        rr, p = nz.step(s, full.arrays["r_var"], a.m)
         assert a.step(rr, p) == b.step(rr, p)
         for k in ("r", "a", "r_t", "r_lh"):
             assert np.array_equal(a.get(k), b.get(k)), (s, k)
