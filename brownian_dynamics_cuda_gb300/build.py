@@ -35,6 +35,7 @@ UNITS = [
     ("k_adjoint.cu", []),
     ("k_noise.cu", []),
     ("k_krylov.cu", []),
+    ("k_tc_gemm.cu", []),
 ]
 
 

@@ -47,15 +47,20 @@ ADJ_HD T ipow(T x, int k) {
   return r;
 }
 
-template <class R, int W>
+// Dual<R, W, G>: value of type R, derivatives of type G (G = R by
+// default).  G = float with R = double keeps every value - and every
+// elementary function's derivative, evaluated at the value - in FP64, while
+// the W directional derivatives propagate in FP32: the FP64 pipe does the
+// primal once, the FP32 pipe the W-fold tangent arithmetic.
+template <class R, int W, class G = R>
 struct Dual {
   using real = R;
   R v;
-  R d[W];
+  G d[W];
   ADJ_HD Dual() {}
   template <class S>
   ADJ_HD explicit Dual(S x) : v(R(x)) {
-    for (int i = 0; i < W; i++) d[i] = R(0);
+    for (int i = 0; i < W; i++) d[i] = G(0);
   }
 };
 
@@ -63,105 +68,110 @@ template <class T>
 struct RealOf {
   using type = T;
 };
-template <class R, int W>
-struct RealOf<Dual<R, W>> {
+template <class R, int W, class G>
+struct RealOf<Dual<R, W, G>> {
   using type = R;
 };
 
-template <class R, int W>
-ADJ_HD R val(const Dual<R, W>& a) {
+template <class R, int W, class G>
+ADJ_HD R val(const Dual<R, W, G>& a) {
   return a.v;
 }
 
-#define ADJ_DUAL template <class R, int W> ADJ_HD Dual<R, W>
-ADJ_DUAL operator+(const Dual<R, W>& a, const Dual<R, W>& b) {
-  Dual<R, W> o;
+#define ADJ_DUAL template <class R, int W, class G> ADJ_HD Dual<R, W, G>
+ADJ_DUAL operator+(const Dual<R, W, G>& a, const Dual<R, W, G>& b) {
+  Dual<R, W, G> o;
   o.v = a.v + b.v;
   for (int i = 0; i < W; i++) o.d[i] = a.d[i] + b.d[i];
   return o;
 }
-ADJ_DUAL operator-(const Dual<R, W>& a, const Dual<R, W>& b) {
-  Dual<R, W> o;
+ADJ_DUAL operator-(const Dual<R, W, G>& a, const Dual<R, W, G>& b) {
+  Dual<R, W, G> o;
   o.v = a.v - b.v;
   for (int i = 0; i < W; i++) o.d[i] = a.d[i] - b.d[i];
   return o;
 }
-ADJ_DUAL operator-(const Dual<R, W>& a) {
-  Dual<R, W> o;
+ADJ_DUAL operator-(const Dual<R, W, G>& a) {
+  Dual<R, W, G> o;
   o.v = -a.v;
   for (int i = 0; i < W; i++) o.d[i] = -a.d[i];
   return o;
 }
-ADJ_DUAL operator*(const Dual<R, W>& a, const Dual<R, W>& b) {
-  Dual<R, W> o;
+ADJ_DUAL operator*(const Dual<R, W, G>& a, const Dual<R, W, G>& b) {
+  Dual<R, W, G> o;
   o.v = a.v * b.v;
-  for (int i = 0; i < W; i++) o.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  const G av = G(a.v), bv = G(b.v);
+  for (int i = 0; i < W; i++) o.d[i] = a.d[i] * bv + av * b.d[i];
   return o;
 }
-ADJ_DUAL operator/(const Dual<R, W>& a, const Dual<R, W>& b) {
-  Dual<R, W> o;
+ADJ_DUAL operator/(const Dual<R, W, G>& a, const Dual<R, W, G>& b) {
+  Dual<R, W, G> o;
   const R ib = R(1) / b.v;
   o.v = a.v * ib;
-  for (int i = 0; i < W; i++) o.d[i] = (a.d[i] - o.v * b.d[i]) * ib;
+  const G ov = G(o.v), ibg = G(ib);
+  for (int i = 0; i < W; i++) o.d[i] = (a.d[i] - ov * b.d[i]) * ibg;
   return o;
 }
-ADJ_DUAL operator+(const Dual<R, W>& a, typename Dual<R, W>::real b) {
-  Dual<R, W> o = a;
+ADJ_DUAL operator+(const Dual<R, W, G>& a, typename Dual<R, W, G>::real b) {
+  Dual<R, W, G> o = a;
   o.v = a.v + b;
   return o;
 }
-ADJ_DUAL operator+(typename Dual<R, W>::real b, const Dual<R, W>& a) { return a + b; }
-ADJ_DUAL operator-(const Dual<R, W>& a, typename Dual<R, W>::real b) {
-  Dual<R, W> o = a;
+ADJ_DUAL operator+(typename Dual<R, W, G>::real b, const Dual<R, W, G>& a) { return a + b; }
+ADJ_DUAL operator-(const Dual<R, W, G>& a, typename Dual<R, W, G>::real b) {
+  Dual<R, W, G> o = a;
   o.v = a.v - b;
   return o;
 }
-ADJ_DUAL operator-(typename Dual<R, W>::real b, const Dual<R, W>& a) {
-  Dual<R, W> o = -a;
+ADJ_DUAL operator-(typename Dual<R, W, G>::real b, const Dual<R, W, G>& a) {
+  Dual<R, W, G> o = -a;
   o.v = b - a.v;
   return o;
 }
-ADJ_DUAL operator*(const Dual<R, W>& a, typename Dual<R, W>::real b) {
-  Dual<R, W> o;
+ADJ_DUAL operator*(const Dual<R, W, G>& a, typename Dual<R, W, G>::real b) {
+  Dual<R, W, G> o;
   o.v = a.v * b;
-  for (int i = 0; i < W; i++) o.d[i] = a.d[i] * b;
+  const G bg = G(b);
+  for (int i = 0; i < W; i++) o.d[i] = a.d[i] * bg;
   return o;
 }
-ADJ_DUAL operator*(typename Dual<R, W>::real b, const Dual<R, W>& a) { return a * b; }
-ADJ_DUAL operator/(const Dual<R, W>& a, typename Dual<R, W>::real b) {
-  Dual<R, W> o;
+ADJ_DUAL operator*(typename Dual<R, W, G>::real b, const Dual<R, W, G>& a) { return a * b; }
+ADJ_DUAL operator/(const Dual<R, W, G>& a, typename Dual<R, W, G>::real b) {
+  Dual<R, W, G> o;
   o.v = a.v / b;
-  for (int i = 0; i < W; i++) o.d[i] = a.d[i] / b;
+  const G bg = G(b);
+  for (int i = 0; i < W; i++) o.d[i] = a.d[i] / bg;
   return o;
 }
-ADJ_DUAL operator/(typename Dual<R, W>::real b, const Dual<R, W>& a) {
-  Dual<R, W> o;
+ADJ_DUAL operator/(typename Dual<R, W, G>::real b, const Dual<R, W, G>& a) {
+  Dual<R, W, G> o;
   o.v = b / a.v;
-  const R k = -o.v / a.v;
+  const G k = G(-o.v / a.v);
   for (int i = 0; i < W; i++) o.d[i] = k * a.d[i];
   return o;
 }
 
 // elementary functions: f(a) with f'(a) applied to every derivative
-template <class R, int W>
-ADJ_HD Dual<R, W> chain_(const Dual<R, W>& a, R fv, R fd) {
-  Dual<R, W> o;
+template <class R, int W, class G>
+ADJ_HD Dual<R, W, G> chain_(const Dual<R, W, G>& a, R fv, R fd) {
+  Dual<R, W, G> o;
   o.v = fv;
-  for (int i = 0; i < W; i++) o.d[i] = fd * a.d[i];
+  const G f = G(fd);
+  for (int i = 0; i < W; i++) o.d[i] = f * a.d[i];
   return o;
 }
-ADJ_DUAL vsqrt(const Dual<R, W>& a) {
+ADJ_DUAL vsqrt(const Dual<R, W, G>& a) {
   const R s = vsqrt(a.v);
   return chain_(a, s, R(0.5) / s);
 }
-ADJ_DUAL vsin(const Dual<R, W>& a) { return chain_(a, vsin(a.v), vcos(a.v)); }
-ADJ_DUAL vcos(const Dual<R, W>& a) { return chain_(a, vcos(a.v), -vsin(a.v)); }
-ADJ_DUAL vtan(const Dual<R, W>& a) {
+ADJ_DUAL vsin(const Dual<R, W, G>& a) { return chain_(a, vsin(a.v), vcos(a.v)); }
+ADJ_DUAL vcos(const Dual<R, W, G>& a) { return chain_(a, vcos(a.v), -vsin(a.v)); }
+ADJ_DUAL vtan(const Dual<R, W, G>& a) {
   const R t = vtan(a.v);
   return chain_(a, t, R(1) + t * t);
 }
-ADJ_DUAL vacos(const Dual<R, W>& a) { return chain_(a, vacos(a.v), -R(1) / vsqrt(R(1) - a.v * a.v)); }
-ADJ_DUAL vexp(const Dual<R, W>& a) {
+ADJ_DUAL vacos(const Dual<R, W, G>& a) { return chain_(a, vacos(a.v), -R(1) / vsqrt(R(1) - a.v * a.v)); }
+ADJ_DUAL vexp(const Dual<R, W, G>& a) {
   const R e = vexp(a.v);
   return chain_(a, e, e);
 }
@@ -192,23 +202,31 @@ ADJ_HD T norm3(const T* v) {
 #if defined(__CUDACC__)
 #pragma nv_exec_check_disable
 #endif
-template <int W, int NIN, int NOUT, class R, class F>
-ADJ_HD void vjp_chunk(const F& f, const R* x, const R* ybar, int chunk, R* xbar) {
-  using D = Dual<R, W>;
+template <int W, int NIN, int NOUT, class G, class R, class F>
+ADJ_HD void vjp_chunk_g(const F& f, const R* x, const R* ybar, int chunk, R* xbar) {
+  using D = Dual<R, W, G>;
   D xd[NIN];
   D yd[NOUT];
   for (int k = 0; k < NIN; k++) {
     xd[k] = D(x[k]);
     const int j = k - chunk * W;
-    if (j >= 0 && j < W) xd[k].d[j] = R(1);
+    if (j >= 0 && j < W) xd[k].d[j] = G(1);
   }
   for (int o = 0; o < NOUT; o++) yd[o] = D(0.0);
   f(xd, yd);
   for (int j = 0; j < W; j++) {
     R s = R(0);
-    for (int o = 0; o < NOUT; o++) s += ybar[o] * yd[o].d[j];
+    for (int o = 0; o < NOUT; o++) s += ybar[o] * R(yd[o].d[j]);
     xbar[j] = s;
   }
+}
+// derivatives in the value's own type
+#if defined(__CUDACC__)
+#pragma nv_exec_check_disable
+#endif
+template <int W, int NIN, int NOUT, class R, class F>
+ADJ_HD void vjp_chunk(const F& f, const R* x, const R* ybar, int chunk, R* xbar) {
+  vjp_chunk_g<W, NIN, NOUT, R>(f, x, ybar, chunk, xbar);
 }
 
 }  // namespace adj

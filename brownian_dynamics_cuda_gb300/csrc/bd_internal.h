@@ -156,6 +156,13 @@ int potrf_mixed(int m, double* A, int lda, unsigned char* PS, int* negpiv, int* 
 int mixed_tiles(int m);
 // k_krylov.cu: rd = s2dt D^{1/2} p by Lanczos on the lower-stored tensor
 size_t krylov_scratch_doubles(int m, int kmax);
+// tc_gemm.cu: C = alpha A op(B) on tcgen05 (row-major FP32, three BF16
+// slices, six products); M, N multiples of 128, K of 64; kmode limits each
+// 128-tile's K range (1: k >= row0, 2: k >= col0, 4: k < col0 + 128);
+// batch products zstride elements apart; a timed-out wait sets *err
+int tc_gemm_f32(cudaStream_t st, int M, int N, int K, float alpha, const float* A, int lda, const float* B, int ldb,
+                float* C, int ldc, bool tb, int kmode, int batch, long zstride, int* err);
+int tc_gemm_attributes();
 // A == nullptr: matrix-free products from the double-float position mirror qh/ql
 int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, const float4* ql, double a1, double a2,
                 const double* p, double s2dt, double tol, int kmax, double* rd, double* scratch, cudaStream_t st,

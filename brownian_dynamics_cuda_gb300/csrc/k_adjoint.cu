@@ -22,6 +22,7 @@
 // (adj_dual.cuh, adj_terms.cuh); the O(m^3) Cholesky backward runs as a
 // blocked triangular inverse and a triangle-aware GEMM.
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include <algorithm>
 #include <cmath>
@@ -76,13 +77,21 @@ __device__ __forceinline__ bool pair_ok(const DevModel& M, int i, int j) {
 
 // ------------------------------------------------------------ chain bonds
 constexpr int kBW = 8;         // inputs seeded per thread (frame refresh, anchors)
-constexpr int kBondW = 2;      // inputs seeded per thread of the bond term (FP64; many short threads)
 constexpr int kBondIn = 39;
-constexpr int kBondChunks = (kBondIn + kBondW - 1) / kBondW;
+// inputs seeded per thread of the bond term (many short threads: the
+// term's FP64 chain is latency-bound), with FP64 derivatives or, on mixed
+// contexts, FP32 derivatives of the FP64 values
+#ifndef BD_BOND_WM
+#define BD_BOND_WM 2
+#endif
+constexpr int kBondW = 2;
+constexpr int kBondWm = BD_BOND_WM;
+__host__ __device__ constexpr int bond_chunks(int w) { return (kBondIn + w - 1) / w; }
 
-template <class R>
+template <class R, class G, int BW>
 __global__ void __launch_bounds__(64) k_adj_bonds(DevModel M, const double* __restrict__ x,
                                                   const double* __restrict__ fb, double* lam, double* th) {
+  constexpr int kBondChunks = bond_chunks(BW);
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / kBondChunks, ch = t % kBondChunks;
   if (i >= M.n - 1) return;
@@ -109,12 +118,12 @@ __global__ void __launch_bounds__(64) k_adj_bonds(DevModel M, const double* __re
     yb[6 + q] = R(fb[n3 + 3 * i + q]);
     yb[9 + q] = R(fb[n3 + 3 * (i + 1) + q]);
   }
-  R xb[kBondW];
-  vjp_chunk<kBondW, kBondIn, 12>(
+  R xb[BW];
+  vjp_chunk_g<BW, kBondIn, 12, G>(
       [&](const auto* xd, auto* yd) { bond_term(k, xd, xd + 12, xd + 24, xd[36], xd[37], xd[38], yd); }, xin, yb,
       ch, xb);
-  for (int j = 0; j < kBondW; j++) {
-    const int q = ch * kBondW + j;
+  for (int j = 0; j < BW; j++) {
+    const int q = ch * BW + j;
     if (q >= kBondIn) break;
     const double v = (double)xb[j];
     if (q < 12) {
@@ -234,8 +243,10 @@ __global__ void __launch_bounds__(128) k_adj_dnacore(DevModel M, const double* _
 // ------------------------------------------------------------ core-core
 // one CTA per core pair; threads over the first core's charges, the second
 // core's sites (position, torque-adjoint terms) staged in shared memory
+constexpr int kCcThreads = 64;  // core i's sites per CTA of a core pair
+
 template <class R>
-__global__ void __launch_bounds__(256) k_adj_corecore(DevModel M, const double* __restrict__ x,
+__global__ void __launch_bounds__(kCcThreads) k_adj_corecore(DevModel M, const double* __restrict__ x,
                                                       const double* __restrict__ fb, double* lam, double* th) {
   extern __shared__ unsigned char smem_raw[];
   R* sl = reinterpret_cast<R*>(smem_raw);  // per site l: p_l(3), Qj(3), Kj(3), cp_l(3), q_l
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__(256) k_adj_corecore(DevModel M, const double* 
   const int Nq = M.Nq;
   for (int l = threadIdx.x; l < Nq; l += blockDim.x) {
     R cp[3] = {R(M.core_pos[3 * l]), R(M.core_pos[3 * l + 1]), R(M.core_pos[3 * l + 2])};
-    R* e = sl + 13 * l;
+    R* e = sl + 13 * l;  // core j's sites, staged by every CTA of the pair
     for (int q = 0; q < 3; q++) e[q] = xj[q] + xj[3 + q] * cp[0] + xj[6 + q] * cp[1] + xj[9 + q] * cp[2];
     R Q[3];
     cross3(Tj, cp, Q);
@@ -275,7 +286,10 @@ __global__ void __launch_bounds__(256) k_adj_corecore(DevModel M, const double* 
   R acc[25];
   for (int q = 0; q < 25; q++) acc[q] = R(0);  // bead i: r a b c (12), bead j: r a b c (12), kappa
   const R ke = R(M.k_e), kex = R(M.k_ex), sg = R(M.sCC);
-  for (int k = threadIdx.x; k < Nq; k += blockDim.x) {
+  // this CTA's slice of core i's sites: one per thread (the pair spread over
+  // gridDim.y small CTAs, so the pairs of a step balance across the SMs)
+  const int kend = min(Nq, (int)(blockIdx.y + 1) * (int)blockDim.x);
+  for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < kend; k += blockDim.x) {
     const R cp[3] = {R(M.core_pos[3 * k]), R(M.core_pos[3 * k + 1]), R(M.core_pos[3 * k + 2])};
     const R qk = R(M.core_q[k]);
     R pk[3], Qi[3], Ki[3];
@@ -334,7 +348,7 @@ __global__ void __launch_bounds__(256) k_adj_corecore(DevModel M, const double* 
 }
 
 // ------------------------------------------------------------ tails
-template <class R>
+template <class R, class G = R>
 __global__ void k_adj_tail_bonded(DevModel M, const double* __restrict__ x, const double* __restrict__ fb,
                                   double* lam) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -346,7 +360,7 @@ __global__ void k_adj_tail_bonded(DevModel M, const double* __restrict__ x, cons
     for (int q = 0; q < 6; q++) xin[q] = R(x[ot + 3 * i + q]);
     for (int q = 0; q < 3; q++) yb[q] = R(fb[of + 3 * i + q] - fb[of + 3 * i + 3 + q]);
     const R ht = R(M.h_t[i]), lo = R(M.lo_t[i]);
-    vjp_chunk<6, 6, 3>([&](const auto* xd, auto* yd) { stretch_f(ht, lo, xd, xd + 3, yd); }, xin, yb, 0, xb);
+    vjp_chunk_g<6, 6, 3, G>([&](const auto* xd, auto* yd) { stretch_f(ht, lo, xd, xd + 3, yd); }, xin, yb, 0, xb);
     for (int q = 0; q < 6; q++) atomicAdd(lam + ot + 3 * i + q, (double)xb[q]);
   }
   if (i < nt - 2 && M.t_grp[i] == M.t_grp[i + 1] && M.t_grp[i] == M.t_grp[i + 2]) {  // func.cpp:1803-1810
@@ -356,7 +370,7 @@ __global__ void k_adj_tail_bonded(DevModel M, const double* __restrict__ x, cons
       yb[q] = -R(fb[of + 3 * i + q]);
     }
     const R gt = R(M.g_t[i]), b0 = R(M.beta_o_t[i]);
-    vjp_chunk<9, 9, 9>([&](const auto* xd, auto* yd) { bend3_f(gt, b0, xd, xd + 3, xd + 6, yd); }, xin, yb, 0, xb);
+    vjp_chunk_g<9, 9, 9, G>([&](const auto* xd, auto* yd) { bend3_f(gt, b0, xd, xd + 3, xd + 6, yd); }, xin, yb, 0, xb);
     for (int q = 0; q < 9; q++) atomicAdd(lam + ot + 3 * i + q, (double)xb[q]);
   }
 }
@@ -407,7 +421,7 @@ __global__ void k_adj_tail_pairs(DevModel M, const double* __restrict__ x, const
 }
 
 // anchors of the template tail beads to their cores (func.cpp:1831-1856)
-template <class R>
+template <class R, class G = R>
 __global__ void k_adj_anchor(DevModel M, const double* __restrict__ x, const double* __restrict__ fb, double* lam,
                              double* th) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -425,7 +439,7 @@ __global__ void k_adj_anchor(DevModel M, const double* __restrict__ x, const dou
     yb[6 + q] = R(fb[n3 + 3 * i + q]);
   }
   const double* P = M.tail_pos + 3 * jt;
-  vjp_chunk<8, 16, 9>([&](const auto* xd, auto* yd) { anchor_term(P, xd, xd + 3, xd[15], yd); }, xin, yb, ch, xb);
+  vjp_chunk_g<8, 16, 9, G>([&](const auto* xd, auto* yd) { anchor_term(P, xd, xd + 3, xd[15], yd); }, xin, yb, ch, xb);
   for (int j = 0; j < 8; j++) {
     const int q = ch * 8 + j;
     const double v = (double)xb[j];
@@ -453,7 +467,7 @@ __global__ void k_pass1_init(DevModel M, const double* lam_in, double* lam_out, 
 constexpr int kP1In = 21;
 constexpr int kP1Chunks = (kP1In + kBW - 1) / kBW;
 
-template <class R>
+template <class R, class G = R>
 __global__ void k_adj_pass1(DevModel M, const double* __restrict__ x, const double* __restrict__ lam_in,
                             double* lam_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -473,7 +487,7 @@ __global__ void k_adj_pass1(DevModel M, const double* __restrict__ x, const doub
     yb[3 + q] = R(lam_in[2 * n3 + 3 * i + q]);
     yb[6 + q] = R(lam_in[3 * n3 + 3 * i + q]);
   }
-  vjp_chunk<kBW, kP1In, 9>(
+  vjp_chunk_g<kBW, kP1In, 9, G>(
       [&](const auto* xd, auto* yd) { frame_pass1(tn, xd, xd + 3, xd + 6, xd + 9, xd + 12, xd + 15, xd + 18, yd); },
       xin, yb, ch, xb);
   for (int j = 0; j < kBW; j++) {
@@ -490,7 +504,7 @@ __global__ void k_adj_pass1(DevModel M, const double* __restrict__ x, const doub
 }
 
 // adjoint of rotate (func.cpp:1607-1670) for one bead: torque and frame
-template <class R>
+template <class R, class G = R>
 __global__ void k_adj_rotate(DevModel M, const double* __restrict__ x, const double* __restrict__ T,
                              const double* __restrict__ rr, const double* __restrict__ lamR, double* lamX,
                              double* Tbar) {
@@ -510,7 +524,7 @@ __global__ void k_adj_rotate(DevModel M, const double* __restrict__ x, const dou
   const int core = M.type[i] != 0;
   const double dt = M.dt;
   const double* rri = rr + 3 * i;
-  vjp_chunk<12, 12, 9>([&](const auto* xd, auto* yd) { rotate_frame(core, dt, rri, xd, xd + 3, yd); }, xin, yb, 0,
+  vjp_chunk_g<12, 12, 9, G>([&](const auto* xd, auto* yd) { rotate_frame(core, dt, rri, xd, xd + 3, yd); }, xin, yb, 0,
                        xb);
   for (int q = 0; q < 3; q++) Tbar[3 * i + q] += (double)xb[q];
   for (int q = 3; q < 12; q++) lamX[sidx(n3, i, q)] += (double)xb[q];
@@ -810,20 +824,35 @@ int gemm(cudaStream_t st, int M_, int N_, int K_, R alpha, const R* A, int lda, 
   return 0;
 }
 
+// The tensor-core form for FP32 operands whose tiles are 128 x 128
+// (tcgen05, three BF16 slices, six products: FP32-class); FP64 operands and
+// the 64-wide first doubling level stay on the SIMT kernel.
+template <class R>
+int gemm_tc(cudaStream_t st, int M_, int N_, int K_, R alpha, const R* A, int lda, const R* B, int ldb, R* C, int ldc,
+            bool tb, int kmode, int* err, int batch = 1, long zstride = 0) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (err && M_ % 128 == 0 && N_ % 128 == 0 && K_ % 64 == 0)
+      return bdk::tc_gemm_f32(st, M_, N_, K_, alpha, A, lda, B, ldb, C, ldc, tb, kmode, batch, zstride, err);
+  }
+  return gemm<R>(st, M_, N_, K_, alpha, A, lda, B, ldb, C, ldc, tb, kmode, batch, zstride);
+}
+
 // V = U^-1 for the upper-triangular U of order mp = 64 * 2^k (diagonal
 // 64-blocks already inverted), by doubling: at block size b every diagonal
 // 2b-block [[V11, V12], [0, V22]] gets V12 = -V11 (U12 V22), all blocks of a
 // level in one batched launch per product (2 launches per level).
 template <class R>
-void inv_upper(cudaStream_t st, int mp, const R* U, R* V, R* tmp, int& launches) {
+int inv_upper(cudaStream_t st, int mp, const R* U, R* V, R* tmp, int& launches, int* err) {
   for (int b = 64; b < mp; b *= 2) {
     const int nodes = mp / (2 * b);
     const long zs = 2L * b * (mp + 1);
-    // T = U12 V22 (V22 upper: k < c0 + 64), then V12 = -V11 T (V11 upper: k >= r0)
-    gemm<R>(st, b, b, b, R(1), U + b, mp, V + (size_t)b * mp + b, mp, tmp + b, mp, false, 4, nodes, zs);
-    gemm<R>(st, b, b, b, R(-1), V, mp, tmp + b, mp, V + b, mp, false, 1, nodes, zs);
+    // T = U12 V22 (V22 upper: k < c0 + tile), then V12 = -V11 T (V11 upper: k >= r0)
+    int rc = gemm_tc<R>(st, b, b, b, R(1), U + b, mp, V + (size_t)b * mp + b, mp, tmp + b, mp, false, 4, err, nodes, zs);
+    if (!rc) rc = gemm_tc<R>(st, b, b, b, R(-1), V, mp, tmp + b, mp, V + b, mp, false, 1, err, nodes, zs);
+    if (rc) return rc;
     launches += 2;
   }
+  return 0;
 }
 
 }  // namespace
@@ -936,15 +965,21 @@ int forces_vjp(bd_ctx* c, const double* x, const double* fbar, double* lamOut, d
   const DevModel& M = c->M;
   cudaStream_t st = c->stream;
   const int n = M.n, nt = M.n_tail;
-  k_adj_bonds<double><<<cdiv((long)(n - 1) * kBondChunks, 64), 64, 0, st>>>(M, x, fbar, lamOut, th);
+  if (std::is_same<R, float>::value)
+    k_adj_bonds<double, float, kBondWm><<<cdiv((long)(n - 1) * bond_chunks(kBondWm), 64), 64, 0, st>>>(M, x, fbar,
+                                                                                                    lamOut, th);
+  else
+    k_adj_bonds<double, double, kBondW><<<cdiv((long)(n - 1) * bond_chunks(kBondW), 64), 64, 0, st>>>(M, x, fbar,
+                                                                                                   lamOut, th);
   k_adj_dnadna<R><<<cdiv((long)n * n, 128), 128, 0, st>>>(M, x, fbar, lamOut, th);
   if (M.n_dna > 0) k_adj_dnacore<R><<<M.n_dna * M.n_c, 128, 0, st>>>(M, x, fbar, lamOut, th);
-  k_adj_corecore<R><<<M.n_c * M.n_c, 256, 13 * M.Nq * sizeof(R), st>>>(M, x, fbar, lamOut, th);
+  k_adj_corecore<R><<<dim3(M.n_c * M.n_c, cdiv(M.Nq, kCcThreads)), kCcThreads, 13 * M.Nq * sizeof(R), st>>>(
+      M, x, fbar, lamOut, th);
   L += 4;
   if (nt > 0) {
-    k_adj_tail_bonded<double><<<cdiv(nt, 128), 128, 0, st>>>(M, x, fbar, lamOut);
+    k_adj_tail_bonded<double, R><<<cdiv(nt, 128), 128, 0, st>>>(M, x, fbar, lamOut);
     k_adj_tail_pairs<R><<<cdiv((long)nt * (nt + n), 256), 256, 0, st>>>(M, x, fbar, lamOut, th);
-    k_adj_anchor<double><<<cdiv((long)M.n_c * M.n_t * 2, 64), 64, 0, st>>>(M, x, fbar, lamOut, th);
+    k_adj_anchor<double, R><<<cdiv((long)M.n_c * M.n_t * 2, 64), 64, 0, st>>>(M, x, fbar, lamOut, th);
     L += 3;
   }
   CK(cudaGetLastError());
@@ -994,11 +1029,11 @@ int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs, int slo
   long& L = w.launches;
   // corrector: refresh, rotation, translation
   k_pass1_init<<<cdiv(ns, 256), 256, 0, st>>>(M, w.lam, w.lamZ, ns);
-  k_adj_pass1<double><<<cdiv((long)(n - 1) * kP1Chunks, 64), 64, 0, st>>>(M, Zraw, w.lam, w.lamZ);
+  k_adj_pass1<double, R><<<cdiv((long)(n - 1) * kP1Chunks, 64), 64, 0, st>>>(M, Zraw, w.lam, w.lamZ);
   CK(cudaMemsetAsync(w.lamX, 0, ns * sizeof(double), st));
   CK(cudaMemsetAsync(w.fbA, 0, nf * sizeof(double), st));
   CK(cudaMemsetAsync(w.rdb, 0, mp * sizeof(double), st));
-  k_adj_rotate<double><<<cdiv(n, 64), 64, 0, st>>>(M, xs, Fa + n3, rr, w.lamZ, w.lamX, w.fbA + n3);
+  k_adj_rotate<double, R><<<cdiv(n, 64), 64, 0, st>>>(M, xs, Fa + n3, rr, w.lamZ, w.lamX, w.fbA + n3);
   k_pos_through<<<cdiv(m, 256), 256, 0, st>>>(n, nt, w.lamZ, w.lamX, w.lz, w.rdb);
   k_dblk<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, r_all, w.lz, M.del, w.fbA);
   k_half<<<cdiv(nf, 256), 256, 0, st>>>(nf, w.fbA, w.fb0, w.fb1);
@@ -1007,8 +1042,8 @@ int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs, int slo
   if ((rc = forces_vjp<R>(c, Yref, w.fb1, w.lamYr, w.th, L))) return rc;
   // predictor: refresh, rotation, translation
   k_pass1_init<<<cdiv(ns, 256), 256, 0, st>>>(M, w.lamYr, w.lamY, ns);
-  k_adj_pass1<double><<<cdiv((long)(n - 1) * kP1Chunks, 64), 64, 0, st>>>(M, Yraw, w.lamYr, w.lamY);
-  k_adj_rotate<double><<<cdiv(n, 64), 64, 0, st>>>(M, xs, F0 + n3, rr, w.lamY, w.lamX, w.fb0 + n3);
+  k_adj_pass1<double, R><<<cdiv((long)(n - 1) * kP1Chunks, 64), 64, 0, st>>>(M, Yraw, w.lamYr, w.lamY);
+  k_adj_rotate<double, R><<<cdiv(n, 64), 64, 0, st>>>(M, xs, F0 + n3, rr, w.lamY, w.lamX, w.fb0 + n3);
   k_pos_through<<<cdiv(m, 256), 256, 0, st>>>(n, nt, w.lamY, w.lamX, w.ly, w.rdb);
   k_dblk<R><<<cdiv((long)(n + nt) * 32, 256), 256, 0, st>>>(M, r_all, w.ly, M.del, w.fb0);
   // forces at the state
@@ -1022,12 +1057,13 @@ int reverse_step(bd_ctx* c, bdh::AdjWork& w, int step, const double* xs, int slo
   k_trmv_u<R><<<cdiv((long)mp * 32, 256), 256, 0, st>>>(mp, U, w.rdb, u);
   k_inv_leaf<R><<<mp / 64, 64, 2 * 64 * 65 * sizeof(R), st>>>(mp, U, V);
   int gl = 0;
-  inv_upper<R>(st, mp, U, V, Xt, gl);
+  if (inv_upper<R>(st, mp, U, V, Xt, gl, c->d_err)) return set_error(BD_ERR_CUDA, "bd_adjoint: triangular inverse");
   k_build_xt<R><<<mp, 256, 0, st>>>(m, mp, V, p, u, R(M.s2dt), Xt);
   // D_bar tiles that k_adj_rpy reads (rows, columns < m); beyond m both
   // factors vanish along k (p and u are zero on the padding)
-  const int m64 = (m + 63) / 64 * 64;
-  gemm<R>(st, m64, m64, m64, R(1), V, mp, Xt, mp, Db, mp, true, 3);
+  const int mt = (std::is_same<R, float>::value && mp >= 128) ? (m + 127) / 128 * 128 : (m + 63) / 64 * 64;
+  if (gemm_tc<R>(st, mt, mt, mt, R(1), V, mp, Xt, mp, Db, mp, true, 3, c->d_err))
+    return set_error(BD_ERR_CUDA, "bd_adjoint: D_bar product");
   // the RPY tensor
   k_stack<<<cdiv(m, 256), 256, 0, st>>>(n, nt, Fa, Fa + 2 * n3, w.fa);
   k_stack<<<cdiv(m, 256), 256, 0, st>>>(n, nt, F0, F0 + 2 * n3, w.f0);
@@ -1124,6 +1160,7 @@ int set_leaf_smem() {
   if (done) return BD_OK;
   CK(cudaFuncSetAttribute(k_inv_leaf<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
   CK(cudaFuncSetAttribute(k_inv_leaf<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 4));
+  if (bdk::tc_gemm_attributes()) return set_error(BD_ERR_CUDA, "bd_adjoint: kernel attributes (shared memory)");
   done = true;
   return BD_OK;
 }
