@@ -628,6 +628,12 @@ def run_batch(args):
     for s in range(args.warmup, args.warmup + args.steps):
         b.step([h[s][0] for h in host], [h[s][1] for h in host])
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    # the run with every replica's noise drawn on the device (bd_batch_run_device:
+    # one noise launch per step for all replicas, one host wait at the end)
+    b.run_device(1, 4242)  # creates the generators
+    t0 = time.perf_counter()
+    b.run_device(args.steps, 4242)
+    dev_run_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     h2d = sum((3 * f.sizes["n"] + f.m) * 8 for f in fibers)
     sizes = [f.m for f in fibers]
     # phases of one eager step (timing on: no graph), for the roofline
@@ -663,6 +669,8 @@ def run_batch(args):
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2"},
                 "e2e": {"value": world * len(fibers) / e2e_s, "unit": "replica-steps/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": 8 * len(fibers)},
+                "device_noise_run": {"value": world * len(fibers) / dev_run_s, "unit": "replica-steps/s",
+                                     "api": "bd_batch_run_device (host wall clock over the timed steps)"},
                 "gpu_launches": launches, "clocks": clocks, "roofline": roof, "vs_fp64": vs64,
                 "phases_ms": {"positions+tensors": float(ph[0]), "factorisation": float(ph[1]),
                               "forces+moves": float(ph[2])},

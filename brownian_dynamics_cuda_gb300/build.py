@@ -33,7 +33,7 @@ UNITS = [
     ("k_tc_chol.cu", []),
     ("k_noalloc.cu", ["-fmad=false"]),
     ("k_adjoint.cu", []),
-    ("k_noise.cu", []),
+    ("k_noise.cu", ["-fmad=false"]),
     ("k_krylov.cu", []),
     ("k_tc_gemm.cu", []),
 ]

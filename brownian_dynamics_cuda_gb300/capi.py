@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libbdgb300.so")
 BD_OK, BD_ERR_ARG, BD_ERR_IO, BD_ERR_CUDA, BD_ERR_NOMEM, BD_ERR_NONFINITE, BD_ERR_NOT_SPD, BD_ERR_STATE = range(8)
 PREC_FP64, PREC_MIXED = 0, 1
 NOISE_CHOLESKY, NOISE_KRYLOV = 0, 1
+LOG_LIBM, LOG_CR = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -132,6 +133,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_noise_u32.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]
     L.bd_noise_free.argtypes = [C.c_void_p]
     L.bd_noise_free.restype = None
+    L.bd_noise_set_log.argtypes = [C.c_void_p, C.c_int]
     L.bd_create.argtypes = [C.POINTER(bd_model), C.POINTER(bd_state), C.POINTER(bd_options), C.POINTER(C.c_void_p)]
     L.bd_destroy.argtypes = [C.c_void_p]
     L.bd_sizes.argtypes = [C.c_void_p, _ip]
@@ -145,6 +147,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.bd_batch_step.argtypes = [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp), _dp]
     L.bd_batch_step_device.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
     L.bd_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_ulong, _dp]
+    L.bd_batch_run_device.argtypes = [C.c_void_p, C.c_int, C.c_ulong, _dp]
     L.bd_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.bd_batch_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.bd_set_mixed_passes.argtypes = [C.c_void_p, C.c_int]
@@ -333,10 +336,17 @@ class Fiber:
 class Noise:
     """Reference-order MT19937 + polar Box-Muller noise (host)."""
 
-    def __init__(self, seed: int):
+    def __init__(self, seed: int, log_mode: int = LOG_LIBM):
         self._L = load_library()
         self._h = C.c_void_p()
         _check(self._L.bd_noise_create(seed, C.byref(self._h)))
+        if log_mode != LOG_LIBM:
+            self.set_log(log_mode)
+
+    def set_log(self, mode: int) -> None:
+        """bd_noise_set_log: LOG_LIBM (the C library's log, the reference) or
+        LOG_CR (correctly rounded: the device stream's, bit for bit)."""
+        _check(self._L.bd_noise_set_log(self._h, mode))
 
     def step(self, step: int, r_var: np.ndarray, n_D3: int) -> tuple[np.ndarray, np.ndarray]:
         rr = np.zeros(r_var.size)
@@ -636,6 +646,14 @@ class Batch:
     def run(self, nsteps: int, seed_base: int) -> np.ndarray:
         e = np.zeros(len(self))
         _check(self._L.bd_batch_run(self._h, nsteps, seed_base, _pd(e)))
+        return e
+
+    def run_device(self, nsteps: int, seed_base: int) -> np.ndarray:
+        """bd_batch_run_device: the same run with the noise generated on the
+        device (the correctly rounded log), no host synchronisation between
+        steps."""
+        e = np.zeros(len(self))
+        _check(self._L.bd_batch_run_device(self._h, nsteps, seed_base, _pd(e)))
         return e
 
     def close(self) -> None:

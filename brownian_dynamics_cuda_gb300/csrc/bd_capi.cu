@@ -877,6 +877,7 @@ struct bd_batch {
   cudaGraphExec_t graph = nullptr;
   std::vector<bd_noise*> noise;
   std::vector<std::vector<double>> h_rr, h_p;
+  bdk::NoiseBatch* dnoise = nullptr;  // bd_batch_run_device: every replica's device noise stream
   bdk::MixedBatch* chol = nullptr;  // the replicas' factorisations as one launch per schedule step
   // side streams: the replicas' position / tensor and move phases run on
   // kBatchLanes streams side by side (no tensor-core kernel among them)
@@ -1053,6 +1054,7 @@ extern "C" int bd_batch_destroy(bd_batch* b) {
     if (e) cudaEventDestroy(e);
   for (bd_ctx* c : b->ctx) bd_destroy(c);
   for (bd_noise* g : b->noise) bd_noise_free(g);
+  bdk::noise_batch_free(b->dnoise);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return BD_OK;
@@ -1213,6 +1215,42 @@ extern "C" int bd_batch_run(bd_batch* b, int nsteps, unsigned long seed_base, do
   return BD_OK;
 }
 
+extern "C" int bd_batch_run_device(bd_batch* b, int nsteps, unsigned long seed_base, double* energies) {
+  if (!b || nsteps < 0) return set_error(BD_ERR_ARG, "bd_batch_run_device: bad argument");
+  const int nr = (int)b->ctx.size();
+  if (nr == 0) return BD_OK;
+  for (bd_ctx* c : b->ctx)
+    if (c->step_count != b->ctx[0]->step_count)
+      return set_error(BD_ERR_STATE, "bd_batch_run_device: the replicas are at different steps");
+  if (!b->dnoise) {
+    std::vector<unsigned long> seeds(nr);
+    std::vector<int> n3(nr), nD3(nr);
+    std::vector<const double*> rv(nr);
+    std::vector<double*> rr(nr), p(nr);
+    for (int i = 0; i < nr; i++) {
+      bd_ctx* c = b->ctx[i];
+      if (c->h_rvar.empty()) return set_error(BD_ERR_ARG, "bd_batch_run_device: a replica's model has no r_var");
+      seeds[i] = seed_base + (unsigned long)i;
+      n3[i] = 3 * c->M.n;
+      nD3[i] = c->m;
+      rv[i] = c->h_rvar.data();
+      rr[i] = c->rr;  // the draws land in the contexts' own noise buffers
+      p[i] = c->p;
+    }
+    int rc = bdk::noise_batch_create(nr, seeds.data(), n3.data(), nD3.data(), rv.data(), rr.data(), p.data(),
+                                     &b->dnoise);
+    if (rc) return rc;
+  }
+  // no host synchronisation between steps: the noise launch and the batch
+  // step (one graph with use_graph) of every step are enqueued back to back
+  for (int s = 0; s < nsteps; s++) {
+    int rc = bdk::noise_batch_step(b->dnoise, (int)b->ctx[0]->step_count, b->stream);
+    if (!rc) rc = batch_device_step(b);
+    if (rc) return rc;
+  }
+  return batch_finish(b, energies);
+}
+
 extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double debye_length) {
   if (!c || !(debye_length > 0.0)) return set_error(BD_ERR_ARG, "bd_set_moduli: bad argument");
   if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_moduli: the context belongs to a batch");
@@ -1233,11 +1271,11 @@ extern "C" int bd_set_moduli(bd_ctx* c, double h, double g, double s, double deb
 }
 
 // main.cpp:386-465 changes which cores carry a linker histone every 100
-// steps and with it n_LH and the size of D.  The context is rebuilt for the
-// new binding from its current device state (chain, tails, frames and
-// angles: the reference keeps them on the device, func_cuda.cu:3434-3490)
-// and the caller's LH positions (main.cpp rebuilds them on the host,
-// main.cpp:418-447), then takes the place of the old one.
+// steps and with it n_LH and the size of D.  The chain, tails, frames and
+// angles stay on the device (as the reference keeps them,
+// func_cuda.cu:3434-3490); the caller's LH positions (main.cpp rebuilds them
+// on the host, main.cpp:418-447) and the new binding's tables go into the
+// buffers bd_create sized for every core bound, so nothing is reallocated.
 extern "C" int bd_set_lh_flags(bd_ctx* c, const int* nc_lh_flag, const double* r_lh, const double* lh_rad) {
   if (!c || !nc_lh_flag || !c->model) return set_error(BD_ERR_ARG, "bd_set_lh_flags: null argument");
   if (c->in_batch) return set_error(BD_ERR_STATE, "bd_set_lh_flags: the context belongs to a batch");

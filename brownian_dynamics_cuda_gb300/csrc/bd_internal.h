@@ -37,6 +37,7 @@ struct Mt19937 {
   int idx = 625;
   double cached = 0.0;
   bool have = false;
+  bool cr_log = false;  // polar transform: the C library's log (reference) or the correctly rounded one
   void seed(uint32_t s);
   uint32_t next();
   double real1() { return next() * (1.0 / 4294967295.0); }
@@ -163,6 +164,12 @@ size_t krylov_scratch_doubles(int m, int kmax);
 int tc_gemm_f32(cudaStream_t st, int M, int N, int K, float alpha, const float* A, int lda, const float* B, int ldb,
                 float* C, int ldc, bool tb, int kmode, int batch, long zstride, int* err);
 int tc_gemm_attributes();
+// k_noise.cu: the device noise stream of every replica of a batch, one launch per step
+struct NoiseBatch;
+int noise_batch_create(int nr, const unsigned long* seeds, const int* n3, const int* nD3,
+                       const double* const* h_rvar, double* const* d_rr, double* const* d_p, NoiseBatch** out);
+int noise_batch_step(NoiseBatch* b, int step, cudaStream_t st);
+void noise_batch_free(NoiseBatch* b);
 // A == nullptr: matrix-free products from the double-float position mirror qh/ql
 int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, const float4* ql, double a1, double a2,
                 const double* p, double s2dt, double tol, int kmax, double* rd, double* scratch, cudaStream_t st,

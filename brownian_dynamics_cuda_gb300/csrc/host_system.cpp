@@ -9,6 +9,7 @@
 //   r_var            main.cpp:292-303
 //   out.xyz          readfile.cpp:346-405
 //   noise            mt.cpp (MT19937), utilities.cpp:304-336, main.cpp:386-388,479-486
+#include "cr_log.cuh"
 #include "bd_internal.h"
 
 #include <cmath>
@@ -461,7 +462,7 @@ double Mt19937::normal(double mean, double sd) {
     y = 2.0 * real1() - 1;
     q = x * x + y * y;
   } while (q == 0.0 || q > 1.0);
-  double d = std::sqrt(-2.0 * std::log(q) / q);
+  double d = std::sqrt(-2.0 * (cr_log ? crlog::log_cr(q) : std::log(q)) / q);
   cached = y * d;
   have = true;
   return x * d * sd + mean;
@@ -543,6 +544,12 @@ extern "C" int bd_noise_u32(bd_noise* gp, int count, uint32_t* out) {
 }
 
 extern "C" void bd_noise_free(bd_noise* g) { delete reinterpret_cast<Mt19937*>(g); }
+
+extern "C" int bd_noise_set_log(bd_noise* gp, int mode) {
+  if (!gp || (mode != BD_LOG_LIBM && mode != BD_LOG_CR)) return set_error(BD_ERR_ARG, "bd_noise_set_log: bad argument");
+  reinterpret_cast<Mt19937*>(gp)->cr_log = mode == BD_LOG_CR;
+  return BD_OK;
+}
 
 extern "C" int bd_noise_get_state(const bd_noise* gp, uint32_t* words624, int* index, int* have_cached,
                                   double* cached) {

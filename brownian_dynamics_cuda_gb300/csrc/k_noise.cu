@@ -17,14 +17,18 @@
 //              consumption stops at exactly the pair that completes the
 //              step, whose second deviate becomes the cache.
 // The 32-bit stream and the accept / reject decisions are the host's bit
-// for bit; the deviates agree to the last bit or two (the device log).
+// for bit.  The logarithm is the correctly rounded one of cr_log.cuh, so
+// the deviates equal a host stream set to BD_LOG_CR bit for bit, and the
+// reference's (the C library's log) wherever that log rounds correctly.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "bd_internal.h"
+#include "cr_log.cuh"
 
 using bdh::set_error;
 
@@ -101,8 +105,8 @@ __device__ __forceinline__ void emit(int i, double z, int n3, const double* r_va
   else p[i - n3] = __dadd_rn(__dmul_rn(z, 1.0), 0.0);
 }
 
-__global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n3, const double* __restrict__ r_var,
-                                                        int nD3, double* rr, double* p) {
+__device__ __forceinline__ void mt_noise_body(DevMt* G, int step, int n3, const double* __restrict__ r_var, int nD3,
+                                              double* rr, double* p) {
   __shared__ uint32_t st[kN];
   __shared__ int s_idx, s_have, s_o, s_carry_ok, s_stop;
   __shared__ uint32_t s_carry;
@@ -178,7 +182,7 @@ __global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n
       __syncthreads();
       const int kstop = s_stop;
       if (acc && r < np) {
-        const double d = sqrt(-2.0 * log(q) / q);
+        const double d = sqrt(-2.0 * crlog::log_cr(q) / q);
         const double zx = __dmul_rn(x, d), zy = __dmul_rn(y, d);
         const int i0 = o + 2 * r;
         emit(i0, zx, n3, r_var, rr, p);
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n
       }
     } else {
       if (acc) {
-        const double d = sqrt(-2.0 * log(q) / q);
+        const double d = sqrt(-2.0 * crlog::log_cr(q) / q);
         emit(o + 2 * r, __dmul_rn(x, d), n3, r_var, rr, p);
         emit(o + 2 * r + 1, __dmul_rn(y, d), n3, r_var, rr, p);
       }
@@ -221,14 +225,26 @@ __global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n
   }
 }
 
-}  // namespace
+__global__ void __launch_bounds__(kThreads) k_mt_noise(DevMt* G, int step, int n3, const double* __restrict__ r_var,
+                                                        int nD3, double* rr, double* p) {
+  mt_noise_body(G, step, n3, r_var, nD3, rr, p);
+}
 
-struct bd_dev_noise {
-  DevMt* d = nullptr;
+// one generator per CTA: every replica's step in one launch
+struct NoiseJob {
+  DevMt* G;
+  const double* r_var;
+  double* rr;
+  double* p;
+  int n3, nD3;
 };
 
-extern "C" int bd_dev_noise_create(unsigned long seed, bd_dev_noise** out) {
-  if (!out) return set_error(BD_ERR_ARG, "bd_dev_noise_create: null argument");
+__global__ void __launch_bounds__(kThreads) k_mt_noise_multi(const NoiseJob* __restrict__ jobs, int step) {
+  const NoiseJob j = jobs[blockIdx.x];
+  mt_noise_body(j.G, step, j.n3, j.r_var, j.nD3, j.rr, j.p);
+}
+
+DevMt seeded(unsigned long seed) {
   bdh::Mt19937 h;
   h.seed((uint32_t)(seed & 0xffffffffUL));
   DevMt m;
@@ -236,6 +252,77 @@ extern "C" int bd_dev_noise_create(unsigned long seed, bd_dev_noise** out) {
   m.idx = h.idx >= kN ? kN : h.idx;
   m.have = 0;
   m.cached = 0.0;
+  return m;
+}
+
+}  // namespace
+
+// Noise of a whole batch: generator i seeded seeds[i] writes n3[i] scaled
+// rotational draws into d_rr[i] and nD3[i] translational ones into d_p[i]
+// (the replica contexts' own noise buffers), all in one launch per step.
+struct bdk::NoiseBatch {
+  int nr = 0;
+  DevMt* G = nullptr;
+  NoiseJob* jobs = nullptr;
+  double* rvar = nullptr;
+};
+
+int bdk::noise_batch_create(int nr, const unsigned long* seeds, const int* n3, const int* nD3,
+                            const double* const* h_rvar, double* const* d_rr, double* const* d_p, NoiseBatch** out) {
+  NoiseBatch* b = new NoiseBatch();
+  b->nr = nr;
+  size_t nv = 0;
+  for (int i = 0; i < nr; i++) nv += (size_t)n3[i];
+  std::vector<DevMt> g(nr);
+  for (int i = 0; i < nr; i++) g[i] = seeded(seeds[i]);
+  std::vector<NoiseJob> jobs(nr);
+  std::vector<double> rv(nv);
+  cudaError_t e = cudaMalloc(&b->G, nr * sizeof(DevMt));
+  if (e == cudaSuccess) e = cudaMalloc(&b->jobs, nr * sizeof(NoiseJob));
+  if (e == cudaSuccess && nv) e = cudaMalloc(&b->rvar, nv * sizeof(double));
+  if (e != cudaSuccess) {
+    noise_batch_free(b);
+    return set_error(BD_ERR_NOMEM, "noise batch: cudaMalloc failed");
+  }
+  size_t o = 0;
+  for (int i = 0; i < nr; i++) {
+    std::memcpy(rv.data() + o, h_rvar[i], n3[i] * sizeof(double));
+    jobs[i] = NoiseJob{b->G + i, b->rvar + o, d_rr[i], d_p[i], n3[i], nD3[i]};
+    o += (size_t)n3[i];
+  }
+  e = cudaMemcpy(b->G, g.data(), nr * sizeof(DevMt), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->jobs, jobs.data(), nr * sizeof(NoiseJob), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && nv) e = cudaMemcpy(b->rvar, rv.data(), nv * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    noise_batch_free(b);
+    return set_error(BD_ERR_CUDA, "noise batch: upload failed");
+  }
+  *out = b;
+  return BD_OK;
+}
+
+int bdk::noise_batch_step(NoiseBatch* b, int step, cudaStream_t st) {
+  if (!b || b->nr == 0) return BD_OK;
+  k_mt_noise_multi<<<b->nr, kThreads, 0, st>>>(b->jobs, step);
+  CK(cudaGetLastError());
+  return BD_OK;
+}
+
+void bdk::noise_batch_free(NoiseBatch* b) {
+  if (!b) return;
+  if (b->G) cudaFree(b->G);
+  if (b->jobs) cudaFree(b->jobs);
+  if (b->rvar) cudaFree(b->rvar);
+  delete b;
+}
+
+struct bd_dev_noise {
+  DevMt* d = nullptr;
+};
+
+extern "C" int bd_dev_noise_create(unsigned long seed, bd_dev_noise** out) {
+  if (!out) return set_error(BD_ERR_ARG, "bd_dev_noise_create: null argument");
+  const DevMt m = seeded(seed);
   bd_dev_noise* g = new bd_dev_noise();
   cudaError_t e = cudaMalloc(&g->d, sizeof(DevMt));
   if (e != cudaSuccess) {

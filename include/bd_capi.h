@@ -152,6 +152,15 @@ int bd_noise_create(unsigned long seed, bd_noise** out);
 int bd_noise_step(bd_noise* g, int step, int n3, const double* r_var, int n_D3, double* rr, double* p);
 int bd_noise_u32(bd_noise* g, int count, uint32_t* out);
 void bd_noise_free(bd_noise* g);
+/* The logarithm of the polar transform.  BD_LOG_LIBM (the default): the C
+ * library's log, as the reference (utilities.cpp:304-336) - glibc's is
+ * not correctly rounded (on ~1 in 1,400 of the transform's arguments it
+ * differs from the correctly rounded value by one ulp), and its results may differ between machines.
+ * BD_LOG_CR: a correctly rounded log (double-double atanh series), the one
+ * the device stream (bd_dev_noise_*) uses, so the two streams are equal
+ * bit for bit on every machine.  No counterpart in the reference. */
+enum { BD_LOG_LIBM = 0, BD_LOG_CR = 1 };
+int bd_noise_set_log(bd_noise* g, int mode);
 /* The step's pieces separately, for a driver that runs the LH binding Monte
  * Carlo between them (bd_lh_mc): `count` uniforms genrand_real1 as main.cpp
  * draws them on steps with step % 100 == 0 (main.cpp:387-388), then the
@@ -195,8 +204,10 @@ int bd_restart_read(const char* path, bd_restart* rs, bd_noise* g);
  * arrays d_rr [n3] (scaled by d_r_var) and d_p [n_D3], stream-ordered on
  * `stream` (a cudaStream_t, NULL for the legacy stream).  The 32-bit words
  * and the polar method's accept / reject decisions are those of
- * bd_noise_step bit for bit; the deviates agree with the host's to the last
- * bit or two (the device log). */
+ * bd_noise_step bit for bit; the deviates equal those of a host stream set
+ * to BD_LOG_CR bit for bit (the device log is the correctly rounded one),
+ * and the reference's (the C library's log) except where that log rounds
+ * differently (one ulp, ~1 in 1,400 of the polar transform's arguments). */
 typedef struct bd_dev_noise bd_dev_noise;
 int bd_dev_noise_create(unsigned long seed, bd_dev_noise** out);
 int bd_dev_noise_step(bd_dev_noise* g, int step, int n3, const double* d_r_var, int n_D3, double* d_rr, double* d_p,
@@ -349,6 +360,13 @@ int bd_batch_step_device(bd_batch* b, const double* const* d_rr, const double* c
  * seed_base + i, draws as main.cpp:479-486); energies as bd_batch_step after
  * the last step. */
 int bd_batch_run(bd_batch* b, int nsteps, unsigned long seed_base, double* energies);
+/* The same run with each replica's stream generated on the device (the
+ * bd_dev_noise_* stream, seeded seed_base + i; one launch per step for all
+ * replicas, the draws written straight into the replicas' noise buffers):
+ * nothing is copied from the host and the host does not wait between
+ * steps; equal bit for bit to bd_batch_run with host streams set to
+ * BD_LOG_CR.  energies as bd_batch_run.  No counterpart in the reference. */
+int bd_batch_run_device(bd_batch* b, int nsteps, unsigned long seed_base, double* energies);
 
 /* Timing of the last step's phases on the device (ms): rpy chol rd forces1
  * update1 frames forces2 update2 total.  Valid after a step with use_graph=0. */

@@ -43,3 +43,24 @@ def test_batch_run_uses_per_replica_streams(replicas):
             ei = c.step(*g.step(step, f.arrays["r_var"], f.m))
         assert ei == e[i]
         assert np.array_equal(c.get("r"), b.contexts[i].get("r"))
+
+
+def test_batch_run_device_noise(replicas):
+    """bd_batch_run_device: each replica's noise generated on the device,
+    one launch for all, no host wait between steps - equal bit for bit to
+    the host-noise run with every stream set to the correctly rounded log,
+    and to single contexts driven by such host streams."""
+    from brownian_dynamics_cuda_gb300 import LOG_CR, Batch, Context, Noise
+    bd = Batch(replicas, precision=1, use_graph=True)
+    e = bd.run_device(3, 900)
+    for i, f in enumerate(replicas):
+        c = Context(f, precision=1)
+        g = Noise(900 + i, log_mode=LOG_CR)
+        for step in range(3):
+            ei = c.step(*g.step(step, f.arrays["r_var"], f.m))
+        assert ei == e[i], i
+        for k in ("r", "a", "r_t"):
+            assert np.array_equal(c.get(k), bd.contexts[i].get(k)), (i, k)
+    # continues from where it stopped, with the generators' state kept
+    e2 = bd.run_device(1, 900)
+    assert np.all(np.isfinite(e2))
