@@ -554,8 +554,20 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
 #ifndef BD_EPI_AHEAD
 #define BD_EPI_AHEAD 8  // chunks of 8 columns whose old values are in flight per epilogue thread (4: 8 % slower bulk)
 #endif
+#ifndef BD_EPI_TMEM_COLS
+#define BD_EPI_TMEM_COLS 8  // accumulator columns per TMEM read of the bulk epilogue (8, 16 or 32)
+#endif
 #ifndef BD_REST_GROUP
 #define BD_REST_GROUP 0  // tiles per CTA; 0: from the tile count
+#endif
+#ifndef BD_REST_WAVES
+#define BD_REST_WAVES 3  // from the tile count: about this many CTAs per SM ...
+#endif
+#ifndef BD_REST_GMIN
+#define BD_REST_GMIN 1  // ... with at least / at most this many tiles each
+#endif
+#ifndef BD_REST_GMAX
+#define BD_REST_GMAX 8
 #endif
 constexpr int kRestThreads = 320;
 constexpr int kStageBytes = kTileSlices * kHalfBytes;  // one K-half of the three B slices
@@ -881,16 +893,24 @@ __device__ __forceinline__ void rest_body(unsigned char* smraw, float2* A, int l
       }
       sm100::tc_fence_after();
       const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * kAccCols + 64 * ch);
+      // the accumulator is read kEpT columns at a time (one wait per read)
+      constexpr int kEpT = BD_EPI_TMEM_COLS, kEpR = kEpT / kEpC;
+      static_assert(kEpT % kEpC == 0 && kEpN % kEpR == 0, "TMEM reads cover whole chunks");
+      float vt[kEpT];
 #pragma unroll
       for (int c = 0; c < kEpN; c++) {
         const int s2 = c % kEpS;
-        float v[kEpC];
-        sm100::tmem_ld8(ta + kEpC * c, v);
-        if (c == kEpN - 1) {  // accumulator read out: hand it back to the MMA issuer
-          sm100::tc_fence_before();
-          __syncwarp();
-          if (lane == 0) sm100::mbar_arrive(&bars->accEmpty[acc]);
+        if (c % kEpR == 0) {
+          if (kEpT == 8) sm100::tmem_ld8(ta + kEpC * c, vt);
+          else if (kEpT == 16) sm100::tmem_ld16(ta + kEpC * c, vt);
+          else sm100::tmem_ld32(ta + kEpC * c, vt);
+          if (c + kEpR == kEpN) {  // accumulator read out: hand it back to the MMA issuer
+            sm100::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) sm100::mbar_arrive(&bars->accEmpty[acc]);
+          }
         }
+        const float* v = vt + kEpC * (c % kEpR);
 #pragma unroll
         for (int j = 0; j < kEpC; j++)
           if (kEpC * c + j < jcnt) st_tile(colp + (size_t)(kEpC * c + j) * lda, df_sub(old[s2][j], v[j]));
@@ -1034,8 +1054,8 @@ static int rest_group(int tiles) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  int g = tiles / (3 * sms);
-  return g < 1 ? 1 : (g > 8 ? 8 : g);
+  int g = tiles / (BD_REST_WAVES * sms);
+  return g < BD_REST_GMIN ? BD_REST_GMIN : (g > BD_REST_GMAX ? BD_REST_GMAX : g);
 }
 
 // Right-looking with a lookahead of one panel, on one stream, no two kernels

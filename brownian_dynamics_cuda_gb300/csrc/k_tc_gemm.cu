@@ -153,13 +153,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     unsigned char* sb = sa + 3 * kSlice;
     const ChunkRegs cur = nxt;
     if (k0 + kGC < ke) load_chunk<TB>(nxt, A, lda, B, ldb, r0, c0, k0 + kGC, tid);
-    if (it >= 2 && tid == 0)  // stage s free: the MMAs of chunk it - 2 are done
-      if (!sm100::mbar_wait(&bars[s], ((it >> 1) - 1) & 1, kGemmWait)) *abortf = 1;
-    __syncthreads();
-    if (*abortf) break;
-    store_chunk<TB>(cur, sa, sb, tid);
+    // stage s free once the MMAs of chunk it - 2 are done: every thread
+    // waits on the stage barrier itself; one that gives up writes nothing,
+    // and the CTA leaves together after the barrier below
+    bool ok = true;
+    if (it >= 2) ok = sm100::mbar_wait(&bars[s], ((it >> 1) - 1) & 1, kGemmWait);
+    if (ok) store_chunk<TB>(cur, sa, sb, tid);
+    else *abortf = 1;
     sm100::fence_proxy_async();  // the slices, written by the threads, are read by the tensor cores
     __syncthreads();
+    if (*abortf) break;
     if (tid == 0) {
       sm100::tc_fence_after();
 #pragma unroll
