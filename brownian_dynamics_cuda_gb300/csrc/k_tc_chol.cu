@@ -1220,6 +1220,9 @@ int potrf_mixed(int m, double* A64, int lda, unsigned char* PS, int* negpiv, int
 // step i of every factorisation whose schedule has one, each in its own CTA
 // range; the step arguments and CTA offsets of every launch are uploaded
 // once (the matrices and buffers do not move).
+#ifndef BD_BATCH_ALIGN
+#define BD_BATCH_ALIGN 0
+#endif
 struct MixedBatch {
   std::vector<int> nrep_at, grid_at;
   std::vector<size_t> args_at, off_at;
@@ -1254,10 +1257,13 @@ MixedBatch* mixed_batch_create(int nrep, const int* m, double* const* A, const i
     b->off_at.push_back(off.size());
     int n = 0, total = 0;
     for (int r = 0; r < nrep; r++) {
-      if (i >= plans[r].size()) continue;
-      args.push_back(plans[r][i].first);
+      // replica r's schedule starts at launch `shift` (BD_BATCH_ALIGN 1: every
+      // schedule ends with the last launch; 0: every one starts with the first)
+      const size_t shift = BD_BATCH_ALIGN ? steps - plans[r].size() : 0;
+      if (i < shift || i - shift >= plans[r].size()) continue;
+      args.push_back(plans[r][i - shift].first);
       off.push_back(total);
-      total += plans[r][i].second;
+      total += plans[r][i - shift].second;
       n++;
     }
     off.push_back(total);
