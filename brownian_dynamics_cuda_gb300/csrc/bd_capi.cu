@@ -890,7 +890,10 @@ struct bd_batch {
   int launches = 0;  // kernel launches of the last batch step enqueued
 };
 
-constexpr int kBatchLanes = 64;
+#ifndef BD_BATCH_LANES
+#define BD_BATCH_LANES 64
+#endif
+constexpr int kBatchLanes = BD_BATCH_LANES;
 
 // One step of every replica.  Mixed precision, D rebuilt every step: the
 // positions and tensors of all replicas, then one batched factorisation
