@@ -181,7 +181,8 @@ static int step_phases(bd_ctx* c, const double* d_rr, const double* d_p, double*
   record(c, 2);
   if (krylov) {
     rc = bdk::krylov_sqrt(c->m, mixed ? nullptr : c->A, c->lda, mixed, c->S.qh, c->S.ql, M.a1, M.a2, d_p, M.s2dt,
-                          c->krylov_tol, c->krylov_kmax, c->rd, c->kscratch, st, &c->krylov_iters, &c->krylov_change);
+                          c->krylov_tol, c->krylov_kmax, c->rd, c->kscratch, st, &c->krylov_iters, &c->krylov_change,
+                          &c->kgraphs);
     if (rc) return set_error(rc, "bd_step: Krylov noise displacement failed");
     L += 10 * c->krylov_iters + 4;
   } else {
@@ -553,6 +554,7 @@ extern "C" int bd_destroy(bd_ctx* c) {
   if (c->A) cudaFree(c->A);
   if (c->PS) cudaFree(c->PS);
   if (c->d_err) cudaFree(c->d_err);
+  c->kgraphs.clear();
   if (c->kscratch) cudaFree(c->kscratch);
   if (c->arena_base) cudaFree(c->arena_base);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -732,7 +734,7 @@ extern "C" int bd_noise_displacement(bd_ctx* c, const double* p, double* rd) {
     CK(cudaMemcpyAsync(c->p, p, (size_t)c->m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     int rc = bdk::krylov_sqrt(c->m, mixed ? nullptr : c->A, c->lda, mixed, c->S.qh, c->S.ql, c->M.a1, c->M.a2, c->p,
                               c->M.s2dt, c->krylov_tol, c->krylov_kmax, c->rd, c->kscratch, c->stream,
-                              &c->krylov_iters, &c->krylov_change);
+                              &c->krylov_iters, &c->krylov_change, &c->kgraphs);
     if (rc) return set_error(rc, "bd_noise_displacement: Krylov iteration failed");
   } else {
     int rc = factor_now(c);
@@ -1077,6 +1079,7 @@ extern "C" int bd_set_noise_mode(bd_ctx* c, int mode, double tol, int kmax) {
   CK(cudaStreamSynchronize(c->stream));
   if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
   if (mode == BD_NOISE_KRYLOV && (!c->kscratch || kmax > c->krylov_kmax)) {
+    c->kgraphs.clear();
     if (c->kscratch) cudaFree(c->kscratch), c->kscratch = nullptr;
     if (cudaMalloc((void**)&c->kscratch, bdk::krylov_scratch_doubles(c->m_cap, kmax) * sizeof(double)) != cudaSuccess)
       return set_error(BD_ERR_NOMEM, "bd_set_noise_mode: Krylov workspace allocation failed");

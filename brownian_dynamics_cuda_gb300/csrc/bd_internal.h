@@ -171,9 +171,25 @@ int noise_batch_create(int nr, const unsigned long* seeds, const int* n3, const 
 int noise_batch_step(NoiseBatch* b, int step, cudaStream_t st);
 void noise_batch_free(NoiseBatch* b);
 // A == nullptr: matrix-free products from the double-float position mirror qh/ql
+// the Lanczos iterations of a context, kCheck at a time, as CUDA graphs
+// (valid while the context's sizes, scratch and tensor pointer stay)
+struct KrylovGraphs {
+  int m = -1, kmax = -1;
+  const double* scratch = nullptr;
+  const double* A = nullptr;
+  bool df = false;
+  double a1 = 0.0, a2 = 0.0;
+  std::vector<cudaGraphExec_t> blocks;
+  void clear() {
+    for (cudaGraphExec_t g : blocks)
+      if (g) cudaGraphExecDestroy(g);
+    blocks.clear();
+  }
+  ~KrylovGraphs() { clear(); }
+};
 int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, const float4* ql, double a1, double a2,
                 const double* p, double s2dt, double tol, int kmax, double* rd, double* scratch, cudaStream_t st,
-                int* iters, double* change);
+                int* iters, double* change, struct KrylovGraphs* graphs = nullptr);
 int mixed_max_launches(int m);  // k_chol_step launches of one factorisation, at most
 // Many mixed factorisations (replicas) advanced together: launch i runs step
 // i of every factorisation's schedule (k_chol_step_multi), then one diagonal
@@ -219,6 +235,7 @@ struct bd_ctx {
   int krylov_kmax = 64, krylov_iters = 0;
   double krylov_change = 0.0;
   double* kscratch = nullptr;
+  bdk::KrylovGraphs kgraphs;  // the Lanczos iteration blocks, captured on first use
   bool a_holds_factor = false;  // A holds L (after a factorisation), not D
   bool need_rebuild = false;    // the next step assembles D whatever frequency_RP says (after a resize)
   long step_count = 0;

@@ -119,15 +119,28 @@ __global__ void k_symv_sum(int m, int nt, const double* __restrict__ P, double* 
 // to x_j; runs of 32 terms in FP32, the runs added with Kahan compensation;
 // lanes summed in FP64 in a fixed order.
 constexpr int kMvTile = 256;
-__global__ void __launch_bounds__(256) k_rpy_mv(int nD, const float4* __restrict__ qh, const float4* __restrict__ ql,
+constexpr int kMvB = 2;   // beads per warp: each staged bead j serves both
+constexpr int kMvW = 8;   // warps per CTA (4 measured slower: the staging is per CTA)
+__global__ void __launch_bounds__(32 * kMvW) k_rpy_mv(int nD, const float4* __restrict__ qh, const float4* __restrict__ ql,
                                                 const float4* __restrict__ xf, float a1f, float a2f,
                                                 double* __restrict__ y) {
   __shared__ float4 sh[kMvTile], sl[kMvTile], sx[kMvTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int i = blockIdx.x * 8 + warp;
-  const bool active = i < nD;
-  const float4 hi_i = active ? qh[i] : make_float4(0.f, 0.f, 0.f, 1.f), lo_i = active ? ql[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float run[3] = {0.f, 0.f, 0.f}, ks[3] = {0.f, 0.f, 0.f}, kc[3] = {0.f, 0.f, 0.f};
+  const int i0 = (blockIdx.x * kMvW + warp) * kMvB;
+  float4 hi[kMvB], lo[kMvB];
+  bool act[kMvB];
+#pragma unroll
+  for (int b = 0; b < kMvB; b++) {
+    const int i = i0 + b;
+    act[b] = i < nD;
+    hi[b] = act[b] ? qh[i] : make_float4(0.f, 0.f, 0.f, 1.f);
+    lo[b] = act[b] ? ql[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  float run[kMvB][3], ks[kMvB][3], kc[kMvB][3];
+#pragma unroll
+  for (int b = 0; b < kMvB; b++)
+#pragma unroll
+    for (int q = 0; q < 3; q++) run[b][q] = ks[b][q] = kc[b][q] = 0.f;
   int cnt = 0;
   for (int base = 0; base < nD; base += kMvTile) {
     __syncthreads();
@@ -137,63 +150,80 @@ __global__ void __launch_bounds__(256) k_rpy_mv(int nD, const float4* __restrict
       sx[t] = xf[base + t];
     }
     __syncthreads();
-    if (!active) continue;
+    if (!act[0]) continue;  // warp-uniform: the warp's first bead is past the end
     const int je = min(nD, base + kMvTile);
     for (int j = base + lane; j < je; j += 32) {
       const int t = j - base;
-      const float4 v = sx[t];
-      if (j == i) {
-        const float d = a1f / hi_i.w;
-        run[0] += d * v.x;
-        run[1] += d * v.y;
-        run[2] += d * v.z;
-      } else {
-        const float4 hj = sh[t], lj = sl[t];
-        float Db[3][3];
-        rpy_block_f((hi_i.x - hj.x) + (lo_i.x - lj.x), (hi_i.y - hj.y) + (lo_i.y - lj.y),
-                    (hi_i.z - hj.z) + (lo_i.z - lj.z), hi_i.w, hj.w, a1f, a2f, Db);
-        run[0] += Db[0][0] * v.x + Db[0][1] * v.y + Db[0][2] * v.z;
-        run[1] += Db[1][0] * v.x + Db[1][1] * v.y + Db[1][2] * v.z;
-        run[2] += Db[2][0] * v.x + Db[2][1] * v.y + Db[2][2] * v.z;
+      const float4 v = sx[t], hj = sh[t], lj = sl[t];
+#pragma unroll
+      for (int b = 0; b < kMvB; b++) {
+        if (j == i0 + b) {
+          const float d = a1f / hi[b].w;
+          run[b][0] += d * v.x;
+          run[b][1] += d * v.y;
+          run[b][2] += d * v.z;
+          continue;
+        }
+        // the RPY block of the pair applied to v without forming it:
+        // D v = c_d v + w s (s . v)
+        const float sxv = (hi[b].x - hj.x) + (lo[b].x - lj.x), syv = (hi[b].y - hj.y) + (lo[b].y - lj.y),
+                    szv = (hi[b].z - hj.z) + (lo[b].z - lj.z);
+        const float ssq = sxv * sxv + syv * syv + szv * szv;
+        const float inv_s = rsqrtf(ssq);
+        const float sd = ssq * inv_s;
+        const float ri = hi[b].w, rj = hj.w;
+        float cd, w;
+        if (sd >= ri + rj) {
+          const float inv_ssq = inv_s * inv_s;
+          const float f = (ri * ri + rj * rj) * inv_ssq;
+          const float as = a2f * inv_s;
+          cd = as * (1.f + f * (1.f / 3.f));
+          w = as * (1.f - f) * inv_ssq;
+        } else {
+          const float se = cbrtf((ri * ri * ri + rj * rj * rj) / 2.f);
+          const float as = a1f / se;
+          cd = as * (1.f - 9.f * sd / (32.f * se));
+          w = as * 3.f / (32.f * se * sd);
+        }
+        const float sv = w * (sxv * v.x + syv * v.y + szv * v.z);
+        run[b][0] += cd * v.x + sxv * sv;
+        run[b][1] += cd * v.y + syv * sv;
+        run[b][2] += cd * v.z + szv * sv;
       }
       if (++cnt == 32) {
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const float u = run[q] - kc[q], t2 = ks[q] + u;
-          kc[q] = (t2 - ks[q]) - u;
-          ks[q] = t2;
-          run[q] = 0.f;
-        }
+        for (int b = 0; b < kMvB; b++)
+#pragma unroll
+          for (int q = 0; q < 3; q++) {
+            const float u = run[b][q] - kc[b][q], t2 = ks[b][q] + u;
+            kc[b][q] = (t2 - ks[b][q]) - u;
+            ks[b][q] = t2;
+            run[b][q] = 0.f;
+          }
         cnt = 0;
       }
     }
   }
-  if (!active) return;
-  double sum[3];
 #pragma unroll
-  for (int q = 0; q < 3; q++) {
-    const float u = run[q] - kc[q], t2 = ks[q] + u;
-    sum[q] = (double)t2 - (double)((t2 - ks[q]) - u);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int b = 0; b < kMvB; b++) {
+    double sum[3];
 #pragma unroll
-    for (int q = 0; q < 3; q++) sum[q] = sum[q] + __shfl_xor_sync(0xffffffffu, sum[q], o);
-  }
-  if (lane == 0) {
-    y[3 * i] = sum[0];
-    y[3 * i + 1] = sum[1];
-    y[3 * i + 2] = sum[2];
+    for (int q = 0; q < 3; q++) {
+      const float u = run[b][q] - kc[b][q], t2 = ks[b][q] + u;
+      sum[q] = (double)t2 - (double)((t2 - ks[b][q]) - u);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) sum[q] = sum[q] + __shfl_xor_sync(0xffffffffu, sum[q], o);
+    }
+    if (act[b] && lane == 0) {
+      const int i = i0 + b;
+      y[3 * i] = sum[0];
+      y[3 * i + 1] = sum[1];
+      y[3 * i + 2] = sum[2];
+    }
   }
 }
-
-// x (3 nD doubles) as float4 per bead
-__global__ void k_to_f4(int nD, const double* __restrict__ x, float4* __restrict__ xf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nD) xf[i] = make_float4((float)x[3 * i], (float)x[3 * i + 1], (float)x[3 * i + 2], 0.f);
-}
-
-// dst[0] = src[0] (a device scalar kept for the host's batched read-back)
-__global__ void k_keep(const double* __restrict__ src, double* __restrict__ dst) { dst[0] = src[0]; }
 
 // partial dot products of the first ncol basis vectors with w, per block;
 // out[col * nb + block]
@@ -215,32 +245,6 @@ __global__ void __launch_bounds__(kDotB) k_dots(int m, const double* __restrict_
   }
 }
 
-// h[col] = sum over blocks of the partials (fixed order)
-__global__ void k_dots_sum(int ncol, int nb, const double* __restrict__ part, double* __restrict__ h) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  double t = 0.0;
-  for (int b = 0; b < nb; b++) t += part[(size_t)col * nb + b];
-  h[col] = t;
-}
-
-// w -= sum_{l < ncol} h[l] V_l   (h on the device)
-__global__ void k_sub_proj(int m, const double* __restrict__ V, int ncol, const double* __restrict__ h,
-                           double* __restrict__ w) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= m) return;
-  double s = w[r];
-  for (int l = 0; l < ncol; l++) s -= h[l] * V[(size_t)l * m + r];
-  w[r] = s;
-}
-
-// v = w / |w| (the norm read on the device)
-__global__ void k_scale(int m, const double* __restrict__ w, const double* __restrict__ nrm, double* __restrict__ v) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= m) return;
-  v[r] = w[r] / nrm[0];
-}
-
 // y = s sum_l c[l] V_l
 __global__ void k_combine(int m, const double* __restrict__ V, int ncol, const double* __restrict__ c, double s,
                           double* __restrict__ y) {
@@ -251,11 +255,54 @@ __global__ void k_combine(int m, const double* __restrict__ V, int ncol, const d
   y[r] = s * t;
 }
 
-// |w| from the partial sums of w . w
-__global__ void k_norm_from(int nb, const double* __restrict__ part, double* __restrict__ out) {
-  double t = 0.0;
-  for (int b = 0; b < nb; b++) t += part[b];
-  out[0] = sqrt(t);
+// w -= sum_{l < ncol} h_l V_l with h_l the fixed-order sums of k_dots'
+// partials (block 0, 1, ...), formed by every block into shared memory;
+// block 0 also stores h_{ncol-1} in *alpha when alpha is given
+constexpr int kProjMax = 520;
+__global__ void __launch_bounds__(128) k_sub_proj_sum(int m, const double* __restrict__ V, int ncol, int nb,
+                                                      const double* __restrict__ part, double* __restrict__ w,
+                                                      double* __restrict__ alpha) {
+  __shared__ double hs[kProjMax];
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
+    double t = 0.0;
+    for (int b = 0; b < nb; b++) t += part[(size_t)col * nb + b];
+    hs[col] = t;
+  }
+  __syncthreads();
+  if (alpha && blockIdx.x == 0 && threadIdx.x == 0) alpha[0] = hs[ncol - 1];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  double s = w[r];
+  for (int l = 0; l < ncol; l++) s -= hs[l] * V[(size_t)l * m + r];
+  w[r] = s;
+}
+
+// |w| from k_dots' partials (fixed order, in every block), kept in *nrm
+// and *beta; then, unless v is null, v = w / |w| and, for matrix-free
+// products, its float4 copy per bead (three rows per thread)
+__global__ void __launch_bounds__(256) k_norm_scale(int nD, int nb, const double* __restrict__ part,
+                                                    const double* __restrict__ w, double* __restrict__ nrm,
+                                                    double* __restrict__ beta, double* __restrict__ v,
+                                                    float4* __restrict__ xf) {
+  __shared__ double sn;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < nb; b++) t += part[b];
+    sn = sqrt(t);
+    if (blockIdx.x == 0) {
+      nrm[0] = sn;
+      if (beta) beta[0] = sn;
+    }
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!v || i >= nD) return;
+  const double n = sn;
+  const double x = w[3 * i] / n, yv = w[3 * i + 1] / n, z = w[3 * i + 2] / n;
+  v[3 * i] = x;
+  v[3 * i + 1] = yv;
+  v[3 * i + 2] = z;
+  if (xf) xf[i] = make_float4((float)x, (float)yv, (float)z, 0.f);
 }
 
 // Eigenvalues and eigenvectors of a symmetric tridiagonal matrix (diagonal d,
@@ -346,7 +393,7 @@ size_t krylov_scratch_doubles(int m, int kmax) {
 constexpr int kCheck = 8;
 int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, const float4* ql, double a1, double a2,
                 const double* p, double s2dt, double tol, int kmax, double* rd, double* scratch, cudaStream_t st,
-                int* iters, double* change) {
+                int* iters, double* change, KrylovGraphs* graphs) {
   const int nt = cdivk(m, kKT), nD = m / 3;
   const int nb = std::min(cdivk(m, kDotB), 64);
   double* V = scratch;
@@ -362,24 +409,22 @@ int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, cons
   float4* xf = reinterpret_cast<float4*>(scratch + xoff);
   const int tb = 256, gm = cdivk(m, tb);
   const long tiles = (long)nt * (nt + 1) / 2;
-  auto dots = [&](int ncol, const double* x) {  // h[0..ncol) = V_l . x
-    k_dots<<<dim3(nb, ncol), kDotB, 0, st>>>(m, V, ncol, x, part);
-    k_dots_sum<<<cdivk(ncol, 128), 128, 0, st>>>(ncol, nb, part, h);
-  };
+  if (kmax + 1 > kProjMax) return BD_ERR_ARG;
+  float4* xfm = A ? nullptr : xf;  // the float4 copy of v_k that matrix-free products read
+  const int gb = cdivk(nD, tb);
+  // x = V_k: its float4 copy (matrix-free) was written with it by k_norm_scale
   auto product = [&](const double* x, double* y) {
     if (A) {
       if (df) k_symv_tiles<true><<<(unsigned)tiles, kKB, 0, st>>>(m, nt, A, lda, x, P);
       else k_symv_tiles<false><<<(unsigned)tiles, kKB, 0, st>>>(m, nt, A, lda, x, P);
       k_symv_sum<<<gm, tb, 0, st>>>(m, nt, P, y);
     } else {
-      k_to_f4<<<cdivk(nD, tb), tb, 0, st>>>(nD, x, xf);
-      k_rpy_mv<<<cdivk(nD, 8), 256, 0, st>>>(nD, qh, ql, xf, (float)a1, (float)a2, y);
+      k_rpy_mv<<<cdivk(nD, kMvW * kMvB), 32 * kMvW, 0, st>>>(nD, qh, ql, xf, (float)a1, (float)a2, y);
     }
   };
   // v_0 = p / |p|
   k_dots<<<dim3(nb, 1), kDotB, 0, st>>>(m, p, 1, p, part);
-  k_norm_from<<<1, 1, 0, st>>>(nb, part, nrm);
-  k_scale<<<gm, tb, 0, st>>>(m, p, nrm, V);
+  k_norm_scale<<<gb, tb, 0, st>>>(nD, nb, part, p, nrm, nullptr, V, xfm);
   double pn = 0.0;
   if (cudaMemcpyAsync(&pn, nrm, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
@@ -391,19 +436,55 @@ int krylov_sqrt(int m, const double* A, int lda, bool df, const float4* qh, cons
     return BD_OK;
   }
   std::vector<double> al, be, c, cprev, hal(kmax + 2), hbe(kmax + 2);
-  int done = -1;
-  for (int k = 0; k < kmax && done < 0; k++) {
+  // one Lanczos iteration in seven launches: the product, twice the
+  // projections on the basis so far (alpha_k from the first), the norm with
+  // v_{k+1} = w / |w| (and its float4 copy)
+  auto iteration = [&](int k) {
     product(V + (size_t)k * m, w);
-    for (int pass = 0; pass < 2; pass++) {  // alpha_k and the projections on the basis so far, twice
-      dots(k + 1, w);
-      if (pass == 0) k_keep<<<1, 1, 0, st>>>(h + k, alpha + k);
-      k_sub_proj<<<gm, tb, 0, st>>>(m, V, k + 1, h, w);
+    for (int pass = 0; pass < 2; pass++) {
+      k_dots<<<dim3(nb, k + 1), kDotB, 0, st>>>(m, V, k + 1, w, part);
+      k_sub_proj_sum<<<cdivk(m, 128), 128, 0, st>>>(m, V, k + 1, nb, part, w, pass == 0 ? alpha + k : nullptr);
     }
     k_dots<<<dim3(nb, 1), kDotB, 0, st>>>(m, w, 1, w, part);
-    k_norm_from<<<1, 1, 0, st>>>(nb, part, nrm);
-    k_keep<<<1, 1, 0, st>>>(nrm, beta + k + 1);
-    if (k + 1 < kmax) k_scale<<<gm, tb, 0, st>>>(m, w, nrm, V + (size_t)(k + 1) * m);
-    if ((k + 1) % kCheck != 0 && k + 1 != kmax) continue;
+    k_norm_scale<<<gb, tb, 0, st>>>(nD, nb, part, w, nrm, beta + k + 1, k + 1 < kmax ? V + (size_t)(k + 1) * m : nullptr,
+                                    xfm);
+  };
+  // a block of kCheck iterations is ~100 small launches: captured once per
+  // context as a CUDA graph (its pointers and sizes are the context's) and
+  // replayed; the legacy stream cannot be captured, so it runs them eagerly
+  if (graphs && (graphs->m != m || graphs->kmax != kmax || graphs->scratch != scratch || graphs->A != A ||
+                 graphs->df != df || graphs->a1 != a1 || graphs->a2 != a2)) {
+    graphs->clear();
+    graphs->m = m, graphs->kmax = kmax, graphs->scratch = scratch, graphs->A = A, graphs->df = df;
+    graphs->a1 = a1, graphs->a2 = a2;
+  }
+  const bool use_graphs = graphs && st != nullptr;
+  int done = -1;
+  for (int k0 = 0; k0 < kmax && done < 0; k0 += kCheck) {
+    const int k1 = std::min(k0 + kCheck, kmax);
+    bool ran = false;
+    if (use_graphs && k1 - k0 == kCheck) {
+      const size_t b = (size_t)(k0 / kCheck);
+      if (graphs->blocks.size() <= b) graphs->blocks.resize(b + 1, nullptr);
+      if (!graphs->blocks[b]) {
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          for (int k = k0; k < k1; k++) iteration(k);
+          if (cudaStreamEndCapture(st, &g) == cudaSuccess && g) {
+            if (cudaGraphInstantiate(&graphs->blocks[b], g, 0) != cudaSuccess) graphs->blocks[b] = nullptr;
+            cudaGraphDestroy(g);
+          }
+        }
+        if (cudaGetLastError() != cudaSuccess) return BD_ERR_CUDA;
+      }
+      if (graphs->blocks[b]) {
+        if (cudaGraphLaunch(graphs->blocks[b], st) != cudaSuccess) return BD_ERR_CUDA;
+        ran = true;
+      }
+    }
+    if (!ran)
+      for (int k = k0; k < k1; k++) iteration(k);
+    int k = k1 - 1;
     if (cudaMemcpyAsync(hal.data(), alpha, (k + 1) * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(hbe.data(), beta, (k + 2) * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
