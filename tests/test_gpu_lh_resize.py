@@ -88,3 +88,45 @@ def test_bind_one_linker_histone_in_place(tmp_path, prec):
         assert a.step(rr, p) == b.step(rr, p)
         for k in ("r", "a", "r_t", "r_lh"):
             assert np.array_equal(a.get(k), b.get(k)), (s, k)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_bind_first_linker_histone(tmp_path, prec):
+    """From no linker histone bound (n_LH = 0) to one: the context still has
+    room for every core's, and continues as one created with the binding."""
+    import torch
+    from brownian_dynamics_cuda_gb300 import Context, Noise
+    from brownian_dynamics_cuda_gb300.fiber_gen import FiberSpec, make_fiber
+    full = make_fiber(FiberSpec(4, [30] * 4, lh=True, seed=4), str(tmp_path))
+    nlh = full.sizes["n_lh_n"] + full.sizes["n_lh_c"]
+    none = np.zeros_like(full.arrays["nc_lh_flag"])
+    part = dataclasses.replace(full, sizes=dict(full.sizes, n_LH=0),
+                               arrays=dict(full.arrays, nc_lh_flag=none, lh_rad=full.arrays["lh_rad"][:0]),
+                               state=dict(full.state, r_lh=full.state["r_lh"][:0]))
+    a = Context(part, precision=prec)
+    nz = Noise(9)
+    for s in range(2):
+        a.step(*nz.step(s, full.arrays["r_var"], a.m))
+    flags = none.copy()
+    flags[2] = 1
+    r_lh_new = full.state["r_lh"].reshape(-1, 3)[2 * nlh:3 * nlh].ravel()
+    rad_new = full.arrays["lh_rad"][2 * nlh:3 * nlh]
+    state = {k: a.get(k) for k in ("r", "a", "b", "c", "r_t")}
+    angles = {k: a.get(k) for k in ANGLES}
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    a.set_lh_flags(flags, r_lh_new, rad_new)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert a.n_LH == nlh and a.m == 3 * (full.sizes["n"] + full.sizes["n_tail"] + nlh)
+    fib1 = dataclasses.replace(full, sizes=dict(full.sizes, n_LH=nlh),
+                               arrays=dict(full.arrays, nc_lh_flag=flags, lh_rad=rad_new),
+                               state=dict(state, r_lh=r_lh_new))
+    b = Context(fib1, precision=prec, refresh=False, angles=angles)
+    for k in ("r", "a", "b", "c", "r_t", "r_lh", "beta", "length", "beta_lh"):
+        assert np.array_equal(a.get(k), b.get(k)), k
+    for s in range(2, 4):
+        rr, p = nz.step(s, full.arrays["r_var"], a.m)
+        assert a.step(rr, p) == b.step(rr, p)
+        for k in ("r", "a", "r_t", "r_lh"):
+            assert np.array_equal(a.get(k), b.get(k)), (s, k)
