@@ -374,7 +374,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
     addD(nt); addD(nL_cap); addD(3 * nlhc_cap * M.n_lh_g);
   }
   for (int q = 0; q < 3; q++) { addD(3 * n); addD(3 * n); addD(3 * nt); addD(3 * (size_t)nL_cap); addD(1); }
-  addD((size_t)nc * nc * 10); addD(ndna * nc * 7); addD(nlhc_cap * nc * 10); addD(ebuf_cap);
+  addD((size_t)nc * nc * 10); addD((size_t)kCCSplit * nc * nc * 10); addD(ndna * nc * 7); addD(nlhc_cap * nc * 10); addD(ebuf_cap);
   addD(3 * (size_t)nD_cap); addD(m_cap); addD(m_cap); addD(3 * n); addD(bdk::trmv_scratch_doubles(m_cap)); addD(1); addI(1);
   const int npos = n + nt + nL + (int)nlhc * M.n_lh_g;
   const int npos_cap = n + nt + nL_cap + (int)nlhc_cap * M.n_lh_g;
@@ -426,6 +426,7 @@ extern "C" int bd_create(const bd_model* m, const bd_state* s, const bd_options*
     fs[q]->lF = ar.take<double>(3 * (size_t)nL_cap); fs[q]->E = ar.take<double>(1);
   }
   c->S.cc = ar.take<double>((size_t)nc * nc * 10);
+  c->S.ccp = ar.take<double>((size_t)kCCSplit * nc * nc * 10);
   c->S.dc = ar.take<double>(ndna * nc * 7);
   c->S.gc = ar.take<double>(nlhc_cap * nc * 10);
   c->S.ebuf = ar.take<double>(ebuf_cap);

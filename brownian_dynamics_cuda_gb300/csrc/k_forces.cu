@@ -332,7 +332,9 @@ template <bool MX>
 __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X, double* slots) {
   extern __shared__ double sm[];
   int I = blockIdx.x, J = blockIdx.y;
-  double* out = slots + ((size_t)I * M.n_c + J) * 10;
+  // gridDim.z CTAs share the pair, each its own interleaved share of the
+  // charge pairs and its own slot (summed by k_cc_sum)
+  double* out = slots + (((size_t)blockIdx.z * M.n_c + I) * M.n_c + J) * 10;
   if (I >= J) return;
   int i = M.core_bead[I], j = M.core_bead[J];
   V3 ri = ld3(X.r + 3 * i), rj = ld3(X.r + 3 * j);
@@ -363,7 +365,7 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
                 biz = (float)bi.z, cix = (float)ci.x, ciy = (float)ci.y, ciz = (float)ci.z;
     const float ajx = (float)aj.x, ajy = (float)aj.y, ajz = (float)aj.z, bjx = (float)bj.x, bjy = (float)bj.y,
                 bjz = (float)bj.z, cjx = (float)cj.x, cjy = (float)cj.y, cjz = (float)cj.z;
-    for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
+    for (int p = blockIdx.z * blockDim.x + threadIdx.x; p < Nq * Nq; p += blockDim.x * gridDim.z) {
       int k = p / Nq, l = p - k * Nq;
       float zx = (float)(si_[3 * k] - sj_[3 * l]), zy = (float)(si_[3 * k + 1] - sj_[3 * l + 1]),
             zz = (float)(si_[3 * k + 2] - sj_[3 * l + 2]);
@@ -391,7 +393,7 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
       v[6] += (double)(fc * cpl1 - fb * cpl2); v[7] += (double)(fa * cpl2 - fc * cpl0); v[8] += (double)(fb * cpl0 - fa * cpl1);
     }
   } else {
-  for (int p = threadIdx.x; p < Nq * Nq; p += blockDim.x) {
+  for (int p = blockIdx.z * blockDim.x + threadIdx.x; p < Nq * Nq; p += blockDim.x * gridDim.z) {
       int k = p / Nq, l = p - k * Nq;
       V3 pk = ld3(si_ + 3 * k), pl = ld3(sj_ + 3 * l);
       V3 z{pk.x - pl.x, pk.y - pl.y, pk.z - pl.z};
@@ -429,6 +431,17 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
   bsum<10>(v, red);
   if (threadIdx.x == 0)
     for (int q = 0; q < 10; q++) out[q] = v[q];
+}
+
+// the FP64 core/core slots: the kCCSplit partials of each pair I < J, summed in order
+__global__ void k_cc_sum(int nc, const double* __restrict__ part, double* __restrict__ slots) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nc * nc * 10) return;
+  const int pr = e / 10, I = pr / nc, J = pr - I * nc;
+  if (I >= J) return;
+  double s = 0.0;
+  for (int z = 0; z < kCCSplit; z++) s += part[(size_t)z * nc * nc * 10 + e];
+  slots[e] = s;
 }
 
 // Core/core, mixed path: the same slot (force on I, body-frame torques on I
@@ -1724,7 +1737,9 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
       k_core_core_mx<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S, S.cc);
     } else {
       size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
-      k_core_coreX<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S.cc);
+      k_core_coreX<<<dim3(M.n_c, M.n_c, kCCSplit), kCCThreads, sm, st>>>(M, X, S.ccp);
+      k_cc_sum<<<cdiv(M.n_c * M.n_c * 10, 256), 256, 0, st>>>(M.n_c, S.ccp, S.cc);
+      L++;
     }
     L++;
   }
