@@ -94,3 +94,12 @@ def test_host_stream_log_modes():
             total += x.size
     assert 0 < diff < 0.01 * total
     assert np.array_equal(a.u32(1000), b.u32(1000))
+
+
+def test_log_mode_argument_checked():
+    from brownian_dynamics_cuda_gb300 import LOG_CR, LOG_LIBM, BDError, Noise
+    g = Noise(1)
+    g.set_log(LOG_CR)
+    g.set_log(LOG_LIBM)
+    with pytest.raises(BDError):
+        g.set_log(7)
