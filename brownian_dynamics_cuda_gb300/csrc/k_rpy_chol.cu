@@ -100,6 +100,10 @@ __global__ void __launch_bounds__(256) k_potrf_diag(double* A, int lda, int k0, 
     S[rr][c] = (rr >= c) ? A[(size_t)(k0 + c) * lda + k0 + rr] : 0.0;
   }
   __syncthreads();
+  // the pivot's reciprocal, formed once per column by thread 0 beside its
+  // square root, scales the column (one FP64 division per column instead of
+  // one per element on the column's critical path)
+  __shared__ double rpiv;
   for (int c = 0; c < kb; c++) {
     if (tid == 0) {
       double f = S[c][c];
@@ -107,11 +111,13 @@ __global__ void __launch_bounds__(256) k_potrf_diag(double* A, int lda, int k0, 
         f = -f;
         atomicAdd(negpiv, 1);
       }
-      S[c][c] = sqrt(f);
+      const double d = sqrt(f);
+      S[c][c] = d;
+      rpiv = 1.0 / d;
     }
     __syncthreads();
-    double piv = S[c][c];
-    for (int rr = c + 1 + tid; rr < kb; rr += blockDim.x) S[rr][c] = S[rr][c] / piv;
+    const double rp = rpiv;
+    for (int rr = c + 1 + tid; rr < kb; rr += blockDim.x) S[rr][c] = S[rr][c] * rp;
     __syncthreads();
     // rank-1 update of the remaining lower triangle
     int rem = kb - c - 1;
@@ -135,10 +141,13 @@ __global__ void __launch_bounds__(256) k_potrf_diag(double* A, int lda, int k0, 
 constexpr int kTrsmThreads = 128;
 __global__ void __launch_bounds__(kTrsmThreads) k_trsm_panel(double* A, int lda, int m, int k0, int kb) {
   __shared__ double Lkk[kNB][kNB + 1];
+  __shared__ double rdiag[kNB];  // 1 / L_cc: the row solves multiply instead of dividing
   for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
     int c = e / kb, rr = e - c * kb;
     Lkk[rr][c] = (rr >= c) ? A[(size_t)(k0 + c) * lda + k0 + rr] : 0.0;
   }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kb; c += blockDim.x) rdiag[c] = 1.0 / Lkk[c][c];
   __syncthreads();
   int r = k0 + kb + blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= m) return;
@@ -154,7 +163,7 @@ __global__ void __launch_bounds__(kTrsmThreads) k_trsm_panel(double* A, int lda,
 #pragma unroll
       for (int q = 0; q < kNB; q++)
         if (q < c) v = v - x[q] * Lkk[c][q];
-      x[c] = v / Lkk[c][c];
+      x[c] = v * rdiag[c];
     }
   }
 #pragma unroll
