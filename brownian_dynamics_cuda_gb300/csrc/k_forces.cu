@@ -325,10 +325,10 @@ __global__ void k_chain_bonded(DevModel M, DevState X, const double* __restrict_
 }
 
 // ------------------------------------------------------------ charge sets
-// Core/core (func.cpp:1489-1566): one CTA per core pair I < J.
+// Core/core (func.cpp:1489-1566), FP64 path: kCCSplit CTAs per core pair
+// I < J (mixed contexts: k_core_core_mx below, one CTA per pair).
 constexpr int kCCThreads = 256;
 
-template <bool MX>
 __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X, double* slots) {
   extern __shared__ double sm[];
   int I = blockIdx.x, J = blockIdx.y;
@@ -359,40 +359,7 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X
   const double* cq = M.core_q;
   const double ke = M.k_e, kap = M.debye, kex = M.k_ex, sg = M.sCC;
   double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if constexpr (MX) {
-    const float kapf = (float)kap, kexf = (float)kex, sgf = (float)sg;
-    const float aix = (float)ai.x, aiy = (float)ai.y, aiz = (float)ai.z, bix = (float)bi.x, biy = (float)bi.y,
-                biz = (float)bi.z, cix = (float)ci.x, ciy = (float)ci.y, ciz = (float)ci.z;
-    const float ajx = (float)aj.x, ajy = (float)aj.y, ajz = (float)aj.z, bjx = (float)bj.x, bjy = (float)bj.y,
-                bjz = (float)bj.z, cjx = (float)cj.x, cjy = (float)cj.y, cjz = (float)cj.z;
-    for (int p = blockIdx.z * blockDim.x + threadIdx.x; p < Nq * Nq; p += blockDim.x * gridDim.z) {
-      int k = p / Nq, l = p - k * Nq;
-      float zx = (float)(si_[3 * k] - sj_[3 * l]), zy = (float)(si_[3 * k + 1] - sj_[3 * l + 1]),
-            zz = (float)(si_[3 * k + 2] - sj_[3 * l + 2]);
-      float dd = sqrtf(zx * zx + zy * zy + zz * zz);
-      float mi = 1.f / dd;
-      zx *= mi; zy *= mi; zz *= mi;
-      float ex = expf(-kapf * dd);
-      float qkl = (float)(ke * cq[k] * cq[l]);
-      float g = qkl * ex * (kapf * dd + 1.f) / (dd * dd);
-      float e = qkl * ex / dd;
-      if (dd <= 8.f) {
-        float sr = sgf / dd, sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-        g += kexf * (12.f * sr12 - 6.f * sr6) / dd;
-        e += kexf * (sr12 - sr6);
-      }
-      v[9] += (double)e;
-      v[0] += (double)(g * zx); v[1] += (double)(g * zy); v[2] += (double)(g * zz);
-      const float cpk0 = (float)cp[3 * k], cpk1 = (float)cp[3 * k + 1], cpk2 = (float)cp[3 * k + 2];
-      const float cpl0 = (float)cp[3 * l], cpl1 = (float)cp[3 * l + 1], cpl2 = (float)cp[3 * l + 2];
-      float fa = g * (aix * zx + aiy * zy + aiz * zz), fb = g * (bix * zx + biy * zy + biz * zz),
-            fc = g * (cix * zx + ciy * zy + ciz * zz);
-      v[3] += (double)(fc * cpk1 - fb * cpk2); v[4] += (double)(fa * cpk2 - fc * cpk0); v[5] += (double)(fb * cpk0 - fa * cpk1);
-      fa = -g * (ajx * zx + ajy * zy + ajz * zz); fb = -g * (bjx * zx + bjy * zy + bjz * zz);
-      fc = -g * (cjx * zx + cjy * zy + cjz * zz);
-      v[6] += (double)(fc * cpl1 - fb * cpl2); v[7] += (double)(fa * cpl2 - fc * cpl0); v[8] += (double)(fb * cpl0 - fa * cpl1);
-    }
-  } else {
+  {
   for (int p = blockIdx.z * blockDim.x + threadIdx.x; p < Nq * Nq; p += blockDim.x * gridDim.z) {
       int k = p / Nq, l = p - k * Nq;
       V3 pk = ld3(si_ + 3 * k), pl = ld3(sj_ + 3 * l);
@@ -1716,7 +1683,6 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   double* Tm = Fm + 3 * M.n;                          // [3n]
   int L = 0;
 #define KSEL(name) (mixed ? name<true> : name<false>)
-  auto k_core_coreX = KSEL(k_core_core);
   auto k_dna_coreX = KSEL(k_dna_core);
   auto k_ghead_coreX = KSEL(k_ghead_core);
   auto k_tail_gatherX = KSEL(k_tail_gather);
@@ -1737,7 +1703,7 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
       k_core_core_mx<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S, S.cc);
     } else {
       size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
-      k_core_coreX<<<dim3(M.n_c, M.n_c, kCCSplit), kCCThreads, sm, st>>>(M, X, S.ccp);
+      k_core_core<<<dim3(M.n_c, M.n_c, kCCSplit), kCCThreads, sm, st>>>(M, X, S.ccp);
       k_cc_sum<<<cdiv(M.n_c * M.n_c * 10, 256), 256, 0, st>>>(M.n_c, S.ccp, S.cc);
       L++;
     }
