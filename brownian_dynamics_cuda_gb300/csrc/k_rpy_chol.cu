@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(kRdRows) k_trmv_part(int m, const double* __re
   double s = 0.0;
   if (i < m) {
     int kend = min(k1, i + 1);
+#pragma unroll 8
     for (int k = k0; k < kend; k++) s = s + (s2dt * A[(size_t)k * lda + i]) * p[k];
   }
   if (i < m) part[(size_t)kc * m + i] = s;
@@ -265,6 +266,9 @@ __global__ void __launch_bounds__(kRdRows) k_trmv_part_df(int m, const float2* _
   if (i >= m) return;
   float sh = 0.f, sc = 0.f;
   int kend = min(k1, i + 1);
+  // unrolled so that eight loads of the factor are in flight per thread (the
+  // sum's order is unchanged)
+#pragma unroll 8
   for (int k = k0; k < kend; k++) {
     const float2 a = A[(size_t)k * lda + i];
     const float2 q = ps[k - k0];
