@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(kRows) k_na_part(int m, const double* __restri
   if (i >= m) return;
   double s = 0.0;
   int kend = min(k1, i + 1);
+#pragma unroll 8  // eight loads of the factor in flight per thread; the sum's order is unchanged
   for (int k = k0; k < kend; k++) s = s + (s2dt * L[(size_t)k * lda + i]) * p[k];
   part[(size_t)kc * m + i] = s;
 }
