@@ -10,7 +10,7 @@
 
 #include "../../include/bd_capi.h"
 
-// FP64 core/core pairs: each pair's charge pairs over this many CTAs
+// core/core pairs: each pair's charge pairs over this many CTAs (both paths)
 constexpr int kCCSplit = 4;
 
 namespace bdh {
@@ -108,7 +108,7 @@ struct DevForces {
 // interacting object pair, reduced per bead in a fixed order).
 struct DevScratch {
   double* cc;    // [n_c * n_c * 10]  core-core: F(3) T_i(3) T_j(3) E
-  double* ccp;   // [kCCSplit * n_c * n_c * 10] FP64 core-core partials (a pair over kCCSplit CTAs)
+  double* ccp;   // [kCCSplit * n_c * n_c * 10] core-core partials (a pair over kCCSplit CTAs)
   double* dc;    // [n_dna * n_c * 7] DNA-core: F_on_dna(3) T_core(3) E
   double* gc;    // [n_lhcore * n_c * 10] G-head(core I) - charges(core L): F_I(3) T_I(3) T_L(3) E
   double* ebuf;  // [nE] per-kernel energy partials

@@ -326,7 +326,7 @@ __global__ void k_chain_bonded(DevModel M, DevState X, const double* __restrict_
 
 // ------------------------------------------------------------ charge sets
 // Core/core (func.cpp:1489-1566), FP64 path: kCCSplit CTAs per core pair
-// I < J (mixed contexts: k_core_core_mx below, one CTA per pair).
+// I < J (mixed contexts: k_core_core_mx below, split the same way).
 constexpr int kCCThreads = 256;
 
 __global__ void __launch_bounds__(kCCThreads) k_core_core(DevModel M, DevState X, double* slots) {
@@ -424,7 +424,9 @@ constexpr int kCCFlush = 32;
 __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevState X, DevScratch S, double* slots) {
   extern __shared__ double sm[];
   const int I = blockIdx.x, J = blockIdx.y;
-  double* out = slots + ((size_t)I * M.n_c + J) * 10;
+  // gridDim.z CTAs share the pair (interleaved sites k of core I), each
+  // with its own slot, summed in order by k_cc_sum
+  double* out = slots + (((size_t)blockIdx.z * M.n_c + I) * M.n_c + J) * 10;
   if (I >= J) return;
   const int i = M.core_bead[I], j = M.core_bead[J];
   // far-pair test and the centre offset in FP32, from the double-float mirror
@@ -475,7 +477,7 @@ __global__ void __launch_bounds__(kCCThreads) k_core_core_mx(DevModel M, DevStat
   // warp w takes sites k = w, w + nw, ... of core I against all sites l of
   // core J (lanes); the force and torque on I are summed per k first
   const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int k = threadIdx.x >> 5; k < Nq; k += nw) {
+  for (int k = (threadIdx.x >> 5) + nw * blockIdx.z; k < Nq; k += nw * gridDim.z) {
     const float sx = sIx[k], sy = sIy[k], sz = sIz[k], qk = qI[k];
     float fkx = 0.f, fky = 0.f, fkz = 0.f;
     for (int l = lane; l < Nq; l += 32) {
@@ -1700,7 +1702,9 @@ int forces(const DevModel& M, DevState& X, DevForces& out, DevScratch& S, int mi
   if (M.n_c > 1) {
     if (mixed) {
       size_t sm = (size_t)((14 * M.Nq + 1) / 2 + 32 * 10) * sizeof(double);
-      k_core_core_mx<<<dim3(M.n_c, M.n_c), kCCThreads, sm, st>>>(M, X, S, S.cc);
+      k_core_core_mx<<<dim3(M.n_c, M.n_c, kCCSplit), kCCThreads, sm, st>>>(M, X, S, S.ccp);
+      k_cc_sum<<<cdiv(M.n_c * M.n_c * 10, 256), 256, 0, st>>>(M.n_c, S.ccp, S.cc);
+      L++;
     } else {
       size_t sm = (size_t)(6 * M.Nq + 32 * 10) * sizeof(double);
       k_core_core<<<dim3(M.n_c, M.n_c, kCCSplit), kCCThreads, sm, st>>>(M, X, S.ccp);
