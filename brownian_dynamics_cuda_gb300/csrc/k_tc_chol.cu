@@ -392,7 +392,7 @@ __device__ __forceinline__ void dpanel_body(float4* sm4, float2* A, float* Ldg, 
     // the products read the stage memory: complete before S overwrites it
     pre_ok = sm100::mbar_wait(&pbar->done, 0, kWaitLimit);
     sm100::tc_fence_after();
-    pre_ok = __syncthreads_and(pre_ok);  // one verdict for the CTA (it gates a named barrier below)
+    pre_ok = __syncthreads_and(pre_ok);  // one decision for the whole CTA (it gates a named barrier below)
     if (!pre_ok && tid == 0) atomicExch(err, 7);
   }
   // Rows [0, nr) of a 128-row part of the panel (columns k0 .. k0 + kb) into
