@@ -412,7 +412,8 @@ int bd_restart_from_context(bd_ctx* ctx, bd_restart* rs);
  * size of D): the context is resized on the device for the new flags [n_c],
  * with r_lh [3 n_LH] the new LH bead positions (bound cores in order, as
  * main.cpp:418-447 builds them) and lh_rad [n_LH] their radii (NULL: the
- * first linker histone's radii repeated).  Nothing is reallocated and no
+ * radii of the first linker histone the context holds, repeated; 0.5 nm for
+ * every bead when it holds none).  Nothing is reallocated and no
  * state leaves the device: bd_create sizes every binding-dependent buffer
  * (D, its factor, the LH arrays, the mirrors) for every core bound, and the
  * call uploads the new LH tables and beads, sets the logical sizes, and makes
